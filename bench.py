@@ -1,0 +1,378 @@
+#!/usr/bin/env python
+"""Benchmark of the FDTD time-stepping path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--form fp32|fp64]
+                    [--workload NAME] [--impl reference]
+
+A "step" is one FDTD time step (H half-step, E half-step, plasma current J,
+CPML, TF/SF, running DFT) over the whole grid.  ``value`` is whole-job
+Gcell-updates/s = cells * K * N / (max over ranks of the device time of the K
+timed steps), measured with CUDA events on the simulation's stream between a
+barrier + synchronize on both sides.  The state of every workload is far larger
+than the 129 MB L2, so no flush is needed between steps.
+
+``e2e`` is the same metric through the public API from host buffers: problem
+creation from host arrays, device allocation and upload, K steps, and the
+device-to-host read of the near-to-far-field sums, timed by the host clock.
+
+``--impl reference`` times the reference's CPU implementation of the path on
+this host's cores (the reference binary built from its sources when present,
+else the C restatement of it in oracle/) on a bounded slab of the same
+workload, and prints the same JSON line with ``"impl": "reference"``.
+
+N > 1 runs independent replicas, one per GPU (the path has no data exchange
+between jobs); rank 0 prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import resource
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from meteorscattering_gb300 import rundir as rd  # noqa: E402
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+# --------------------------------------------------------------------------
+# Workloads
+
+
+def workload(name: str, steps_total: int):
+    """(RunParams, wp2 [Nx][Ny] C-order, nu2, B0, description)."""
+    if name == "trail768":
+        # Large single trail at 768 x 768 x 1536 cells, dx = 0.2 m (50 MHz radar,
+        # gridfactor 30), overdense Gaussian trail r0 = 0.8 m along z,
+        # nu = 3e4 1/s, B0 = 5e-5 T dipped 60 degrees, Lee-Kalluri current.
+        N = (768, 768, 1536)
+        f0, gf = 50e6, 30.0
+        desc = ("768x768x1536 magnetized trail, dx=0.2 m, Lee-Kalluri J, 10-cell CPML, "
+                "plane wave along +x (Ez), z-uniform Gaussian trail n0=1e15 r0=0.8 m, "
+                "nu=3e4, B0=5e-5 T at 60 deg dip")
+        n0, r0, nu = 1e15, 0.8, 3e4
+    elif name == "cfg1":
+        N = (96, 96, 192)
+        f0, gf = 50e6, 24.0
+        desc = ("96x96x192 magnetized trail, dx=0.25 m, Lee-Kalluri J, n0=1e14 r0=1 m, "
+                "nu=5e4, B0=5e-5 T at 60 deg dip")
+        n0, r0, nu = 1e14, 1.0, 5e4
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    Nx, Ny, Nz = N
+    dx = rd.C0 / f0 / gf
+    p = rd.RunParams(Nx=Nx, Ny=Ny, Nz=Nz, tsteps=steps_total, dt=rd.stable_dt(dx), f0=f0,
+                     fsig=20.0, gridfactor=gf, numfiles=1, savefields=0, probex=[Nx // 2],
+                     probey=[Ny // 2], probez=[Nz // 2], fntf=[f0], metsize=(1e200, 1e200),
+                     doB0=1)
+    wp = rd.gaussian_trail_wp(p, n0, r0)
+    nu2 = np.full((Nx, Ny), nu)
+    B0 = (5e-5 * math.cos(math.pi / 3), 0.0, -5e-5 * math.sin(math.pi / 3))
+    wp2 = np.asarray(wp).reshape(-1, order="F").reshape(Nx, Ny)
+    return p, wp2, nu2, B0, desc, wp
+
+
+def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams) -> float:
+    """Compulsory DRAM bytes of one launch of `kernel` (per cell-update figure
+    x cells, plus the CPML psi slabs each launch reads and writes)."""
+    cells = p.Nx * p.Ny * p.Nz
+    L = 10
+    psi = 2 * (2 * L * p.Ny * p.Nz + p.Nx * 2 * L * p.Nz + p.Nx * p.Ny * 2 * L)  # one half-step
+    if form == "fp64":
+        if kernel == "k_plain_h":   # E r(3), H r/w(6), J r/w(6) ; psi r/w
+            return cells * 15 * 8 + psi * 16
+        if kernel == "k_plain_e":   # H r(3), E r/w(6), J r(3) ; psi r/w
+            return cells * 12 * 8 + psi * 16
+    else:
+        # FP32 single pass: E, H, J read and written (18 x 4 B) + per-cell
+        # plasma weight (4 B); both psi halves read and written.
+        return cells * 19 * 4 + 2 * psi * 8
+    raise KeyError(kernel)
+
+
+# --------------------------------------------------------------------------
+# Clock sampling (nvidia-smi during the timed region)
+
+
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        if shutil.which("nvidia-smi") is None:
+            return
+        self.proc = subprocess.Popen(
+            ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+             "--format=csv,noheader,nounits", "-lms", "200"],
+            stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline: the reference implementation on the host cores
+
+
+def _unlimited_stack():
+    resource.setrlimit(resource.RLIMIT_STACK, (resource.RLIM_INFINITY, resource.RLIM_INFINITY))
+
+
+def cpu_baseline(name: str, steps: int, budget_s: float = 20.0):
+    """Time the reference CPU path on a slab of the workload (full Nx x Ny,
+    reduced Nz) for a few steps; returns a cpu_baseline dict."""
+    p, wp2, nu2, B0, desc, wp = workload(name, 4)
+    threads = os.cpu_count() or 1
+    nz = min(p.Nz, max(24, int(4e7 // (p.Nx * p.Ny))))
+    ref_exe = os.path.join(ROOT, "oracle", "_ref", "meteor_fork")
+    use_ref = os.path.exists(ref_exe) and os.access(ref_exe, os.X_OK)
+    oracle_so = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
+    if not use_ref and not os.path.exists(oracle_so):
+        from meteorscattering_gb300 import build as B
+        B.build_oracle(with_reference=False)
+    import dataclasses
+    d = tempfile.mkdtemp(prefix="mfdtd_cpu_")
+    try:
+        def run(nsteps):
+            q = dataclasses.replace(p, Nz=nz, tsteps=nsteps, numfiles=1, savefields=0,
+                                    probez=[nz // 2])
+            shutil.rmtree(d, ignore_errors=True)
+            rd.write_rundir(d, q, wp, np.full((p.Nx, p.Ny), nu2.flat[0]), B0)
+            env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+            if use_ref:
+                t0 = time.perf_counter()
+                r = subprocess.run([ref_exe], cwd=d, preexec_fn=_unlimited_stack, env=env,
+                                   capture_output=True, text=True)
+                if r.returncode != 0:
+                    raise RuntimeError(r.stderr)
+                return time.perf_counter() - t0
+            lib = ctypes.CDLL(oracle_so)
+            lib.oracle_run_dir.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+            secs = ctypes.c_double()
+            rc = lib.oracle_run_dir(os.fsencode(d), -1, threads, 1, ctypes.byref(secs))
+            if rc != 0:
+                raise RuntimeError(f"oracle error {rc}")
+            return secs.value
+        # A one-step run sizes the sample; the reference binary's set-up time is
+        # removed by differencing two runs (the port reports its loop time).
+        t1 = run(1)
+        n = max(2, min(max(steps, 2), int(budget_s / max(t1, 1e-3))))
+        t_run = run(n + 1) - t1 if use_ref else run(n)
+        cells = p.Nx * p.Ny * nz
+        return {"value": cells * n / t_run / 1e9, "unit": "Gcell-updates/s", "cores": threads,
+                "kind": "reference" if use_ref else "port",
+                "sample": f"{p.Nx}x{p.Ny}x{nz} slab of the workload, {n} steps, "
+                          f"{'reference binary (source/meteor-fork.cpp)' if use_ref else 'oracle/fdtd_oracle.c'} "
+                          f"with {threads} OpenMP threads; time-loop seconds"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+
+
+# --------------------------------------------------------------------------
+
+
+def dist_setup(n_gpus: int):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def load_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--workload", default="trail768")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    K, W = args.steps, max(args.warmup, 0)
+
+    rank, world, local, pg = dist_setup(args.gpus)
+    p, wp2, nu2, B0, desc, _ = workload(args.workload, K + W + 1)
+    cells = p.Nx * p.Ny * p.Nz
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(args.workload, K + W)
+        line = {"impl": "reference", "metric": "Gcell-updates/s", "value": cb["value"],
+                "unit": "Gcell-updates/s", "n_gpus": args.gpus, "steps": K, "warmup": W,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic",
+                "config": {"workload": desc, "grid": [p.Nx, p.Ny, p.Nz]},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "Gcell-updates/s",
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    from meteorscattering_gb300 import build as B
+    B.build()
+    from meteorscattering_gb300 import engine as E
+
+    form = E.FORM_FP32_FUSED if args.form == "fp32" else E.FORM_FP64_PLAIN
+    device = local
+    pb = E.Problem.from_params(p, wp2, nu2, B0)
+    sim = E.Simulation(pb, form=form, device=device, profile=True)
+    if W:
+        sim.advance(W)
+    sim.sync()
+    clk = ClockSampler(device)
+    clk.start()
+    barrier(pg)
+    t0 = time.perf_counter()
+    sim.advance(K)  # events around the K steps on the simulation's stream
+    sim.sync()
+    wall = time.perf_counter() - t0
+    barrier(pg)
+    clocks = clk.stop()
+    ms_step, launches = sim.last_timing()
+    kstats = sim.kernel_stats()
+    sim.close()
+    ms_step = max_over_ranks(pg, ms_step)
+    value = cells * world / (ms_step * 1e-3) / 1e9
+
+    # dominant kernel roofline
+    dom = max(kstats, key=lambda r: r[1] * r[2]) if kstats else None
+    peak, peak_kind = load_peaks()
+    roof = None
+    if dom:
+        alg = algorithmic_bytes(args.form, dom[0], p)
+        ach = alg / (dom[1] * 1e-3) / 1e9
+        roof = {"kernel": dom[0], "bound": "hbm", "achieved": ach, "peak": peak,
+                "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
+                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom[1],
+                "traffic": None,
+                "kernel_times_ms": {n: m for n, m, c in kstats}}
+
+    # end to end through the public API from host buffers
+    e2e = None
+    if not args.no_e2e:
+        barrier(pg)
+        t0 = time.perf_counter()
+        pb2 = E.Problem.from_params(p, wp2, nu2, B0)
+        s2 = E.Simulation(pb2, form=form, device=device)
+        s2.advance(K)
+        ntf = s2.read_ntf()
+        s2.close()
+        pb2.close()
+        t_e2e = max_over_ranks(pg, time.perf_counter() - t0)
+        h2d = (wp2.nbytes + nu2.nbytes) / K
+        e2e = {"value": cells * world * K / t_e2e / 1e9, "unit": "Gcell-updates/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": ntf.nbytes / K,
+               "wall_s": t_e2e,
+               "includes": "problem set-up from host arrays, device allocation + upload, "
+                           "K steps, D2H of the near-to-far-field sums"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_baseline(args.workload, K)
+        except Exception as ex:  # report, never fake
+            cpu = {"value": None, "error": str(ex)[:200]}
+
+    if rank == 0:
+        line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell-updates/s",
+                "n_gpus": world, "steps": K, "warmup": W, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if args.form == "fp32" else "f64", "data": "synthetic",
+                "config": {"workload": desc, "grid": [p.Nx, p.Ny, p.Nz],
+                           "form": "fp32_fused" if args.form == "fp32" else "fp64_plain",
+                           "parallelism": f"replicas x{world}",
+                           "l2": "state larger than L2 (no flush needed)"},
+                "hbm_gbs": (algorithmic_bytes(args.form, dom[0], p) / (dom[1] * 1e-3) / 1e9)
+                if dom else None,
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+                "gpu_launches": launches, "host_wall_s": wall}
+        print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

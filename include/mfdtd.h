@@ -1,0 +1,154 @@
+/*
+ * mfdtd.h -- C ABI of the GB300 meteor-scattering FDTD engine.
+ *
+ * The reference solver (source/meteor-2.1.cpp, and its magnetized variant
+ * source/meteor-fork.cpp) has no library interface: its boundary is a process
+ * started in a run directory (setup/writepbsfile.m:15, qsub -d in
+ * setup/meteorrun.m:169) that reads inputs.dat, B0.dat, wp.dat, nu.dat and
+ * writes log.txt, output_{E,H,J}.dat, output_NTF.dat and Probe.dat.  The entry
+ * points below replace that process: mfdtd_run_rundir() is the whole program,
+ * the finer-grained calls expose its stages (input parse, device state, time
+ * stepping, output write-out) to callers that keep data in memory.
+ *
+ * Conventions: every call returns an mfdtd_status (0 = success); no C++
+ * exception crosses this boundary; the text of the last error on the calling
+ * thread is available from mfdtd_last_error().  Handles are independent: calls
+ * on different handles may run concurrently from different threads; calls on
+ * one handle must be serialised by the caller.  All arrays are plain host
+ * pointers in C order unless a comment says otherwise.
+ */
+#ifndef MFDTD_H
+#define MFDTD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MFDTD_OK = 0,
+    MFDTD_EINVAL = -1,   /* invalid argument or input-file content            */
+    MFDTD_EIO = -2,      /* missing or short input file, unwritable output     */
+    MFDTD_ECUDA = -3,    /* CUDA runtime error                                 */
+    MFDTD_ENOMEM = -4,   /* device or host allocation failed / over the limit  */
+    MFDTD_ETIMEOUT = -5, /* a bounded wait ran out                             */
+    MFDTD_ENUMERIC = -6, /* NaN/Inf detected by the field guard                */
+    MFDTD_ESTATE = -7    /* call not valid in the handle's current state        */
+} mfdtd_status;
+
+/* Arithmetic form of the time stepping. */
+typedef enum {
+    MFDTD_FORM_FP64_PLAIN = 0, /* FP64, reference operation order, no FMA
+                                  contraction: the drop-in form              */
+    MFDTD_FORM_FP32_FUSED = 1  /* FP32 fields/currents/psi, FP64 DFT sums    */
+} mfdtd_form;
+
+/* Contents of inputs.dat in file order (source/meteor-2.1.cpp:84-112, plus
+ * doB0 read by source/meteor-fork.cpp:115).  Pointers are borrowed for the
+ * duration of the call that receives the struct. */
+typedef struct {
+    int32_t dopml, savefields;
+    double f0, fsig;
+    int32_t sourcetype, sourcepol;
+    double gridfactor, dt;
+    int32_t tsteps, Nx, Ny, Nz;
+    double metsize[2];
+    double wpmax, numax;
+    double metloc[3];
+    double metangle;
+    int32_t mettype, numfiles, nprobes;
+    const int32_t *probex, *probey, *probez; /* [nprobes] */
+    int32_t nntf;
+    const double *fntf;                      /* [nntf] Hz */
+    int32_t doplate;
+    double platesize;
+    int32_t doB0;                            /* 0: Young DI J, 1: Lee-Kalluri */
+} mfdtd_params;
+
+/* Run options.  A zeroed struct (or NULL) selects the defaults shown. */
+typedef struct {
+    int32_t form;          /* mfdtd_form; default FP64_PLAIN                     */
+    int32_t device;        /* CUDA device ordinal; default 0                     */
+    int32_t guard_period;  /* >0: check max|E| for NaN/Inf every N steps and
+                              stop with MFDTD_ENUMERIC; default 0 (off)          */
+    int32_t quiet;         /* nonzero: no stdout lines                            */
+    double timeout_s;      /* >0: bound on each host wait for the device          */
+    int32_t profile;       /* nonzero: time every kernel class with CUDA events
+                              on the simulation's stream (mfdtd_sim_kernel_stats) */
+} mfdtd_run_opts;
+
+typedef struct mfdtd_problem mfdtd_problem; /* parsed inputs + derived tables */
+typedef struct mfdtd_sim mfdtd_sim;         /* device-resident state          */
+
+/* ---- whole-program entry point ------------------------------------------
+ * Replaces running the `meteor` executable with `dir` as the working
+ * directory (source/meteor-2.1.cpp:42-1649; invocation setup/writepbsfile.m:15).
+ * Reads the four input files, runs every step on the GPU, and writes the same
+ * output files byte for byte (log.txt differs only in timing/memory lines).
+ * Like the reference, output_{E,H,J}.dat are appended to; removing stale ones
+ * is the job script's task (setup/writepbsfile.m:10-13). */
+int mfdtd_run_rundir(const char *dir, const mfdtd_run_opts *opts);
+
+/* ---- problem (host) -------------------------------------------------------
+ * From a run directory: replaces the input parse of
+ * source/meteor-2.1.cpp:51-114 and source/meteor-fork.cpp:115,219-224,
+ * source/meteor-2.1.cpp:301-315.  wp.dat/nu.dat keep their on-disk order:
+ * C [Nx][Ny] as the reference reads them. */
+int mfdtd_problem_from_rundir(const char *dir, mfdtd_problem **out);
+/* From memory: same content.  wp2/nu2 are [Nx][Ny] C-order (the byte order of
+ * wp.dat/nu.dat), B0 = {Bx, By, Bz} in tesla. */
+int mfdtd_problem_create(const mfdtd_params *p, const double *wp2, const double *nu2,
+                         const double B0[3], mfdtd_problem **out);
+void mfdtd_problem_destroy(mfdtd_problem *pb);
+/* Grid and run sizes: out[0..5] = Nx, Ny, Nz, tsteps, nntf, nprobes. */
+int mfdtd_problem_dims(const mfdtd_problem *pb, int64_t out[6]);
+/* Device bytes a simulation of this problem in `form` will hold. */
+int mfdtd_problem_footprint(const mfdtd_problem *pb, int32_t form, int64_t *bytes);
+
+/* ---- simulation (device) -------------------------------------------------- */
+int mfdtd_sim_create(const mfdtd_problem *pb, const mfdtd_run_opts *opts, mfdtd_sim **out);
+void mfdtd_sim_destroy(mfdtd_sim *s);
+/* Advance `nsteps` time steps (source/meteor-2.1.cpp:652-1574 per step).
+ * Record-step side effects (max|Ex| log line, slice records) are kept in the
+ * handle when `collect_records` is nonzero. Asynchronous unless a record step
+ * or guard check falls in the range. */
+int mfdtd_sim_advance(mfdtd_sim *s, int32_t nsteps, int32_t collect_records);
+/* Wait for queued work; returns MFDTD_ETIMEOUT if opts.timeout_s elapses. */
+int mfdtd_sim_sync(mfdtd_sim *s);
+/* Steps completed so far. */
+int mfdtd_sim_step_index(const mfdtd_sim *s, int32_t *t);
+/* Near-to-far-field sums in the layout of output_NTF.dat after the two ints
+ * and fntf (source/meteor-2.1.cpp:1588-1620): Eydft[2n], Ezdft[2n], then 24
+ * face arrays.  `out` must hold mfdtd_sim_ntf_size() doubles. */
+int64_t mfdtd_sim_ntf_size(const mfdtd_sim *s);
+int mfdtd_sim_read_ntf(mfdtd_sim *s, double *out, int64_t n);
+/* Probe series [6][tsteps][nprobes] (Ex,Ey,Ez,Hx,Hy,Hz; Probe.dat order). */
+int mfdtd_sim_read_probes(mfdtd_sim *s, double *out, int64_t n);
+/* One field component as [Nx][Ny][Nz] doubles: comp 0..8 = Ex,Ey,Ez,Hx,Hy,Hz,Jx,Jy,Jz. */
+int mfdtd_sim_read_field(mfdtd_sim *s, int32_t comp, double *out, int64_t n);
+/* Write output_{E,H,J}.dat (collected records), output_NTF.dat, Probe.dat
+ * and the log.txt record lines into `dir`. */
+int mfdtd_sim_write_outputs(mfdtd_sim *s, const char *dir);
+/* Mean device time per step of the last mfdtd_sim_advance (CUDA events on the
+ * simulation's stream), and the number of kernels it launched. */
+int mfdtd_sim_last_timing(const mfdtd_sim *s, double *ms_per_step, int64_t *launches);
+
+/* Per-kernel-class device time of the last mfdtd_sim_advance when the
+ * simulation was created with opts.profile set: for class `which` (0, 1, ...)
+ * its name, mean duration of one launch in ms, and launch count.  Returns
+ * MFDTD_EINVAL when `which` is past the last class. */
+int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t name_len,
+                           double *avg_ms, int64_t *launches);
+
+/* ---- errors ---------------------------------------------------------------- */
+/* Copy the last error message of the calling thread into buf (NUL-terminated). */
+int mfdtd_last_error(char *buf, size_t n);
+/* Library version string. */
+const char *mfdtd_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFDTD_H */

@@ -1,0 +1,661 @@
+// sim.cpp -- device-resident simulation, output writers and the C ABI.
+#include <cuda_runtime.h>
+#include <sys/resource.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "common.hpp"
+#include "fp32.hpp"
+
+using mfdtd::Error;
+using mfdtd::Problem;
+
+struct mfdtd_problem {
+    Problem P;
+};
+
+namespace mfdtd {
+namespace {
+
+thread_local std::string g_last_error;
+
+void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess)
+        throw Error(MFDTD_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+double wall_s() {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+// One record step's output (source/meteor-2.1.cpp:1523-1568).
+struct Record {
+    int t = 0;
+    double emax = 0;
+    std::vector<double> E, H;  // slices + incident arrays, file layout
+};
+
+// Appends records to the run directory like the reference does.
+struct FileSink {
+    std::string dir;
+    void append(const std::string &name, const void *p, size_t bytes) {
+        std::string path = dir + "/" + name;
+        FILE *f = std::fopen(path.c_str(), "ab");
+        if (!f) throw Error(MFDTD_EIO, "cannot append to " + path);
+        if (bytes && std::fwrite(p, 1, bytes, f) != bytes) {
+            std::fclose(f);
+            throw Error(MFDTD_EIO, "short write to " + path);
+        }
+        std::fclose(f);
+    }
+    void log(const std::string &line) {
+        std::string path = dir + "/log.txt";
+        FILE *f = std::fopen(path.c_str(), "a");
+        if (!f) throw Error(MFDTD_EIO, "cannot append to " + path);
+        std::fputs(line.c_str(), f);
+        std::fclose(f);
+    }
+};
+
+std::string fmt_g(double v) {
+    char b[64];
+    std::snprintf(b, sizeof b, "%g", v);
+    return b;
+}
+
+}  // namespace
+}  // namespace mfdtd
+
+struct mfdtd_sim {
+    Problem P;
+    mfdtd_run_opts opts{};
+    int form = MFDTD_FORM_FP64_PLAIN;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<void *> allocs;
+    int64_t device_bytes = 0;
+    mfdtd::PlainArgs pa{};
+    std::unique_ptr<mfdtd::Fp32Sim> f32;
+    int t = 0;
+    bool flushed = false;
+    std::vector<mfdtd::Record> records;
+    mfdtd::FileSink *sink = nullptr;
+    double loop_start = 0;
+    double last_ms_per_step = 0;
+    int64_t last_launches = 0;
+    // opts.profile: per-kernel-class totals of the last advance
+    std::vector<std::string> kname;
+    std::vector<double> ktotal_ms;
+    std::vector<int64_t> kcount;
+    std::vector<cudaEvent_t> kev;  // event pool, (classes+1) per profiled step
+    size_t slice_len = 0;  // doubles in one slice block (3 planes x 2 comps)
+
+    template <class T> T *dalloc(size_t n) {
+        void *p = nullptr;
+        size_t bytes = std::max<size_t>(n, 1) * sizeof(T);
+        mfdtd::ck(cudaMalloc(&p, bytes), "cudaMalloc");
+        allocs.push_back(p);
+        device_bytes += (int64_t)bytes;
+        mfdtd::ck(cudaMemsetAsync(p, 0, bytes, stream), "cudaMemset");
+        return (T *)p;
+    }
+    template <class T> T *upload(const std::vector<T> &v) {
+        T *d = dalloc<T>(v.size());
+        if (!v.empty())
+            mfdtd::ck(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, stream),
+                      "cudaMemcpy H2D");
+        return d;
+    }
+
+    void init(const Problem &pb, const mfdtd_run_opts *o) {
+        P = pb;
+        if (o) opts = *o;
+        form = opts.form;
+        mfdtd::ck(cudaSetDevice(opts.device), "cudaSetDevice");
+        mfdtd::ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        mfdtd::ck(cudaEventCreate(&ev0), "cudaEventCreate");
+        mfdtd::ck(cudaEventCreate(&ev1), "cudaEventCreate");
+        slice_len = 2 * ((size_t)P.Nx * P.Ny + (size_t)P.Nx * P.Nz + (size_t)P.Ny * P.Nz);
+        if (form == MFDTD_FORM_FP64_PLAIN) init_plain();
+        else if (form == MFDTD_FORM_FP32_FUSED) {
+            f32.reset(new mfdtd::Fp32Sim());
+            f32->init(P, stream);
+            device_bytes = f32->device_bytes();
+        } else throw Error(MFDTD_EINVAL, "unknown form");
+        mfdtd::ck(cudaStreamSynchronize(stream), "set-up");
+    }
+
+    void init_plain() {
+        const size_t NC = P.cells();
+        mfdtd::PlainArgs &a = pa;
+        std::memset(&a, 0, sizeof a);
+        a.Nx = P.Nx; a.Ny = P.Ny; a.Nz = P.Nz; a.L = P.L;
+        a.xshift = P.xshift; a.yshift = P.yshift; a.zshift = P.zshift;
+        a.bx1 = P.bx1; a.bx2 = P.bx2; a.by1 = P.by1; a.by2 = P.by2; a.bz1 = P.bz1; a.bz2 = P.bz2;
+        a.ntfb = P.ntfb; a.nntf = P.nntf(); a.ssx = P.ssx; a.ssy = P.ssy; a.ssz = P.ssz;
+        a.dopml = P.dopml; a.doplate = P.doplate; a.doB0 = P.doB0; a.lk_mode = P.lk_mode;
+        a.plate_lo = P.plate_lo; a.plate_up = P.plate_up; a.nprobes = P.nprobes();
+        a.tsteps = P.tsteps;
+        a.dx = P.dx; a.dy = P.dy; a.dz = P.dz; a.c1h = P.c1h; a.c2h = P.c2h;
+        a.c1e0 = P.c1e0; a.c2e0 = P.c2e0; a.c1s = P.c1s; a.c2s = P.c2s;
+        a.platesize = P.platesize; a.dt = P.dt;
+        for (int m = 0; m < 2 * P.L; m++) {
+            a.Be[m] = P.Be[m]; a.Ae[m] = P.Ae[m]; a.Bh[m] = P.Bh[m]; a.Ah[m] = P.Ah[m];
+        }
+        double **f[9] = {&a.Ex, &a.Ey, &a.Ez, &a.Hx, &a.Hy, &a.Hz, &a.Jx, &a.Jy, &a.Jz};
+        for (auto p : f) *p = dalloc<double>(NC);
+        const size_t L2 = 2 * (size_t)P.L;
+        const size_t nxs = L2 * P.Ny * P.Nz, nys = (size_t)P.Nx * L2 * P.Nz, nzs = (size_t)P.Nx * P.Ny * L2;
+        if (P.dopml) {
+            a.Phxy = dalloc<double>(nys); a.Phxz = dalloc<double>(nzs); a.Phyx = dalloc<double>(nxs);
+            a.Phyz = dalloc<double>(nzs); a.Phzx = dalloc<double>(nxs); a.Phzy = dalloc<double>(nys);
+            a.Pexy = dalloc<double>(nys); a.Pexz = dalloc<double>(nzs); a.Peyx = dalloc<double>(nxs);
+            a.Peyz = dalloc<double>(nzs); a.Pezx = dalloc<double>(nxs); a.Pezy = dalloc<double>(nys);
+        }
+        a.Eyinc = dalloc<double>(P.Nx); a.Ezinc = dalloc<double>(P.Nx);
+        a.Hyinc = dalloc<double>(P.Nx); a.Hzinc = dalloc<double>(P.Nx);
+        a.PeyxI = dalloc<double>(L2); a.PezxI = dalloc<double>(L2);
+        a.PhyxI = dalloc<double>(L2); a.PhzxI = dalloc<double>(L2);
+        a.wp2 = upload(P.wp2e); a.nu2 = upload(P.nu2e); a.G = upload(P.G);
+        a.xc = upload(P.x); a.yc = upload(P.y); a.zc = upload(P.z);
+        a.lk = upload(P.lk); a.src = upload(P.src); a.phase = upload(P.phase);
+        const size_t nf2 = 2 * (size_t)P.nntf();
+        const size_t fb = (size_t)P.Ny * P.Nz * nf2, tb = (size_t)P.Nx * P.Nz * nf2, lr = (size_t)P.Nx * P.Ny * nf2;
+        for (int q = 0; q < 24; q++) a.ntf[q] = dalloc<double>(q < 8 ? fb : q < 16 ? tb : lr);
+        a.probe = dalloc<double>((size_t)6 * P.tsteps * P.nprobes());
+        std::vector<int> ijk;
+        for (int n = 0; n < P.nprobes(); n++) {
+            ijk.push_back(P.probex[n]); ijk.push_back(P.probey[n]); ijk.push_back(P.probez[n]);
+        }
+        a.probe_ijk = upload(ijk);
+        a.slE = dalloc<double>(slice_len);
+        a.slH = dalloc<double>(slice_len);
+        a.emax = dalloc<unsigned long long>(1);
+        a.flag = dalloc<unsigned int>(1);
+    }
+
+    ~mfdtd_sim() {
+        if (stream) cudaStreamSynchronize(stream);
+        for (cudaEvent_t e : kev) cudaEventDestroy(e);
+        f32.reset();
+        for (void *p : allocs) cudaFree(p);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    void wait() {
+        if (opts.timeout_s > 0) {
+            cudaEvent_t e;
+            mfdtd::ck(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+            mfdtd::ck(cudaEventRecord(e, stream), "cudaEventRecord");
+            double t0 = mfdtd::wall_s();
+            for (;;) {
+                cudaError_t q = cudaEventQuery(e);
+                if (q == cudaSuccess) break;
+                if (q != cudaErrorNotReady) { cudaEventDestroy(e); mfdtd::ck(q, "device"); }
+                if (mfdtd::wall_s() - t0 > opts.timeout_s) {
+                    cudaEventDestroy(e);
+                    throw Error(MFDTD_ETIMEOUT, "device did not finish within timeout_s");
+                }
+                std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
+            cudaEventDestroy(e);
+        } else {
+            mfdtd::ck(cudaStreamSynchronize(stream), "device");
+        }
+    }
+
+    // Record step: max|Ex| and the slice/incident arrays after step t.
+    void do_record(int tt, bool collect) {
+        mfdtd::Record r;
+        r.t = tt;
+        const size_t Nx = P.Nx;
+        unsigned long long bits = 0;
+        r.E.resize(slice_len + 2 * Nx);
+        r.H.resize(slice_len + 2 * Nx);
+        if (form == MFDTD_FORM_FP64_PLAIN) {
+            mfdtd::plain_launch_emax(pa, stream);
+            mfdtd::ck(cudaMemcpyAsync(&bits, pa.emax, 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(r.E.data(), pa.slE, slice_len * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(r.E.data() + slice_len, pa.Eyinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(r.E.data() + slice_len + Nx, pa.Ezinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(r.H.data(), pa.slH, slice_len * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(r.H.data() + slice_len, pa.Hyinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(r.H.data() + slice_len + Nx, pa.Hzinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            wait();
+            std::memcpy(&r.emax, &bits, 8);
+        } else {
+            f32->record(r.E.data(), r.H.data(), &r.emax, stream);
+            wait();
+        }
+        if (sink) {
+            char line[256];
+            double partialtime = 100 * tt / P.tsteps;
+            std::snprintf(line, sizeof line, "t = %d: %s %% Done...  Maximum abs(Ex) is %s\n", tt,
+                          mfdtd::fmt_g(partialtime).c_str(), mfdtd::fmt_g(r.emax).c_str());
+            sink->log(line);
+            if (P.savefields) {
+                std::vector<double> zeros(slice_len, 0.0);  // output_J.dat: never assigned
+                sink->append("output_E.dat", r.E.data(), r.E.size() * 8);
+                sink->append("output_J.dat", zeros.data(), zeros.size() * 8);
+                sink->append("output_H.dat", r.H.data(), r.H.size() * 8);
+            }
+        }
+        if (collect) records.push_back(std::move(r));
+    }
+
+    int kernel_classes() const {
+        return form == MFDTD_FORM_FP64_PLAIN ? 2 : mfdtd::Fp32Sim::kernel_classes();
+    }
+
+    void advance(int nsteps, bool collect) {
+        if (nsteps < 0 || t + nsteps > P.tsteps)
+            throw Error(MFDTD_EINVAL, "advance past tsteps");
+        int64_t launches = 0;
+        const int nk = kernel_classes();
+        const int prof_steps = opts.profile ? std::min(nsteps, 512) : 0;
+        if (prof_steps) {
+            kname.assign(nk, "");
+            for (int q = 0; q < nk; q++)
+                kname[q] = form == MFDTD_FORM_FP64_PLAIN ? (q == 0 ? "k_plain_h" : "k_plain_e")
+                                                         : mfdtd::Fp32Sim::kernel_name(q);
+            ktotal_ms.assign(nk, 0.0);
+            kcount.assign(nk, 0);
+            while ((int)kev.size() < (nk + 1) * prof_steps) {
+                cudaEvent_t e;
+                mfdtd::ck(cudaEventCreate(&e), "cudaEventCreate");
+                kev.push_back(e);
+            }
+        }
+        mfdtd::ck(cudaEventRecord(ev0, stream), "cudaEventRecord");
+        const int t_begin = t, t_end = t + nsteps;
+        for (; t < t_end; t++) {
+            const bool rec = (t % P.record_period) == 0;
+            const int ps = t - t_begin;
+            void *const *ev = ps < prof_steps ? (void *const *)&kev[(size_t)(nk + 1) * ps] : nullptr;
+            if (form == MFDTD_FORM_FP64_PLAIN) launches += mfdtd::plain_launch_step(pa, t, rec, stream, ev);
+            else launches += f32->step(t, rec, stream, ev);
+            mfdtd::ck(cudaGetLastError(), "kernel launch");
+            if (rec && (collect || sink)) {
+                mfdtd::ck(cudaEventRecord(ev1, stream), "cudaEventRecord");
+                do_record(t, collect);
+            }
+            if (t == 20 && sink) {
+                wait();
+                double runtimemin = (mfdtd::wall_s() - loop_start) / 60.0;
+                double totaltime = runtimemin * P.tsteps / 20.0;
+                sink->log("t = 20, time taken = " + mfdtd::fmt_g(runtimemin) + " minutes.\n");
+                sink->log("You can expect the total simulation to take " + mfdtd::fmt_g(totaltime) +
+                          " minutes.\n");
+            }
+            if (opts.guard_period > 0 && (t + 1) % opts.guard_period == 0) guard();
+        }
+        mfdtd::ck(cudaEventRecord(ev1, stream), "cudaEventRecord");
+        mfdtd::ck(cudaGetLastError(), "kernel launch");
+        last_launches = launches;
+        if (nsteps > 0) {
+            wait();
+            float ms = 0;
+            mfdtd::ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
+            last_ms_per_step = ms / nsteps;
+            for (int ps = 0; ps < prof_steps; ps++)
+                for (int q = 0; q < nk; q++) {
+                    float kms = 0;
+                    mfdtd::ck(cudaEventElapsedTime(&kms, kev[(size_t)(nk + 1) * ps + q],
+                                                   kev[(size_t)(nk + 1) * ps + q + 1]),
+                              "cudaEventElapsedTime");
+                    ktotal_ms[q] += kms;
+                    kcount[q] += 1;
+                }
+        }
+    }
+
+    void guard() {
+        bool bad;
+        if (form == MFDTD_FORM_FP64_PLAIN) {
+            unsigned int flag = 0;
+            mfdtd::plain_launch_guard(pa, stream);
+            mfdtd::ck(cudaMemcpyAsync(&flag, pa.flag, 4, cudaMemcpyDeviceToHost, stream), "D2H");
+            wait();
+            bad = flag != 0;
+        } else {
+            bad = f32->guard(stream) != 0;
+        }
+        if (bad) throw Error(MFDTD_ENUMERIC, "non-finite E field after step " + std::to_string(t));
+    }
+
+    // E probes of the final step ride in the next H kernel; emit them once.
+    void flush() {
+        if (flushed || t == 0) return;
+        if (form == MFDTD_FORM_FP64_PLAIN) mfdtd::plain_launch_flush(pa, t - 1, stream);
+        else f32->flush(t - 1, stream);
+        flushed = true;
+    }
+
+    int64_t ntf_size() const {
+        const int64_t nf2 = 2 * (int64_t)P.nntf();
+        return 2 * nf2 + 8 * ((int64_t)P.Ny * P.Nz * nf2) + 8 * ((int64_t)P.Nx * P.Nz * nf2) +
+               8 * ((int64_t)P.Nx * P.Ny * nf2);
+    }
+
+    void read_ntf(double *out) {
+        flush();
+        const size_t nf2 = 2 * (size_t)P.nntf();
+        // Source DFT sums: a function of the injected waveform only.  They
+        // cover the steps run so far.
+        std::vector<double> sd(4 * (size_t)P.nntf(), 0.0);
+        {
+            const double PI = 3.141592653589793;
+            const int nf = P.nntf();
+            for (int tt = 0; tt < t; tt++)
+                for (int m = 0; m < nf; m++) {
+                    double s = sin(2 * PI * P.fntf[m] * (tt + 1 / 2) * P.dt);
+                    double c = cos(2 * PI * P.fntf[m] * (tt + 1 / 2) * P.dt);
+                    sd[2 * nf + 2 * m] += P.src[2 * tt] * s;
+                    sd[2 * nf + 2 * m + 1] += P.src[2 * tt] * c;
+                    sd[2 * m] += P.src[2 * tt + 1] * s;
+                    sd[2 * m + 1] += P.src[2 * tt + 1] * c;
+                }
+        }
+        std::memcpy(out, sd.data(), sd.size() * 8);
+        double *o = out + sd.size();
+        const size_t fb = (size_t)P.Ny * P.Nz * nf2, tb = (size_t)P.Nx * P.Nz * nf2, lr = (size_t)P.Nx * P.Ny * nf2;
+        for (int q = 0; q < 24; q++) {
+            size_t n = q < 8 ? fb : q < 16 ? tb : lr;
+            if (form == MFDTD_FORM_FP64_PLAIN)
+                mfdtd::ck(cudaMemcpyAsync(o, pa.ntf[q], n * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            else f32->read_ntf(q, o, stream);
+            o += n;
+        }
+        wait();
+    }
+
+    void read_probes(double *out) {
+        flush();
+        size_t n = (size_t)6 * P.tsteps * P.nprobes();
+        if (form == MFDTD_FORM_FP64_PLAIN)
+            mfdtd::ck(cudaMemcpyAsync(out, pa.probe, n * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        else f32->read_probes(out, stream);
+        wait();
+    }
+
+    void read_field(int comp, double *out) {
+        if (comp < 0 || comp > 8) throw Error(MFDTD_EINVAL, "component must be 0..8");
+        if (form == MFDTD_FORM_FP64_PLAIN) {
+            double *f[9] = {pa.Ex, pa.Ey, pa.Ez, pa.Hx, pa.Hy, pa.Hz, pa.Jx, pa.Jy, pa.Jz};
+            mfdtd::ck(cudaMemcpyAsync(out, f[comp], P.cells() * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+        } else {
+            f32->read_field(comp, out, stream);
+        }
+        wait();
+    }
+
+    void write_final(const std::string &dir) {
+        mfdtd::FileSink fs{dir};
+        std::vector<double> ntf((size_t)ntf_size());
+        read_ntf(ntf.data());
+        // output_NTF.dat, source/meteor-2.1.cpp:1579-1620
+        std::string path = dir + "/output_NTF.dat";
+        FILE *f = std::fopen(path.c_str(), "wb");
+        if (!f) throw Error(MFDTD_EIO, "cannot write " + path);
+        int32_t hdr[2] = {P.nntf(), P.ntfb};
+        std::fwrite(hdr, 4, 2, f);
+        std::fwrite(P.fntf.data(), 8, P.fntf.size(), f);
+        std::fwrite(ntf.data(), 8, ntf.size(), f);
+        std::fclose(f);
+        // Probe.dat, source/meteor-2.1.cpp:1624-1636
+        std::vector<double> pr((size_t)6 * P.tsteps * P.nprobes());
+        read_probes(pr.data());
+        path = dir + "/Probe.dat";
+        f = std::fopen(path.c_str(), "wb");
+        if (!f) throw Error(MFDTD_EIO, "cannot write " + path);
+        int32_t np = P.nprobes();
+        std::fwrite(&np, 4, 1, f);
+        if (np) {
+            std::fwrite(P.probex.data(), 4, np, f);
+            std::fwrite(P.probey.data(), 4, np, f);
+            std::fwrite(P.probez.data(), 4, np, f);
+        }
+        if (!pr.empty()) std::fwrite(pr.data(), 8, pr.size(), f);
+        std::fclose(f);
+    }
+};
+
+namespace {
+
+int fail(const Error &e) {
+    mfdtd::g_last_error = e.what();
+    return e.code;
+}
+
+template <class F> int guarded(F &&fn) {
+    try {
+        fn();
+        return MFDTD_OK;
+    } catch (const Error &e) {
+        return fail(e);
+    } catch (const std::bad_alloc &) {
+        mfdtd::g_last_error = "host allocation failed";
+        return MFDTD_ENOMEM;
+    } catch (const std::exception &e) {
+        mfdtd::g_last_error = e.what();
+        return MFDTD_EINVAL;
+    }
+}
+
+void log_header(mfdtd::FileSink &fs, const Problem &P) {
+    struct rusage ru;
+    getrusage(RUSAGE_SELF, &ru);
+    double memusage = (double)ru.ru_maxrss / 1024 / 1024;
+    std::string dir = fs.dir + "/log.txt";
+    FILE *f = std::fopen(dir.c_str(), "w");
+    if (!f) throw Error(MFDTD_EIO, "cannot write " + dir);
+    std::fprintf(f, "------------------------------------------\n");
+    std::fprintf(f, "3D Meteor Scattering Simulation\n");
+    std::fprintf(f, "------------------------------------------\n");
+    std::fprintf(f, "dx = %g\n", P.dx);
+    std::fprintf(f, "source type = %d\n", P.sourcetype);
+    std::fprintf(f, "source polarization = %d\n", P.sourcepol);
+    std::fprintf(f, "Time step = %g\n", P.dt);
+    std::fprintf(f, "Total time steps = %d\n", P.tsteps);
+    std::fprintf(f, "Total NTF frequencies = %d\n", P.nntf());
+    std::fprintf(f, "last NTF frequency = %g\n", P.fntf.back());
+    std::fprintf(f, "Total memory usage = %g GB\n", memusage);
+    std::fclose(f);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *mfdtd_version(void) { return "mfdtd-gb300 0.1"; }
+
+int mfdtd_last_error(char *buf, size_t n) {
+    if (!buf || n == 0) return MFDTD_EINVAL;
+    std::snprintf(buf, n, "%s", mfdtd::g_last_error.c_str());
+    return MFDTD_OK;
+}
+
+int mfdtd_problem_from_rundir(const char *dir, mfdtd_problem **out) {
+    return guarded([&] {
+        if (!dir || !out) throw Error(MFDTD_EINVAL, "NULL argument");
+        std::unique_ptr<mfdtd_problem> p(new mfdtd_problem());
+        p->P = mfdtd::problem_from_rundir(dir);
+        *out = p.release();
+    });
+}
+
+int mfdtd_problem_create(const mfdtd_params *prm, const double *wp2, const double *nu2,
+                         const double B0[3], mfdtd_problem **out) {
+    return guarded([&] {
+        if (!prm || !out) throw Error(MFDTD_EINVAL, "NULL argument");
+        std::unique_ptr<mfdtd_problem> p(new mfdtd_problem());
+        p->P = mfdtd::problem_from_params(*prm, wp2, nu2, B0);
+        *out = p.release();
+    });
+}
+
+void mfdtd_problem_destroy(mfdtd_problem *pb) { delete pb; }
+
+int mfdtd_problem_dims(const mfdtd_problem *pb, int64_t out[6]) {
+    return guarded([&] {
+        if (!pb || !out) throw Error(MFDTD_EINVAL, "NULL argument");
+        const Problem &P = pb->P;
+        out[0] = P.Nx; out[1] = P.Ny; out[2] = P.Nz;
+        out[3] = P.tsteps; out[4] = P.nntf(); out[5] = P.nprobes();
+    });
+}
+
+int mfdtd_problem_footprint(const mfdtd_problem *pb, int32_t form, int64_t *bytes) {
+    return guarded([&] {
+        if (!pb || !bytes) throw Error(MFDTD_EINVAL, "NULL argument");
+        const Problem &P = pb->P;
+        const int64_t NC = (int64_t)P.cells(), L2 = 2 * P.L;
+        const int64_t psi = P.dopml ? 4 * (L2 * P.Ny * P.Nz + (int64_t)P.Nx * L2 * P.Nz + (int64_t)P.Nx * P.Ny * L2) : 0;
+        const int64_t nf2 = 2 * P.nntf();
+        const int64_t ntf = 8 * nf2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz + (int64_t)P.Nx * P.Ny);
+        const int64_t misc = 8 * ((int64_t)P.tsteps * (2 + nf2 + 6 * P.nprobes()) + (int64_t)P.lk.size() +
+                                  4 * ((int64_t)P.Nx * P.Ny + P.Nx + P.Ny + P.Nz));
+        if (form == MFDTD_FORM_FP64_PLAIN) *bytes = 8 * (9 * NC + psi) + 8 * ntf + misc;
+        else *bytes = mfdtd::Fp32Sim::footprint(P);
+    });
+}
+
+int mfdtd_sim_create(const mfdtd_problem *pb, const mfdtd_run_opts *opts, mfdtd_sim **out) {
+    return guarded([&] {
+        if (!pb || !out) throw Error(MFDTD_EINVAL, "NULL argument");
+        std::unique_ptr<mfdtd_sim> s(new mfdtd_sim());
+        s->init(pb->P, opts);
+        *out = s.release();
+    });
+}
+
+void mfdtd_sim_destroy(mfdtd_sim *s) { delete s; }
+
+int mfdtd_sim_advance(mfdtd_sim *s, int32_t nsteps, int32_t collect_records) {
+    return guarded([&] {
+        if (!s) throw Error(MFDTD_EINVAL, "NULL sim");
+        s->advance(nsteps, collect_records != 0);
+    });
+}
+
+int mfdtd_sim_sync(mfdtd_sim *s) {
+    return guarded([&] {
+        if (!s) throw Error(MFDTD_EINVAL, "NULL sim");
+        s->wait();
+    });
+}
+
+int mfdtd_sim_step_index(const mfdtd_sim *s, int32_t *t) {
+    return guarded([&] {
+        if (!s || !t) throw Error(MFDTD_EINVAL, "NULL argument");
+        *t = s->t;
+    });
+}
+
+int64_t mfdtd_sim_ntf_size(const mfdtd_sim *s) { return s ? s->ntf_size() : -1; }
+
+int mfdtd_sim_read_ntf(mfdtd_sim *s, double *out, int64_t n) {
+    return guarded([&] {
+        if (!s || !out) throw Error(MFDTD_EINVAL, "NULL argument");
+        if (n < s->ntf_size()) throw Error(MFDTD_EINVAL, "output buffer too small");
+        s->read_ntf(out);
+    });
+}
+
+int mfdtd_sim_read_probes(mfdtd_sim *s, double *out, int64_t n) {
+    return guarded([&] {
+        if (!s || (!out && n)) throw Error(MFDTD_EINVAL, "NULL argument");
+        if (n < (int64_t)6 * s->P.tsteps * s->P.nprobes()) throw Error(MFDTD_EINVAL, "output buffer too small");
+        s->read_probes(out);
+    });
+}
+
+int mfdtd_sim_read_field(mfdtd_sim *s, int32_t comp, double *out, int64_t n) {
+    return guarded([&] {
+        if (!s || !out) throw Error(MFDTD_EINVAL, "NULL argument");
+        if (n < (int64_t)s->P.cells()) throw Error(MFDTD_EINVAL, "output buffer too small");
+        s->read_field(comp, out);
+    });
+}
+
+int mfdtd_sim_write_outputs(mfdtd_sim *s, const char *dir) {
+    return guarded([&] {
+        if (!s || !dir) throw Error(MFDTD_EINVAL, "NULL argument");
+        mfdtd::FileSink fs{dir};
+        for (auto &r : s->records) {
+            char line[256];
+            double partialtime = 100 * r.t / s->P.tsteps;
+            std::snprintf(line, sizeof line, "t = %d: %s %% Done...  Maximum abs(Ex) is %s\n", r.t,
+                          mfdtd::fmt_g(partialtime).c_str(), mfdtd::fmt_g(r.emax).c_str());
+            fs.log(line);
+            if (s->P.savefields) {
+                std::vector<double> zeros(s->slice_len, 0.0);
+                fs.append("output_E.dat", r.E.data(), r.E.size() * 8);
+                fs.append("output_J.dat", zeros.data(), zeros.size() * 8);
+                fs.append("output_H.dat", r.H.data(), r.H.size() * 8);
+            }
+        }
+        s->write_final(dir);
+    });
+}
+
+int mfdtd_sim_last_timing(const mfdtd_sim *s, double *ms_per_step, int64_t *launches) {
+    return guarded([&] {
+        if (!s) throw Error(MFDTD_EINVAL, "NULL sim");
+        if (ms_per_step) *ms_per_step = s->last_ms_per_step;
+        if (launches) *launches = s->last_launches;
+    });
+}
+
+int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t name_len,
+                           double *avg_ms, int64_t *launches) {
+    return guarded([&] {
+        if (!s) throw Error(MFDTD_EINVAL, "NULL sim");
+        if (which < 0 || which >= (int32_t)s->kname.size())
+            throw Error(MFDTD_EINVAL, "no such kernel class (was opts.profile set?)");
+        if (name && name_len) std::snprintf(name, name_len, "%s", s->kname[which].c_str());
+        if (avg_ms) *avg_ms = s->kcount[which] ? s->ktotal_ms[which] / s->kcount[which] : 0.0;
+        if (launches) *launches = s->kcount[which];
+    });
+}
+
+int mfdtd_run_rundir(const char *dir, const mfdtd_run_opts *opts) {
+    return guarded([&] {
+        if (!dir) throw Error(MFDTD_EINVAL, "NULL dir");
+        double tStart = mfdtd::wall_s();
+        Problem P = mfdtd::problem_from_rundir(dir);
+        mfdtd::FileSink fs{dir};
+        log_header(fs, P);
+        std::unique_ptr<mfdtd_sim> s(new mfdtd_sim());
+        s->init(P, opts);
+        s->sink = &fs;
+        s->loop_start = mfdtd::wall_s();
+        s->advance(P.tsteps, false);
+        s->write_final(dir);
+        const bool quiet = opts && opts->quiet;
+        if (!quiet && P.Ny > 39 && P.Nz > 79) {
+            // debug print of source/meteor-2.1.cpp:1601-1602, in bounds only
+            std::vector<double> ntf((size_t)s->ntf_size());
+            s->read_ntf(ntf.data());
+            const size_t nf2 = 2 * (size_t)P.nntf();
+            const size_t at = 4 * (size_t)P.nntf() + ((size_t)39 * P.Nz + 79) * nf2;
+            const size_t fb = (size_t)P.Ny * P.Nz * nf2;
+            std::printf("My-front at y = 40, z = 80 is %g\n", ntf[at]);
+            std::printf("Mz-front at y = 40, z = 80 is %g\n", ntf[at + fb]);
+        }
+        fs.log("All done!\n");
+        fs.log("Total run time = " + mfdtd::fmt_g((mfdtd::wall_s() - tStart) / 60.0) + "minutes.\n");
+    });
+}
+
+}  // extern "C"

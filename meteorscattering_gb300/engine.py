@@ -1,0 +1,269 @@
+"""ctypes binding of the C ABI in ``include/mfdtd.h``.
+
+This is the Python face of the engine.  It mirrors the reference's interface
+for the path: :func:`run_rundir` is the reference executable run in a run
+directory (``source/meteor-2.1.cpp:42``); :class:`Problem` and
+:class:`Simulation` expose the same stages for callers that keep data in
+memory.  There is no CPU fallback: if ``libmfdtd.so`` has not been built, or a
+call needs a GPU and none is present, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libmfdtd.so")
+EXE_PATH = os.path.join(_HERE, "_lib", "meteor")
+
+FORM_FP64_PLAIN = 0
+FORM_FP32_FUSED = 1
+
+STATUS = {0: "OK", -1: "EINVAL", -2: "EIO", -3: "ECUDA", -4: "ENOMEM", -5: "ETIMEOUT",
+          -6: "ENUMERIC", -7: "ESTATE"}
+
+# Every entry point declared in include/mfdtd.h.
+EXPORTS = (
+    "mfdtd_run_rundir", "mfdtd_problem_from_rundir", "mfdtd_problem_create",
+    "mfdtd_problem_destroy", "mfdtd_problem_dims", "mfdtd_problem_footprint",
+    "mfdtd_sim_create", "mfdtd_sim_destroy", "mfdtd_sim_advance", "mfdtd_sim_sync",
+    "mfdtd_sim_step_index", "mfdtd_sim_ntf_size", "mfdtd_sim_read_ntf",
+    "mfdtd_sim_read_probes", "mfdtd_sim_read_field", "mfdtd_sim_write_outputs",
+    "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_last_error", "mfdtd_version",
+)
+
+
+class MfdtdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class RunOpts(C.Structure):
+    _fields_ = [("form", C.c_int32), ("device", C.c_int32), ("guard_period", C.c_int32),
+                ("quiet", C.c_int32), ("timeout_s", C.c_double), ("profile", C.c_int32)]
+
+
+class Params(C.Structure):
+    """``mfdtd_params`` -- the fields of inputs.dat in file order."""
+    _fields_ = [
+        ("dopml", C.c_int32), ("savefields", C.c_int32), ("f0", C.c_double), ("fsig", C.c_double),
+        ("sourcetype", C.c_int32), ("sourcepol", C.c_int32), ("gridfactor", C.c_double),
+        ("dt", C.c_double), ("tsteps", C.c_int32), ("Nx", C.c_int32), ("Ny", C.c_int32),
+        ("Nz", C.c_int32), ("metsize", C.c_double * 2), ("wpmax", C.c_double),
+        ("numax", C.c_double), ("metloc", C.c_double * 3), ("metangle", C.c_double),
+        ("mettype", C.c_int32), ("numfiles", C.c_int32), ("nprobes", C.c_int32),
+        ("probex", C.POINTER(C.c_int32)), ("probey", C.POINTER(C.c_int32)),
+        ("probez", C.POINTER(C.c_int32)), ("nntf", C.c_int32), ("fntf", C.POINTER(C.c_double)),
+        ("doplate", C.c_int32), ("platesize", C.c_double), ("doB0", C.c_int32),
+    ]
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load ``libmfdtd.so`` (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: run meteorscattering_gb300.build.build() "
+                           "(or __graft_entry__.build()) first; there is no CPU fallback")
+    lib = C.CDLL(path)
+    vp, i32, i64, dp = C.c_void_p, C.c_int32, C.c_int64, C.POINTER(C.c_double)
+    sig = {
+        "mfdtd_run_rundir": (C.c_int, [C.c_char_p, C.POINTER(RunOpts)]),
+        "mfdtd_problem_from_rundir": (C.c_int, [C.c_char_p, C.POINTER(vp)]),
+        "mfdtd_problem_create": (C.c_int, [C.POINTER(Params), dp, dp, dp, C.POINTER(vp)]),
+        "mfdtd_problem_destroy": (None, [vp]),
+        "mfdtd_problem_dims": (C.c_int, [vp, C.POINTER(i64)]),
+        "mfdtd_problem_footprint": (C.c_int, [vp, i32, C.POINTER(i64)]),
+        "mfdtd_sim_create": (C.c_int, [vp, C.POINTER(RunOpts), C.POINTER(vp)]),
+        "mfdtd_sim_destroy": (None, [vp]),
+        "mfdtd_sim_advance": (C.c_int, [vp, i32, i32]),
+        "mfdtd_sim_sync": (C.c_int, [vp]),
+        "mfdtd_sim_step_index": (C.c_int, [vp, C.POINTER(i32)]),
+        "mfdtd_sim_ntf_size": (i64, [vp]),
+        "mfdtd_sim_read_ntf": (C.c_int, [vp, dp, i64]),
+        "mfdtd_sim_read_probes": (C.c_int, [vp, dp, i64]),
+        "mfdtd_sim_read_field": (C.c_int, [vp, i32, dp, i64]),
+        "mfdtd_sim_write_outputs": (C.c_int, [vp, C.c_char_p]),
+        "mfdtd_sim_last_timing": (C.c_int, [vp, dp, C.POINTER(i64)]),
+        "mfdtd_sim_kernel_stats": (C.c_int, [vp, i32, C.c_char_p, C.c_size_t, dp,
+                                             C.POINTER(i64)]),
+        "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+        "mfdtd_version": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(4096)
+    load_library().mfdtd_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise MfdtdError(rc, last_error())
+
+
+def _opts(form: int = FORM_FP64_PLAIN, device: int = 0, guard_period: int = 0,
+          quiet: bool = True, timeout_s: float = 0.0, profile: bool = False) -> RunOpts:
+    return RunOpts(form, device, guard_period, 1 if quiet else 0, timeout_s, 1 if profile else 0)
+
+
+def run_rundir(path: str, form: int = FORM_FP64_PLAIN, device: int = 0,
+               quiet: bool = True, timeout_s: float = 0.0) -> None:
+    """Run the whole solver in run directory ``path`` (the reference's
+    ``meteor`` executable contract)."""
+    lib = load_library()
+    o = _opts(form, device, 0, quiet, timeout_s)
+    _check(lib.mfdtd_run_rundir(os.fsencode(path), C.byref(o)))
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Problem:
+    """Parsed inputs (host only; no GPU needed)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    @classmethod
+    def from_rundir(cls, path: str) -> "Problem":
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.mfdtd_problem_from_rundir(os.fsencode(path), C.byref(h)))
+        return cls(h)
+
+    @classmethod
+    def from_params(cls, p, wp2_c: np.ndarray, nu2_c: np.ndarray,
+                    B0: Sequence[float] = (0.0, 0.0, 0.0)) -> "Problem":
+        """``p`` is a :class:`meteorscattering_gb300.rundir.RunParams`;
+        ``wp2_c``/``nu2_c`` are ``[Nx][Ny]`` C-order arrays (wp.dat byte order)."""
+        lib = load_library()
+        px = np.ascontiguousarray(p.probex, dtype=np.int32)
+        py = np.ascontiguousarray(p.probey, dtype=np.int32)
+        pz = np.ascontiguousarray(p.probez, dtype=np.int32)
+        ff = np.ascontiguousarray(p.fntf, dtype=np.float64)
+        i32p = lambda a: a.ctypes.data_as(C.POINTER(C.c_int32))
+        prm = Params(p.dopml, p.savefields, p.f0, p.fsig, p.sourcetype, p.sourcepol,
+                     p.gridfactor, p.dt, p.tsteps, p.Nx, p.Ny, p.Nz,
+                     (C.c_double * 2)(*p.metsize), p.wpmax, p.numax,
+                     (C.c_double * 3)(*p.metloc), p.metangle, p.mettype, p.numfiles,
+                     len(px), i32p(px), i32p(py), i32p(pz), len(ff), _dp(ff), p.doplate,
+                     p.platesize, int(p.doB0 or 0))
+        w = np.ascontiguousarray(wp2_c, dtype=np.float64)
+        n = np.ascontiguousarray(nu2_c, dtype=np.float64)
+        b = np.ascontiguousarray(B0, dtype=np.float64)
+        h = C.c_void_p()
+        _check(lib.mfdtd_problem_create(C.byref(prm), _dp(w), _dp(n), _dp(b), C.byref(h)))
+        return cls(h)
+
+    def dims(self):
+        out = (C.c_int64 * 6)()
+        _check(load_library().mfdtd_problem_dims(self._h, out))
+        return tuple(out)
+
+    def footprint(self, form: int = FORM_FP64_PLAIN) -> int:
+        v = C.c_int64()
+        _check(load_library().mfdtd_problem_footprint(self._h, form, C.byref(v)))
+        return v.value
+
+    def close(self):
+        if self._h:
+            load_library().mfdtd_problem_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Simulation:
+    """Device-resident state of one run."""
+
+    def __init__(self, problem: Problem, form: int = FORM_FP64_PLAIN, device: int = 0,
+                 guard_period: int = 0, timeout_s: float = 0.0, profile: bool = False):
+        lib = load_library()
+        self.dims = problem.dims()
+        o = _opts(form, device, guard_period, True, timeout_s, profile)
+        h = C.c_void_p()
+        _check(lib.mfdtd_sim_create(problem._h, C.byref(o), C.byref(h)))
+        self._h = h
+
+    def advance(self, nsteps: int, collect_records: bool = False) -> None:
+        _check(load_library().mfdtd_sim_advance(self._h, nsteps, 1 if collect_records else 0))
+
+    def sync(self) -> None:
+        _check(load_library().mfdtd_sim_sync(self._h))
+
+    @property
+    def step_index(self) -> int:
+        v = C.c_int32()
+        _check(load_library().mfdtd_sim_step_index(self._h, C.byref(v)))
+        return v.value
+
+    def read_ntf(self) -> np.ndarray:
+        lib = load_library()
+        n = lib.mfdtd_sim_ntf_size(self._h)
+        out = np.empty(n, dtype=np.float64)
+        _check(lib.mfdtd_sim_read_ntf(self._h, _dp(out), n))
+        return out
+
+    def read_probes(self) -> np.ndarray:
+        Nx, Ny, Nz, T, nf, npb = self.dims
+        out = np.empty((6, T, npb), dtype=np.float64)
+        _check(load_library().mfdtd_sim_read_probes(self._h, _dp(out), out.size))
+        return out
+
+    def read_field(self, comp: int) -> np.ndarray:
+        Nx, Ny, Nz = self.dims[:3]
+        out = np.empty((Nx, Ny, Nz), dtype=np.float64)
+        _check(load_library().mfdtd_sim_read_field(self._h, comp, _dp(out), out.size))
+        return out
+
+    def write_outputs(self, path: str) -> None:
+        _check(load_library().mfdtd_sim_write_outputs(self._h, os.fsencode(path)))
+
+    def last_timing(self):
+        ms, n = C.c_double(), C.c_int64()
+        _check(load_library().mfdtd_sim_last_timing(self._h, C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def kernel_stats(self):
+        """[(name, mean ms per launch, launches)] of the last advance (profile=True)."""
+        lib, out, q = load_library(), [], 0
+        while True:
+            name = C.create_string_buffer(128)
+            ms, n = C.c_double(), C.c_int64()
+            if lib.mfdtd_sim_kernel_stats(self._h, q, name, 128, C.byref(ms), C.byref(n)) != 0:
+                break
+            out.append((name.value.decode(), ms.value, n.value))
+            q += 1
+        return out
+
+    def close(self):
+        if self._h:
+            load_library().mfdtd_sim_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
