@@ -65,6 +65,13 @@ def workload(name: str, steps_total: int):
                 "plane wave along +x (Ez), z-uniform Gaussian trail n0=1e15 r0=0.8 m, "
                 "nu=3e4, B0=5e-5 T at 60 deg dip")
         n0, r0, nu = 1e15, 0.8, 3e4
+    elif name == "trail256":
+        # Profiling-size version of trail768 (2 GB of FP32 state, > L2).
+        N = (256, 256, 512)
+        f0, gf = 50e6, 30.0
+        desc = ("256x256x512 magnetized trail, dx=0.2 m, Lee-Kalluri J, 10-cell CPML, "
+                "plane wave along +x (Ez), z-uniform Gaussian trail n0=1e15 r0=0.8 m")
+        n0, r0, nu = 1e15, 0.8, 3e4
     elif name == "cfg1":
         N = (96, 96, 192)
         f0, gf = 50e6, 24.0
@@ -98,9 +105,10 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams) -> float:
         if kernel == "k_plain_e":   # H r(3), E r/w(6), J r(3) ; psi r/w
             return cells * 12 * 8 + psi * 16
     else:
-        # FP32 single pass: E, H, J read and written (18 x 4 B) + per-cell
-        # plasma weight (4 B); both psi halves read and written.
-        return cells * 19 * 4 + 2 * psi * 8
+        # FP32 single pass: E, H, J read and written (18 x 4 B); the plasma
+        # weight comes from 2-D/1-D tables (no per-cell read); every psi cell
+        # of both half-steps read and written once.
+        return cells * 18 * 4 + 2 * psi * 8
     raise KeyError(kernel)
 
 
@@ -265,7 +273,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--form", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--form", default="fp32", choices=["fp64", "fp32"])
     ap.add_argument("--workload", default="trail768")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -22,12 +22,15 @@ public:
     void read_ntf(int q, double *out, void *stream);
     void read_probes(double *out, void *stream);
     void read_field(int comp, double *out, void *stream);
+    // Throws if a kernel set the device error flag (a bounded wait ran out).
+    void check(void *stream);
     ~Fp32Sim();
 
 private:
     struct Impl;
     Impl *impl_ = nullptr;
     int64_t bytes_ = 0;
+    int m_cur_ = 0;  // which ping-pong set holds the current E/H state
 };
 
 }  // namespace mfdtd

@@ -1,25 +1,1050 @@
-// fp32_fused.cu -- FP32 fused form of the time step.
+// fp32_fused.cu -- FP32 fused form: one pass over the grid per time step.
+//
+// Storage: E, H, J and the CPML psi slabs in FP32; the running-DFT sums of the
+// Huygens surface in FP64 (the same 24 arrays and layout as the reference's
+// output_NTF.dat).  The arithmetic follows the reference's discretisation
+// (source/meteor-2.1.cpp:656-1504, source/meteor-fork.cpp:1539-1595) with the
+// division by the cell size folded into precomputed FP32 coefficients and FMA
+// contraction allowed.
+//
+// One kernel launch advances one time step.  Each CTA owns a TJ x TK tile of
+// (j,k) columns and marches along x (the slowest axis, stride Ny*Nzp), one
+// plane per iteration:
+//   * the plane's E, H and J tiles (plus one-cell halos) arrive by TMA
+//     (cp.async.bulk.tensor.3d) into a ring of NS shared-memory stages, each
+//     guarded by an mbarrier; the producer runs NS-2 planes ahead;
+//   * J of the previous step is advanced first (it needs E of this step's
+//     start, which is read-only in this pass), then H of this plane (tile plus
+//     a low-side halo row and column, which the E update needs), then E;
+//   * H and E of the previous plane stay in registers (Hy, Hz, Ex), so each
+//     field value is read from DRAM once and written once per step.
+// E, H and the H-psi slabs are double-buffered (a pass reads set `par` and
+// writes set `par^1`), because neighbouring CTAs read halo cells that another
+// CTA writes in the same pass.  J and the E-psi slabs are touched only by
+// their owning thread and are updated in place.
+#include <cuda.h>
 #include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "fp32.hpp"
 
 namespace mfdtd {
+namespace {
 
-struct Fp32Sim::Impl {};
+constexpr int TJ = 8, TK = 32;             // tile rows (j) x columns (k)
+constexpr int EJ = TJ + 2, EK = TK + 8;    // E box: rows j0-1..j0+TJ, cols k0-4..k0+TK+3
+constexpr int HJ = TJ + 1, HK = TK + 4;    // H box: rows j0-1..j0+TJ-1, cols k0-4..k0+TK-1
+constexpr int NS = 4;                      // pipeline stages
+constexpr int NTHREADS = 320;              // 8 tile warps + halo-row warp + halo-column warp
+constexpr int PROD = NTHREADS - 1;         // producer thread (idle lane of the halo-column warp)
+constexpr int align128(int b) { return (b + 127) / 128 * 128; }
+constexpr int E_B = align128(EJ * EK * 4), H_B = align128(HJ * HK * 4), J_B = TJ * TK * 4;
+constexpr int STAGE_B = 3 * E_B + 3 * H_B + 3 * J_B;
+constexpr int STAGE_TX = 3 * EJ * EK * 4 + 3 * HJ * HK * 4 + 3 * TJ * TK * 4;  // bytes per stage
+constexpr int HN_COLS = TK + 1;            // new-H plane: cols k0-1..k0+TK-1
+constexpr int HN_B = 3 * HJ * HN_COLS * 4;
+constexpr int SMEM_B = NS * STAGE_B + align128(HN_B) + NS * 8 + 128;
+constexpr double kE0 = 8.85419e-12;
 
-int64_t Fp32Sim::footprint(const Problem &P) { return (int64_t)P.cells() * 76; }
-void Fp32Sim::init(const Problem &, void *) {
-    throw Error(MFDTD_EINVAL, "FP32 fused form is not available in this build");
+struct Maps {
+    CUtensorMap E[2][3], H[2][3], J[3];
+};
+
+struct Args {
+    int Nx, Ny, Nz, Nzp, L, xshift, yshift, zshift;
+    int bx1, bx2, by1, by2, bz1, bz2, ntfb, nntf, ssx, ssy, ssz;
+    int dopml, doplate, doB0, lk_mode, plate_lo, plate_up, nprobes, tsteps;
+    int chunk;           // planes per CTA along x
+    // coefficients
+    float c1h, chx, chy, chz, c2h;           // c2h/dx ...
+    float c1e0, c2e0, cex, cey, cez;         // c2e0/dx ...
+    float c1s, c2s, csx, csy, csz;           // sphere (doplate == 2)
+    float dtf, c0di;                         // dt, 2*E0*dt
+    double platesize;
+    float Bh[2 * kMaxPml], Ahx[2 * kMaxPml], Ahy[2 * kMaxPml], Ahz[2 * kMaxPml];
+    float Be[2 * kMaxPml], Aex[2 * kMaxPml], Aey[2 * kMaxPml], Aez[2 * kMaxPml];
+    // state
+    float *E[2][3], *H[2][3], *J[3];
+    float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
+    float *Pe[6];        // E psi: xy, xz, yx, yz, zx, zy
+    float *inc[2][4];    // 1-D line: Eyinc, Ezinc, Hyinc, Hzinc
+    float *incP[2][4];   // 1-D psi: PeyxI, PezxI, PhyxI, PhzxI
+    const float *wq2;    // E0 * wp2^2 per (i,j)
+    const float *nu2;    // nu2 per (i,j)
+    const float *G, *G2; // z-Gaussian and its square per k
+    const float *lk;     // Lee-Kalluri table (18 per entry)
+    const float *src;    // [tsteps][2]
+    const double *phase; // [tsteps][nntf][2]
+    const double *xc, *yc, *zc;
+    double *ntf[24];
+    double *probe;       // [6][tsteps][nprobes]
+    const int *probe_ijk;
+    float *slE, *slH;
+    unsigned int *err;   // bit 0: a TMA wait ran out
+};
+
+// ---------------------------------------------------------------------------
+// PTX helpers: mbarrier and TMA
+__device__ __forceinline__ unsigned smem_u32(const void *p) {
+    return (unsigned)__cvta_generic_to_shared(p);
 }
-int Fp32Sim::step(int, bool, void *, void *const *) { return 0; }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arm(uint64_t *bar, unsigned tx) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(tx)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ uint64_t globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: gives up after ~2 s of wall time.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    if (mbar_test(bar, parity)) return true;
+    const uint64_t t0 = globaltimer();
+    for (;;) {
+        if (mbar_test(bar, parity)) return true;
+        if (globaltimer() - t0 > 2000000000ull) return false;
+    }
+}
+__device__ __forceinline__ void tma3(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                     uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+        "%3, %4}], [%5];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ int hslab(int n, int N, int L, int shift) {
+    if (n < L) return n;
+    if (n >= N - L - 1 && n < N - 1) return n - shift;
+    return -1;
+}
+__device__ __forceinline__ int eslab(int n, int N, int L, int shift) {
+    if (n >= 1 && n < L + 1) return n - 1;
+    if (n >= N - L - 1 && n < N - 1) return n - shift;
+    return -1;
+}
+
+// Views of one stage.
+struct Stage {
+    float *e[3], *h[3], *j[3];
+};
+__device__ __forceinline__ Stage stage_at(unsigned char *base) {
+    Stage s;
+    for (int c = 0; c < 3; c++) {
+        s.e[c] = (float *)(base + c * E_B);
+        s.h[c] = (float *)(base + 3 * E_B + c * H_B);
+        s.j[c] = (float *)(base + 3 * E_B + 3 * H_B + c * J_B);
+    }
+    return s;
+}
+// E box element at (j,k) relative to the tile origin: row j - (j0-1), col k - (k0-4)
+#define EIDX(dj, dk) (((dj) + 1) * EK + (dk) + 4)
+#define HIDX(dj, dk) (((dj) + 1) * HK + (dk) + 4)
+#define HN(c, dj, dk) hn[((c) * HJ + (dj) + 1) * HN_COLS + (dk) + 1]
+
+struct HVal {
+    float x, y, z;
+};
+
+// H half-step of one cell (source/meteor-2.1.cpp:656-937 in FP32).  `dj,dk`
+// are relative to the tile origin; the E box of the plane and of the next
+// plane, and the old H box, are in shared memory.  Components outside their
+// update domain keep their old value.  `store_psi` is false for halo cells
+// computed on behalf of a neighbouring tile.
+__device__ __forceinline__ HVal h_cell(const Args &a, int par, int i, int j, int k, int dj, int dk,
+                                       const Stage &s, const Stage &s1, bool has_next,
+                                       bool store_psi, bool want_x, bool want_y, bool want_z) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
+    HVal o;
+    o.x = s.h[0][HIDX(dj, dk)];
+    o.y = s.h[1][HIDX(dj, dk)];
+    o.z = s.h[2][HIDX(dj, dk)];
+    const float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
+    const float *rd[6];
+    float *wr[6];
+    for (int q = 0; q < 6; q++) { rd[q] = a.Ph[par][q]; wr[q] = a.Ph[par ^ 1][q]; }
+    const bool inbx = i >= a.bx1 && i < a.bx2, inby = j >= a.by1 && j < a.by2,
+               inbz = k >= a.bz1 && k < a.bz2;
+    if (want_x && j < Ny - 1 && k < Nz - 1) {
+        const float dEz = s.e[2][EIDX(dj + 1, dk)] - ez;
+        const float dEy = s.e[1][EIDX(dj, dk + 1)] - ey;
+        float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
+        if (inbx && inbz) {
+            const float ezi = a.inc[par][1][i];
+            if (j == a.by1 - 1) h += a.chy * ezi;
+            if (j == a.by2 - 1) h -= a.chy * ezi;
+        }
+        if (inbx && inby) {
+            const float eyi = a.inc[par][0][i];
+            if (k == a.bz1 - 1) h -= a.chz * eyi;
+            if (k == a.bz2 - 1) h += a.chz * eyi;
+        }
+        if (a.dopml) {
+            const int sy = hslab(j, Ny, L, a.yshift);
+            if (sy >= 0) {
+                const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                const float p = a.Bh[sy] * rd[0][o2] + a.Ahy[sy] * dEz;
+                if (store_psi) wr[0][o2] = p;
+                h -= a.c2h * p;
+            }
+            const int sz = hslab(k, Nz, L, a.zshift);
+            if (sz >= 0) {
+                const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                const float p = a.Bh[sz] * rd[1][o2] + a.Ahz[sz] * dEy;
+                if (store_psi) wr[1][o2] = p;
+                h += a.c2h * p;
+            }
+        }
+        o.x = h;
+    }
+    if (want_y && i < Nx - 1 && k < Nz - 1 && has_next) {
+        const float dEx = s.e[0][EIDX(dj, dk + 1)] - ex;
+        const float dEz = s1.e[2][EIDX(dj, dk)] - ez;
+        float h = a.c1h * o.y - (a.chz * dEx - a.chx * dEz);
+        if (inby && inbz) {
+            if (i == a.bx1 - 1) h -= a.chx * a.inc[par][1][a.bx1];
+            if (i == a.bx2 - 1) h += a.chx * a.inc[par][1][a.bx2 - 1];
+        }
+        if (a.dopml) {
+            const int sx = hslab(i, Nx, L, a.xshift);
+            if (sx >= 0) {
+                const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
+                const float p = a.Bh[sx] * rd[2][o2] + a.Ahx[sx] * dEz;
+                if (store_psi) wr[2][o2] = p;
+                h += a.c2h * p;
+            }
+            const int sz = hslab(k, Nz, L, a.zshift);
+            if (sz >= 0) {
+                const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                const float p = a.Bh[sz] * rd[3][o2] + a.Ahz[sz] * dEx;
+                if (store_psi) wr[3][o2] = p;
+                h -= a.c2h * p;
+            }
+        }
+        o.y = h;
+    }
+    if (want_z && i < Nx - 1 && j < Ny - 1 && has_next) {
+        const float dEy = s1.e[1][EIDX(dj, dk)] - ey;
+        const float dEx = s.e[0][EIDX(dj + 1, dk)] - ex;
+        float h = a.c1h * o.z - (a.chx * dEy - a.chy * dEx);
+        if (inby && inbz) {
+            if (i == a.bx1 - 1) h += a.chx * a.inc[par][0][a.bx1];
+            if (i == a.bx2 - 1) h -= a.chx * a.inc[par][0][a.bx2 - 1];
+        }
+        if (a.dopml) {
+            const int sx = hslab(i, Nx, L, a.xshift);
+            if (sx >= 0) {
+                const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
+                const float p = a.Bh[sx] * rd[4][o2] + a.Ahx[sx] * dEy;
+                if (store_psi) wr[4][o2] = p;
+                h -= a.c2h * p;
+            }
+            const int sy = hslab(j, Ny, L, a.yshift);
+            if (sy >= 0) {
+                const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                const float p = a.Bh[sy] * rd[5][o2] + a.Ahy[sy] * dEx;
+                if (store_psi) wr[5][o2] = p;
+                h += a.c2h * p;
+            }
+        }
+        o.z = h;
+    }
+    return o;
+}
+
+// Incident-line H value of this step at index i (the 1-D update of
+// source/meteor-2.1.cpp:833, 892 without the +x CPML term, which never
+// reaches the TF/SF planes).
+__device__ __forceinline__ float hyinc_new(const Args &a, int par, int i) {
+    const float *ez = a.inc[par][1];
+    return a.c1h * a.inc[par][2][i] + a.chx * (ez[i + 1] - ez[i]);
+}
+__device__ __forceinline__ float hzinc_new(const Args &a, int par, int i) {
+    const float *ey = a.inc[par][0];
+    return a.c1h * a.inc[par][3][i] - a.chx * (ey[i + 1] - ey[i]);
+}
+
+// The whole 1-D incident line for this step, written to set par^1 (one CTA).
+__device__ void line_update(const Args &a, int par, int t) {
+    const int Nx = a.Nx, L = a.L;
+    const float *ey = a.inc[par][0], *ez = a.inc[par][1], *hy = a.inc[par][2], *hz = a.inc[par][3];
+    float *ey2 = a.inc[par ^ 1][0], *ez2 = a.inc[par ^ 1][1], *hy2 = a.inc[par ^ 1][2],
+          *hz2 = a.inc[par ^ 1][3];
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) {
+        float vy = hy[i], vz = hz[i];
+        if (i < Nx - 1) {
+            vy = a.c1h * hy[i] + a.chx * (ez[i + 1] - ez[i]);
+            vz = a.c1h * hz[i] - a.chx * (ey[i + 1] - ey[i]);
+            if (a.dopml && i >= Nx - L - 1) {
+                const int s = i - a.xshift;
+                const float py = a.Bh[s] * a.incP[par][2][s] + a.Ahx[s] * (ez[i + 1] - ez[i]);
+                const float pz = a.Bh[s] * a.incP[par][3][s] + a.Ahx[s] * (ey[i + 1] - ey[i]);
+                a.incP[par ^ 1][2][s] = py;
+                a.incP[par ^ 1][3][s] = pz;
+                vy += a.c2h * py;
+                vz -= a.c2h * pz;
+            }
+        }
+        hy2[i] = vy;
+        hz2[i] = vz;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < Nx; i += blockDim.x) {
+        float vy = ey[i], vz = ez[i];
+        if (i >= 1 && i < Nx - 1) {
+            vy = a.c1e0 * ey[i] - a.cex * (hz2[i] - hz2[i - 1]);
+            vz = a.c1e0 * ez[i] + a.cex * (hy2[i] - hy2[i - 1]);
+            if (a.dopml && i >= Nx - L - 1) {
+                const int s = i - a.xshift;
+                const float py = a.Be[s] * a.incP[par][0][s] + a.Aex[s] * (hz2[i] - hz2[i - 1]);
+                const float pz = a.Be[s] * a.incP[par][1][s] + a.Aex[s] * (hy2[i] - hy2[i - 1]);
+                a.incP[par ^ 1][0][s] = py;
+                a.incP[par ^ 1][1][s] = pz;
+                vy -= a.c2e0 * py;
+                vz += a.c2e0 * pz;
+            }
+        } else if (i == 0) {
+            vz = a.src[2 * t];
+            vy = a.src[2 * t + 1];
+        }
+        ey2[i] = vy;
+        ez2[i] = vz;
+    }
+}
+
+__device__ __forceinline__ void acc2(double *A, double *B, size_t base, double va, double vb,
+                                     const double *ph, int nf) {
+    for (int m = 0; m < nf; m++) {
+        const double s = ph[2 * m], c = ph[2 * m + 1];
+        A[base + 2 * m] += va * s;
+        A[base + 2 * m + 1] += va * c;
+        B[base + 2 * m] += vb * s;
+        B[base + 2 * m + 1] += vb * c;
+    }
+}
+
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(NTHREADS, 2)
+    k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // TMA destinations must be 128-byte aligned; the launch reserves 128 spare bytes.
+    unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+    float *hn = (float *)(smem + NS * STAGE_B);
+    uint64_t *bar = (uint64_t *)(smem + NS * STAGE_B + align128(HN_B));
+
+    const int par = t & 1;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, Nzp = a.Nzp, L = a.L;
+    const int k0 = blockIdx.x * TK, j0 = blockIdx.y * TJ;
+    const int i_begin = blockIdx.z * a.chunk;
+    const int i_end = min(Nx, i_begin + a.chunk);
+    if (i_begin >= Nx) return;
+    const int p0 = max(i_begin - 1, 0);
+    const int q_last = min(i_end, Nx - 1);  // last plane loaded
+    const size_t plane = (size_t)Ny * Nzp;
+
+    const bool first_cta = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
+    if (first_cta) line_update(a, par, t);
+
+    // Probes of the previous step from the read set (source/meteor-2.1.cpp:1443-1455).
+    if (first_cta && t > 0 && warp == 9 && lane >= 8 && lane - 8 < a.nprobes) {
+        const int pidx = lane - 8;
+        const int ix = a.probe_ijk[3 * pidx], iy = a.probe_ijk[3 * pidx + 1], iz = a.probe_ijk[3 * pidx + 2];
+        const size_t sI = plane, sJ = Nzp;
+        const size_t c = ix * sI + iy * sJ + iz;
+        const float *E0 = a.E[par][0], *E1 = a.E[par][1], *E2 = a.E[par][2];
+        const float *H0 = a.H[par][0], *H1 = a.H[par][1], *H2 = a.H[par][2];
+        const size_t o = (size_t)(t - 1) * a.nprobes + pidx, T = (size_t)a.tsteps * a.nprobes;
+        a.probe[o] = 0.5 * ((double)E0[c] + E0[c - sI]);
+        a.probe[T + o] = 0.5 * ((double)E1[c] + E1[c - sJ]);
+        a.probe[2 * T + o] = 0.5 * ((double)E2[c] + E2[c - 1]);
+        a.probe[3 * T + o] = 0.25 * ((double)H0[c] + H0[c - sJ] + H0[c - 1] + H0[c - sJ - 1]);
+        a.probe[4 * T + o] = 0.25 * ((double)H1[c] + H1[c - sI] + H1[c - 1] + H1[c - sI - 1]);
+        a.probe[5 * T + o] = 0.25 * ((double)H2[c] + H2[c - sJ] + H2[c - sI] + H2[c - sI - sJ]);
+    }
+
+    if (tid == PROD) {
+        for (int s = 0; s < NS; s++) mbar_init(&bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    auto issue = [&](int q) {
+        const int slot = (q - p0) % NS;
+        unsigned char *base = smem + slot * STAGE_B;
+        Stage st = stage_at(base);
+        mbar_arm(&bar[slot], STAGE_TX);
+        for (int c = 0; c < 3; c++) {
+            tma3(st.e[c], &maps.E[par][c], k0 - 4, j0 - 1, q, &bar[slot]);
+            tma3(st.h[c], &maps.H[par][c], k0 - 4, j0 - 1, q, &bar[slot]);
+            tma3(st.j[c], &maps.J[c], k0, j0, q, &bar[slot]);
+        }
+    };
+    int issued = p0 - 1;  // last plane whose copies were issued (producer's view)
+    if (tid == PROD) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int q = p0; q <= q_last && q < p0 + NS; q++) { issue(q); issued = q; }
+    }
+
+    // role of this thread
+    const bool tile = warp < TJ;
+    const int dj = tile ? warp : (warp == TJ ? -1 : lane);
+    const int dk = tile ? lane : (warp == TJ ? lane : -1);
+    const int j = j0 + dj, k = k0 + dk;
+    const bool role_ok = tile || warp == TJ || (warp == TJ + 1 && lane < TJ);
+    const bool in_grid = role_ok && j >= 0 && j < Ny && k >= 0 && k < Nz;
+    const bool valid = tile && in_grid;
+
+    // Lee-Kalluri matrices for this k (LK_PER_K) in registers
+    float lkm[18];
+    if (a.doB0 && a.lk_mode == LK_PER_K && valid)
+        for (int q = 0; q < 18; q++) lkm[q] = a.lk[(size_t)k * 18 + q];
+    const float Gk = valid ? a.G[k] : 0.f, G2k = valid ? a.G2[k] : 0.f;
+
+    float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
+    bool failed = false;
+    int fail_q = 0;
+    const int nf = a.nntf;
+    const double *ph = a.phase + (size_t)t * nf * 2;
+
+    for (int q = p0; q < i_end; q++) {
+        const int i = q;
+        const int slot = (q - p0) % NS;
+        const unsigned parity = ((q - p0) / NS) & 1;
+        const bool has_next = q + 1 <= q_last;
+        bool ok = mbar_wait(&bar[slot], parity);
+        if (has_next) ok = ok && mbar_wait(&bar[(q + 1 - p0) % NS], ((q + 1 - p0) / NS) & 1);
+        if (__syncthreads_or(!ok)) { failed = true; fail_q = q; break; }
+        const Stage s = stage_at(smem + slot * STAGE_B);
+        const Stage s1 = stage_at(smem + ((q + 1 - p0) % NS) * STAGE_B);
+        const bool real = q >= i_begin;
+        const size_t cg = (size_t)i * plane + (size_t)j * Nzp + k;
+
+        // ---- J of the previous step (lagged), source/meteor-fork.cpp:1523-1595
+        float jx = 0.f, jy = 0.f, jz = 0.f;
+        if (valid && real) {
+            jx = s.j[0][dj * TK + dk];
+            jy = s.j[1][dj * TK + dk];
+            jz = s.j[2][dj * TK + dk];
+            if (t > 0 && i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1) {
+                const float exc = s.e[0][EIDX(dj, dk)], eyc = s.e[1][EIDX(dj, dk)],
+                            ezc = s.e[2][EIDX(dj, dk)];
+                const size_t ij = (size_t)i * Ny + j;
+                if (!a.doB0) {
+                    const float nue = a.doplate ? 0.f : a.nu2[ij] * Gk;
+                    const float wq = a.doplate ? 0.f : a.wq2[ij] * G2k;
+                    const float den = 2.f + nue * a.dtf;
+                    const float ca = (2.f - nue * a.dtf) / den;
+                    const float cb = (2.f * a.dtf) * wq / den;
+                    jx = ca * jx + cb * exc;
+                    jy = ca * jy + cb * eyc;
+                    jz = ca * jz + cb * ezc;
+                } else {
+                    const float m0 = 0.5f * (exc + ex_prev);
+                    const float m1 = 0.5f * (eyc + s.e[1][EIDX(dj - 1, dk)]);
+                    const float m2 = 0.5f * (ezc + s.e[2][EIDX(dj, dk - 1)]);
+                    const float wq = a.doplate ? 0.f : a.wq2[ij] * G2k;
+                    const float *m = lkm;
+                    float tbl[18];
+                    if (a.lk_mode != LK_PER_K) {
+                        const size_t e = a.lk_mode == LK_PER_IJ ? ij : cg;
+                        for (int u = 0; u < 18; u++) tbl[u] = a.lk[e * 18 + u];
+                        m = tbl;
+                    }
+                    const float nx = m[0] * jx + m[1] * jy + m[2] * jz + wq * (m[9] * m0 + m[10] * m1 + m[11] * m2);
+                    const float ny = m[3] * jx + m[4] * jy + m[5] * jz + wq * (m[12] * m0 + m[13] * m1 + m[14] * m2);
+                    const float nz = m[6] * jx + m[7] * jy + m[8] * jz + wq * (m[15] * m0 + m[16] * m1 + m[17] * m2);
+                    jx = nx; jy = ny; jz = nz;
+                }
+            }
+        }
+
+        // ---- H of this plane: tile (all comps), halo row (Hx, Hz), halo column (Hx, Hy)
+        HVal hv = {0.f, 0.f, 0.f};
+        if (in_grid) {
+            hv = h_cell(a, par, i, j, k, dj, dk, s, s1, has_next, tile && real,
+                        true, warp != TJ, warp != TJ + 1);
+        }
+        if (role_ok) {
+            HN(0, dj, dk) = hv.x;
+            if (warp != TJ) HN(1, dj, dk) = hv.y;
+            if (warp != TJ + 1) HN(2, dj, dk) = hv.z;
+        }
+        if (valid && real) {
+            a.H[par ^ 1][0][cg] = hv.x;
+            a.H[par ^ 1][1][cg] = hv.y;
+            a.H[par ^ 1][2][cg] = hv.z;
+        }
+        __syncthreads();
+
+        // ---- E of this plane (tile), source/meteor-2.1.cpp:1020-1374
+        if (valid && real) {
+            const bool sphere = a.doplate == 2 && [&] {
+                const double x = a.xc[i], y = a.yc[j], z = a.zc[k];
+                return sqrt(x * x + y * y + z * z) < a.platesize;
+            }();
+            const float c1 = sphere ? a.c1s : a.c1e0, c2 = sphere ? a.c2s : a.c2e0;
+            const float cx = sphere ? a.csx : a.cex, cy = sphere ? a.csy : a.cey,
+                        cz = sphere ? a.csz : a.cez;
+            const bool plate_row = a.doplate == 1 && i == a.ssx;
+            float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
+            const float ex_old = ex;
+            // Ex
+            if (i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1) {
+                const float dHz = hv.z - HN(2, dj - 1, dk);
+                const float dHy = hv.y - HN(1, dj, dk - 1);
+                float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
+                if (i >= a.bx1 && i < a.bx2 - 1) {
+                    if (j >= a.by1 && j < a.by2) {
+                        if (k == a.bz1) e += a.cez * hyinc_new(a, par, i);
+                        if (k == a.bz2) e -= a.cez * hyinc_new(a, par, i);
+                    }
+                    if (k >= a.bz1 && k < a.bz2) {
+                        if (j == a.by1) e -= a.cey * hzinc_new(a, par, i);
+                        if (j == a.by2) e += a.cey * hzinc_new(a, par, i);
+                    }
+                }
+                if (a.dopml) {
+                    const int sy = eslab(j, Ny, L, a.yshift);
+                    if (sy >= 0) {
+                        const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                        const float p = a.Be[sy] * a.Pe[0][o2] + a.Aey[sy] * dHz;
+                        a.Pe[0][o2] = p;
+                        e += a.c2e0 * p;
+                    }
+                    const int sz = eslab(k, Nz, L, a.zshift);
+                    if (sz >= 0) {
+                        const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                        const float p = a.Be[sz] * a.Pe[1][o2] + a.Aez[sz] * dHy;
+                        a.Pe[1][o2] = p;
+                        e -= a.c2e0 * p;
+                    }
+                }
+                ex = e;
+            }
+            // Ey
+            const bool ey_plate = plate_row && j >= a.plate_lo && j < a.plate_up - 1 &&
+                                  k >= a.plate_lo && k < a.plate_up;
+            if (i >= 1 && i < Nx - 1 && k >= 1) {
+                const float dHx = hv.x - HN(0, dj, dk - 1);
+                const float dHz = hv.z - hz_prev;
+                float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
+                if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
+                    if (i == a.bx1) e += a.cex * hzinc_new(a, par, a.bx1 - 1);
+                    if (i == a.bx2 - 1) e -= a.cex * hzinc_new(a, par, a.bx2 - 1);
+                }
+                if (a.dopml) {
+                    const int sx = eslab(i, Nx, L, a.xshift);
+                    if (sx >= 0) {
+                        float p = 0.f;
+                        if (j < Ny - 1 && k < Nz - 1) {
+                            const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
+                            p = a.Be[sx] * a.Pe[2][o2] + a.Aex[sx] * dHz;
+                            a.Pe[2][o2] = p;
+                        }
+                        e -= a.c2e0 * p;
+                    }
+                    const int sz = eslab(k, Nz, L, a.zshift);
+                    if (sz >= 0) {
+                        float p = 0.f;
+                        if (j < Ny - 1) {
+                            const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                            p = a.Be[sz] * a.Pe[3][o2] + a.Aez[sz] * dHx;
+                            a.Pe[3][o2] = p;
+                        }
+                        e += a.c2e0 * p;
+                    }
+                }
+                ey = e;
+            }
+            if (ey_plate) ey = 0.f;
+            // Ez
+            const bool ez_plate = plate_row && j >= a.plate_lo && j < a.plate_up &&
+                                  k >= a.plate_lo && k < a.plate_up - 1;
+            float ez_slice = ez;
+            if (i >= 1 && i < Nx - 1 && j >= 1) {
+                const float dHy = hv.y - hy_prev;
+                const float dHx = hv.x - HN(0, dj - 1, dk);
+                float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
+                if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
+                    if (i == a.bx1) e -= a.cex * hyinc_new(a, par, a.bx1 - 1);
+                    if (i == a.bx2 - 1) e += a.cex * hyinc_new(a, par, a.bx2 - 1);
+                }
+                if (ez_plate) e = 0.f;
+                ez_slice = e;
+                if (a.dopml) {
+                    const int sx = eslab(i, Nx, L, a.xshift);
+                    if (sx >= 0) {
+                        float p = 0.f;
+                        if (j < Ny - 1 && k < Nz - 1) {
+                            const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
+                            p = a.Be[sx] * a.Pe[4][o2] + a.Aex[sx] * dHy;
+                            a.Pe[4][o2] = p;
+                        }
+                        e += a.c2e0 * p;
+                    }
+                    const int sy = eslab(j, Ny, L, a.yshift);
+                    if (sy >= 0 && k < Nz - 1) {
+                        const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                        const float p = a.Be[sy] * a.Pe[5][o2] + a.Aey[sy] * dHx;
+                        a.Pe[5][o2] = p;
+                        e -= a.c2e0 * p;
+                    }
+                }
+                ez = e;
+            } else if (ez_plate) {
+                ez = 0.f;
+                ez_slice = 0.f;
+            }
+            a.E[par ^ 1][0][cg] = ex;
+            a.E[par ^ 1][1][cg] = ey;
+            a.E[par ^ 1][2][cg] = ez;
+            a.J[0][cg] = jx;
+            a.J[1][cg] = jy;
+            a.J[2][cg] = jz;
+
+            // ---- running DFT on the Huygens surface (FP64 sums)
+            const int nb = a.ntfb;
+            const bool fr = i == nb, bk = i == Nx - nb, tp = j == Ny - nb, bt = j == nb,
+                       lf = k == nb, rt = k == Nz - nb;
+            if (fr || bk || tp || bt || lf || rt) {
+                const size_t n2 = 2 * (size_t)nf;
+                if (fr || bk) {
+                    const size_t base = ((size_t)j * Nz + k) * n2;
+                    const double hz = 0.5 * ((double)hv.z + hz_prev), hy = 0.5 * ((double)hv.y + hy_prev);
+                    if (fr) { acc2(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
+                    if (bk) { acc2(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
+                }
+                if (tp || bt) {
+                    const size_t base = ((size_t)i * Nz + k) * n2;
+                    const double hz = 0.5 * ((double)hv.z + HN(2, dj - 1, dk));
+                    const double hx = 0.5 * ((double)hv.x + HN(0, dj - 1, dk));
+                    if (tp) { acc2(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
+                    if (bt) { acc2(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
+                }
+                if (lf || rt) {
+                    const size_t base = ((size_t)i * Ny + j) * n2;
+                    const double hy = 0.5 * ((double)hv.y + HN(1, dj, dk - 1));
+                    const double hx = 0.5 * ((double)hv.x + HN(0, dj, dk - 1));
+                    if (lf) { acc2(a.ntf[18], a.ntf[19], base, hy, -hx, ph, nf); acc2(a.ntf[16], a.ntf[17], base, -(double)ey, ex, ph, nf); }
+                    if (rt) { acc2(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
+                }
+            }
+
+            // ---- slices on record steps
+            if (record) {
+                const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
+                if (k == a.ssz) {
+                    a.slE[oz + (size_t)i * Ny + j] = ey;
+                    a.slE[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] = ez_slice;
+                    if (j < Ny - 1) {
+                        a.slH[oz + (size_t)i * Ny + j] = hv.y;
+                        a.slH[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] = hv.z;
+                    }
+                }
+                if (j == a.ssy) {
+                    a.slE[oy + (size_t)i * Nz + k] = ey;
+                    a.slE[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] = ez_slice;
+                    if (k < Nz - 1) {
+                        a.slH[oy + (size_t)i * Nz + k] = hv.y;
+                        a.slH[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] = hv.z;
+                    }
+                }
+                if (i == a.ssx) {
+                    a.slE[ox + (size_t)j * Nz + k] = ey;
+                    a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = ez_slice;
+                    if (j < Ny - 1 && k < Nz - 1) {
+                        a.slH[ox + (size_t)j * Nz + k] = hv.y;
+                        a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = hv.z;
+                    }
+                }
+            }
+            ex_prev = ex_old;
+        } else if (valid) {
+            ex_prev = s.e[0][EIDX(dj, dk)];  // warm-up plane
+        }
+        hy_prev = hv.y;
+        hz_prev = hv.z;
+        __syncthreads();
+        if (tid == PROD && q + NS <= q_last) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q + NS);
+            issued = q + NS;
+        }
+    }
+
+    if (failed && tid == PROD) {
+        atomicOr(a.err, 1u);
+        // Let the copies already issued land (bounded) before the CTA exits.
+        for (int qq = fail_q; qq <= issued; qq++) {
+            const int sl = (qq - p0) % NS;
+            const unsigned pp = ((qq - p0) / NS) & 1;
+            const uint64_t t0 = globaltimer();
+            while (!mbar_test(&bar[sl], pp) && globaltimer() - t0 < 200000000ull) {
+            }
+        }
+    }
+}
+
+// E probes of the final step (the per-step ones ride in the next pass).
+__global__ void k_fp32_flush(const Args a, int t_last) {
+    const int p = threadIdx.x;
+    if (p >= a.nprobes) return;
+    const int par = (t_last + 1) & 1;  // set written by the last pass
+    const size_t sI = (size_t)a.Ny * a.Nzp, sJ = a.Nzp;
+    const int ix = a.probe_ijk[3 * p], iy = a.probe_ijk[3 * p + 1], iz = a.probe_ijk[3 * p + 2];
+    const size_t c = ix * sI + iy * sJ + iz;
+    const float *E0 = a.E[par][0], *E1 = a.E[par][1], *E2 = a.E[par][2];
+    const float *H0 = a.H[par][0], *H1 = a.H[par][1], *H2 = a.H[par][2];
+    const size_t o = (size_t)t_last * a.nprobes + p, T = (size_t)a.tsteps * a.nprobes;
+    a.probe[o] = 0.5 * ((double)E0[c] + E0[c - sI]);
+    a.probe[T + o] = 0.5 * ((double)E1[c] + E1[c - sJ]);
+    a.probe[2 * T + o] = 0.5 * ((double)E2[c] + E2[c - 1]);
+    a.probe[3 * T + o] = 0.25 * ((double)H0[c] + H0[c - sJ] + H0[c - 1] + H0[c - sJ - 1]);
+    a.probe[4 * T + o] = 0.25 * ((double)H1[c] + H1[c - sI] + H1[c - 1] + H1[c - sI - 1]);
+    a.probe[5 * T + o] = 0.25 * ((double)H2[c] + H2[c - sJ] + H2[c - sI] + H2[c - sI - sJ]);
+}
+
+// max |Ex| (record steps) and the non-finite guard, over the padded grid.
+__global__ void __launch_bounds__(256) k_fp32_scan(const float *__restrict__ ex,
+                                                   const float *__restrict__ ey,
+                                                   const float *__restrict__ ez, size_t n,
+                                                   unsigned int *maxbits, unsigned int *bad) {
+    float m = 0.f;
+    unsigned int nb = 0;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const float a = ex[q];
+        const float v = fabsf(a);
+        if (v > m) m = v;
+        nb |= !isfinite(a) | !isfinite(ey[q]) | !isfinite(ez[q]);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+        nb |= __shfl_down_sync(0xffffffffu, nb, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(maxbits, __float_as_uint(m));
+        if (nb) atomicOr(bad, 1u);
+    }
+}
+
+// Copy one slice/field buffer of floats to doubles.
+__global__ void k_f2d(const float *__restrict__ in, double *__restrict__ out, size_t n) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x)
+        out[q] = in[q];
+}
+
+// Unpadded [Nx][Ny][Nz] view of a padded [Nx][Ny][Nzp] component.
+__global__ void k_unpad(const float *__restrict__ in, double *__restrict__ out, int Nx, int Ny,
+                        int Nz, int Nzp) {
+    const size_t n = (size_t)Nx * Ny * Nz;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const size_t k = q % Nz, ij = q / Nz;
+        out[q] = in[ij * Nzp + k];
+    }
+}
+
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                              CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                              CUtensorMapFloatOOBfill);
+
+EncodeFn encoder() {
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            throw Error(MFDTD_ECUDA, "cuTensorMapEncodeTiled is not available");
+        fn = (EncodeFn)p;
+    }
+    return fn;
+}
+
+void make_map(CUtensorMap *m, float *base, int Nx, int Ny, int Nz, int Nzp, int bk, int bj) {
+    cuuint64_t dims[3] = {(cuuint64_t)Nz, (cuuint64_t)Ny, (cuuint64_t)Nx};
+    cuuint64_t strides[2] = {(cuuint64_t)Nzp * 4, (cuuint64_t)Ny * Nzp * 4};
+    cuuint32_t box[3] = {(cuuint32_t)bk, (cuuint32_t)bj, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = encoder()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(MFDTD_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
+void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw Error(MFDTD_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+}  // namespace
+
+struct Fp32Sim::Impl {
+    Args a;
+    Maps maps;
+    std::vector<void *> allocs;
+    int64_t bytes = 0;
+    int Nx = 0, Ny = 0, Nz = 0, Nzp = 0, tsteps = 0, nntf = 0, nprobes = 0;
+    size_t slice_len = 0;
+    dim3 grid;
+    double *dtmp = nullptr;      // FP64 staging for conversions
+    size_t dtmp_len = 0;
+    unsigned int *scan = nullptr;  // [0] max|Ex| bits, [1] bad flag
+
+    template <class T> T *alloc(size_t n, cudaStream_t s) {
+        void *p = nullptr;
+        size_t b = std::max<size_t>(n, 1) * sizeof(T);
+        ck(cudaMalloc(&p, b), "cudaMalloc");
+        allocs.push_back(p);
+        bytes += (int64_t)b;
+        ck(cudaMemsetAsync(p, 0, b, s), "cudaMemset");
+        return (T *)p;
+    }
+    template <class T> T *upload(const std::vector<T> &v, cudaStream_t s) {
+        T *d = alloc<T>(v.size(), s);
+        if (!v.empty()) ck(cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s), "H2D");
+        return d;
+    }
+    ~Impl() {
+        for (void *p : allocs) cudaFree(p);
+    }
+};
+
+int64_t Fp32Sim::footprint(const Problem &P) {
+    const int64_t Nzp = (P.Nz + TK - 1) / TK * TK;
+    const int64_t cells = (int64_t)P.Nx * P.Ny * Nzp;
+    const int64_t L2 = 2 * P.L;
+    const int64_t psi = P.dopml ? (L2 * P.Ny * P.Nz + (int64_t)P.Nx * L2 * P.Nz + (int64_t)P.Nx * P.Ny * L2) * 2 : 0;
+    const int64_t nf2 = 2 * P.nntf();
+    const int64_t ntf = 8 * nf2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz + (int64_t)P.Nx * P.Ny);
+    return cells * 4 * 15 + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2);
+}
+
+void Fp32Sim::init(const Problem &P, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (P.doB0 && P.lk_mode == LK_PER_CELL)
+        throw Error(MFDTD_EINVAL, "FP32 form: collision frequency varying along all three axes "
+                                  "is not supported (use the FP64 plain form)");
+    if (P.L > kMaxPml) throw Error(MFDTD_EINVAL, "CPML too thick");
+    impl_ = new Impl();
+    Impl &m = *impl_;
+    Args &a = m.a;
+    std::memset(&a, 0, sizeof a);
+    m.Nx = P.Nx; m.Ny = P.Ny; m.Nz = P.Nz; m.Nzp = (P.Nz + TK - 1) / TK * TK;
+    m.tsteps = P.tsteps; m.nntf = P.nntf(); m.nprobes = P.nprobes();
+    if (m.nprobes > 24) throw Error(MFDTD_EINVAL, "FP32 form supports at most 24 probes");
+    a.Nx = P.Nx; a.Ny = P.Ny; a.Nz = P.Nz; a.Nzp = m.Nzp; a.L = P.L;
+    a.xshift = P.xshift; a.yshift = P.yshift; a.zshift = P.zshift;
+    a.bx1 = P.bx1; a.bx2 = P.bx2; a.by1 = P.by1; a.by2 = P.by2; a.bz1 = P.bz1; a.bz2 = P.bz2;
+    a.ntfb = P.ntfb; a.nntf = P.nntf(); a.ssx = P.ssx; a.ssy = P.ssy; a.ssz = P.ssz;
+    a.dopml = P.dopml; a.doplate = P.doplate; a.doB0 = P.doB0; a.lk_mode = P.lk_mode;
+    a.plate_lo = P.plate_lo; a.plate_up = P.plate_up; a.nprobes = P.nprobes(); a.tsteps = P.tsteps;
+    a.c1h = (float)P.c1h; a.c2h = (float)P.c2h;
+    a.chx = (float)(P.c2h / P.dx); a.chy = (float)(P.c2h / P.dy); a.chz = (float)(P.c2h / P.dz);
+    a.c1e0 = (float)P.c1e0; a.c2e0 = (float)P.c2e0;
+    a.cex = (float)(P.c2e0 / P.dx); a.cey = (float)(P.c2e0 / P.dy); a.cez = (float)(P.c2e0 / P.dz);
+    a.c1s = (float)P.c1s; a.c2s = (float)P.c2s;
+    a.csx = (float)(P.c2s / P.dx); a.csy = (float)(P.c2s / P.dy); a.csz = (float)(P.c2s / P.dz);
+    a.dtf = (float)P.dt; a.c0di = (float)(2 * kE0 * P.dt);
+    a.platesize = P.platesize;
+    for (int q = 0; q < 2 * P.L; q++) {
+        a.Bh[q] = (float)P.Bh[q];
+        a.Ahx[q] = (float)(P.Ah[q] / P.dx); a.Ahy[q] = (float)(P.Ah[q] / P.dy); a.Ahz[q] = (float)(P.Ah[q] / P.dz);
+        a.Be[q] = (float)P.Be[q];
+        a.Aex[q] = (float)(P.Ae[q] / P.dx); a.Aey[q] = (float)(P.Ae[q] / P.dy); a.Aez[q] = (float)(P.Ae[q] / P.dz);
+    }
+    const size_t NC = (size_t)P.Nx * P.Ny * m.Nzp;
+    for (int b = 0; b < 2; b++)
+        for (int c = 0; c < 3; c++) {
+            a.E[b][c] = m.alloc<float>(NC, s);
+            a.H[b][c] = m.alloc<float>(NC, s);
+        }
+    for (int c = 0; c < 3; c++) a.J[c] = m.alloc<float>(NC, s);
+    const size_t L2 = 2 * (size_t)P.L;
+    const size_t nxs = L2 * P.Ny * P.Nz, nys = (size_t)P.Nx * L2 * P.Nz, nzs = (size_t)P.Nx * P.Ny * L2;
+    const size_t psz[6] = {nys, nzs, nxs, nzs, nxs, nys};  // xy, xz, yx, yz, zx, zy
+    if (P.dopml) {
+        for (int q = 0; q < 6; q++) {
+            a.Ph[0][q] = m.alloc<float>(psz[q], s);
+            a.Ph[1][q] = m.alloc<float>(psz[q], s);
+            a.Pe[q] = m.alloc<float>(psz[q], s);
+        }
+    }
+    for (int b = 0; b < 2; b++)
+        for (int q = 0; q < 4; q++) {
+            a.inc[b][q] = m.alloc<float>(P.Nx + 1, s);
+            a.incP[b][q] = m.alloc<float>(L2, s);
+        }
+    {
+        std::vector<float> wq2(P.wp2e.size()), nu2(P.nu2e.size()), G(P.Nz), G2(P.Nz);
+        for (size_t q = 0; q < wq2.size(); q++) wq2[q] = (float)(kE0 * P.wp2e[q] * P.wp2e[q]);
+        for (size_t q = 0; q < nu2.size(); q++) nu2[q] = (float)P.nu2e[q];
+        for (int k = 0; k < P.Nz; k++) { G[k] = (float)P.G[k]; G2[k] = (float)(P.G[k] * P.G[k]); }
+        a.wq2 = m.upload(wq2, s); a.nu2 = m.upload(nu2, s); a.G = m.upload(G, s); a.G2 = m.upload(G2, s);
+        std::vector<float> lk(P.lk.begin(), P.lk.end());
+        a.lk = m.upload(lk, s);
+        std::vector<float> src(P.src.begin(), P.src.end());
+        a.src = m.upload(src, s);
+    }
+    a.phase = m.upload(P.phase, s);
+    a.xc = m.upload(P.x, s); a.yc = m.upload(P.y, s); a.zc = m.upload(P.z, s);
+    const size_t nf2 = 2 * (size_t)P.nntf();
+    const size_t fb = (size_t)P.Ny * P.Nz * nf2, tb = (size_t)P.Nx * P.Nz * nf2, lr = (size_t)P.Nx * P.Ny * nf2;
+    for (int q = 0; q < 24; q++) a.ntf[q] = m.alloc<double>(q < 8 ? fb : q < 16 ? tb : lr, s);
+    a.probe = m.alloc<double>((size_t)6 * P.tsteps * P.nprobes(), s);
+    std::vector<int> ijk;
+    for (int n = 0; n < P.nprobes(); n++) { ijk.push_back(P.probex[n]); ijk.push_back(P.probey[n]); ijk.push_back(P.probez[n]); }
+    a.probe_ijk = m.upload(ijk, s);
+    m.slice_len = 2 * ((size_t)P.Nx * P.Ny + (size_t)P.Nx * P.Nz + (size_t)P.Ny * P.Nz);
+    a.slE = m.alloc<float>(m.slice_len, s);
+    a.slH = m.alloc<float>(m.slice_len, s);
+    a.err = m.alloc<unsigned int>(1, s);
+    m.scan = m.alloc<unsigned int>(2, s);
+    m.dtmp_len = std::max(m.slice_len, (size_t)1);
+    m.dtmp = m.alloc<double>(m.dtmp_len, s);
+
+    for (int b = 0; b < 2; b++)
+        for (int c = 0; c < 3; c++) {
+            make_map(&m.maps.E[b][c], a.E[b][c], P.Nx, P.Ny, P.Nz, m.Nzp, EK, EJ);
+            make_map(&m.maps.H[b][c], a.H[b][c], P.Nx, P.Ny, P.Nz, m.Nzp, HK, HJ);
+        }
+    for (int c = 0; c < 3; c++) make_map(&m.maps.J[c], a.J[c], P.Nx, P.Ny, P.Nz, m.Nzp, TK, TJ);
+
+    ck(cudaFuncSetAttribute(k_fp32_step, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B),
+       "cudaFuncSetAttribute");
+    // Split x into chunks so that the grid fills the machine several times over.
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int tiles = (m.Nzp / TK) * ((P.Ny + TJ - 1) / TJ);
+    const int want = sms * 2 * 8;
+    int chunks = std::max(1, std::min(P.Nx / 16 > 0 ? P.Nx / 16 : 1, (want + tiles - 1) / tiles));
+    a.chunk = (P.Nx + chunks - 1) / chunks;
+    chunks = (P.Nx + a.chunk - 1) / a.chunk;
+    m.grid = dim3(m.Nzp / TK, (P.Ny + TJ - 1) / TJ, chunks);
+    bytes_ = m.bytes;
+}
+
 int Fp32Sim::kernel_classes() { return 1; }
-const char *Fp32Sim::kernel_name(int) { return "fp32_step"; }
-void Fp32Sim::record(double *, double *, double *, void *) {}
-double Fp32Sim::guard(void *) { return 0; }
-void Fp32Sim::flush(int, void *) {}
-void Fp32Sim::read_ntf(int, double *, void *) {}
-void Fp32Sim::read_probes(double *, void *) {}
-void Fp32Sim::read_field(int, double *, void *) {}
+const char *Fp32Sim::kernel_name(int) { return "k_fp32_step"; }
+
+int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
+    cudaStream_t s = (cudaStream_t)stream;
+    Impl &m = *impl_;
+    if (ev) cudaEventRecord((cudaEvent_t)ev[0], s);
+    k_fp32_step<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t, record ? 1 : 0);
+    if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
+    m_cur_ = (t + 1) & 1;
+    return 1;
+}
+
+void Fp32Sim::check(void *stream) {
+    unsigned int err = 0;
+    ck(cudaMemcpyAsync(&err, impl_->a.err, 4, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "D2H");
+    ck(cudaStreamSynchronize((cudaStream_t)stream), "sync");
+    if (err) throw Error(MFDTD_ETIMEOUT, "FP32 step: a TMA wait ran out (device error flag set)");
+}
+
+void Fp32Sim::record(double *E, double *H, double *emax, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    Impl &m = *impl_;
+    const size_t n = m.slice_len, Nx = m.Nx;
+    // After an odd number of passes the current state is in set 1, else set 0;
+    // the caller invokes this right after the step's pass, so the state is in
+    // the set that pass wrote.
+    const int cur = m_cur_;
+    ck(cudaMemsetAsync(m.scan, 0, 8, s), "memset");
+    const size_t NC = (size_t)m.Nx * m.Ny * m.Nzp;
+    k_fp32_scan<<<152 * 8, 256, 0, s>>>(m.a.E[cur][0], m.a.E[cur][1], m.a.E[cur][2], NC, m.scan, m.scan + 1);
+    unsigned int bits[2];
+    ck(cudaMemcpyAsync(bits, m.scan, 8, cudaMemcpyDeviceToHost, s), "D2H");
+    k_f2d<<<256, 256, 0, s>>>(m.a.slE, m.dtmp, n);
+    ck(cudaMemcpyAsync(E, m.dtmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    std::vector<float> inc(2 * Nx);
+    ck(cudaMemcpyAsync(inc.data(), m.a.inc[cur][0], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaMemcpyAsync(inc.data() + Nx, m.a.inc[cur][1], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    for (size_t q = 0; q < 2 * Nx; q++) E[n + q] = inc[q];
+    k_f2d<<<256, 256, 0, s>>>(m.a.slH, m.dtmp, n);
+    ck(cudaMemcpyAsync(H, m.dtmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaMemcpyAsync(inc.data(), m.a.inc[cur][2], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaMemcpyAsync(inc.data() + Nx, m.a.inc[cur][3], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    for (size_t q = 0; q < 2 * Nx; q++) H[n + q] = inc[q];
+    float f;
+    std::memcpy(&f, &bits[0], 4);
+    *emax = f;
+}
+
+double Fp32Sim::guard(void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    Impl &m = *impl_;
+    ck(cudaMemsetAsync(m.scan, 0, 8, s), "memset");
+    const size_t NC = (size_t)m.Nx * m.Ny * m.Nzp;
+    const int cur = m_cur_;
+    k_fp32_scan<<<152 * 8, 256, 0, s>>>(m.a.E[cur][0], m.a.E[cur][1], m.a.E[cur][2], NC, m.scan, m.scan + 1);
+    unsigned int bits[2];
+    ck(cudaMemcpyAsync(bits, m.scan, 8, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    check(stream);
+    return bits[1] ? 1.0 : 0.0;
+}
+
+void Fp32Sim::flush(int t_last, void *stream) {
+    Impl &m = *impl_;
+    if (m.nprobes <= 0) return;
+    k_fp32_flush<<<1, 32, 0, (cudaStream_t)stream>>>(m.a, t_last);
+}
+
+void Fp32Sim::read_ntf(int q, double *out, void *stream) {
+    Impl &m = *impl_;
+    const size_t nf2 = 2 * (size_t)m.nntf;
+    const size_t n = q < 8 ? (size_t)m.Ny * m.Nz * nf2 : q < 16 ? (size_t)m.Nx * m.Nz * nf2 : (size_t)m.Nx * m.Ny * nf2;
+    ck(cudaMemcpyAsync(out, m.a.ntf[q], n * 8, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "D2H");
+}
+
+void Fp32Sim::read_probes(double *out, void *stream) {
+    Impl &m = *impl_;
+    size_t n = (size_t)6 * m.tsteps * m.nprobes;
+    if (n) ck(cudaMemcpyAsync(out, m.a.probe, n * 8, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "D2H");
+}
+
+void Fp32Sim::read_field(int comp, double *out, void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    Impl &m = *impl_;
+    const int cur = m_cur_;
+    const float *src = comp < 3 ? m.a.E[cur][comp] : comp < 6 ? m.a.H[cur][comp - 3] : m.a.J[comp - 6];
+    const size_t n = (size_t)m.Nx * m.Ny * m.Nz;
+    double *tmp = nullptr;
+    ck(cudaMallocAsync((void **)&tmp, n * 8, s), "cudaMallocAsync");
+    k_unpad<<<1024, 256, 0, s>>>(src, tmp, m.Nx, m.Ny, m.Nz, m.Nzp);
+    ck(cudaMemcpyAsync(out, tmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaFreeAsync(tmp, s), "cudaFreeAsync");
+}
+
 Fp32Sim::~Fp32Sim() { delete impl_; }
 
 }  // namespace mfdtd

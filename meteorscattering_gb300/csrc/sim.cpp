@@ -304,6 +304,7 @@ struct mfdtd_sim {
         last_launches = launches;
         if (nsteps > 0) {
             wait();
+            if (f32) f32->check(stream);
             float ms = 0;
             mfdtd::ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
             last_ms_per_step = ms / nsteps;

@@ -1,0 +1,114 @@
+"""GPU: the FP32 fused form against the FP64 CPU oracle.
+
+Everything integer must match exactly (file sizes, headers, probe indices,
+number of record steps); floating-point outputs must agree within the stated
+relative-L2 tolerance.  FP32 storage and arithmetic over a few dozen steps
+gives errors of order 1e-6; the bound below leaves margin.
+"""
+import dataclasses
+import os
+
+import numpy as np
+import pytest
+
+import cases as golden_cases
+import helpers as H
+from meteorscattering_gb300 import engine as E
+from meteorscattering_gb300 import rundir as rd
+
+pytestmark = pytest.mark.gpu
+CASES = golden_cases.cases()
+TOL = 2e-4  # relative L2, FP32 fields / FP64 sums vs FP64 reference order
+
+
+def compare_fp32(da, db, p):
+    for name in H.OUTPUTS:
+        pa, pb = os.path.join(da, name), os.path.join(db, name)
+        assert os.path.exists(pa) == os.path.exists(pb), name
+        if os.path.exists(pa):
+            assert os.path.getsize(pa) == os.path.getsize(pb), name
+    na = rd.read_ntf(os.path.join(da, "output_NTF.dat"), p)
+    nb = rd.read_ntf(os.path.join(db, "output_NTF.dat"), p)
+    assert na["nntf"] == nb["nntf"] and na["ntfb"] == nb["ntfb"]
+    assert np.array_equal(na["fntf"], nb["fntf"])
+    faces_a = np.concatenate([na[n].ravel() for n, _ in rd.NTF_FACE_ORDER])
+    faces_b = np.concatenate([nb[n].ravel() for n, _ in rd.NTF_FACE_ORDER])
+    assert H.rel_l2(faces_a, faces_b) < TOL
+    for key in ("Eydft", "Ezdft"):
+        np.testing.assert_allclose(na[key], nb[key], rtol=1e-6, atol=1e-12)
+    if p.nprobes:
+        pa = rd.read_probes(os.path.join(da, "Probe.dat"), p.tsteps)
+        pb = rd.read_probes(os.path.join(db, "Probe.dat"), p.tsteps)
+        for key in ("probex", "probey", "probez"):
+            assert np.array_equal(pa[key], pb[key])
+        for key in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
+            if np.linalg.norm(pb[key]) > 0:
+                assert H.rel_l2(pa[key], pb[key]) < TOL, key
+    if p.savefields:
+        for fname, inc in (("output_E.dat", True), ("output_H.dat", True)):
+            ra = rd.read_slices(os.path.join(da, fname), p, inc)
+            rb = rd.read_slices(os.path.join(db, fname), p, inc)
+            assert len(ra) == len(rb)
+            for x, y in zip(ra, rb):
+                for key in x:
+                    if np.linalg.norm(y[key]) > 0:
+                        assert H.rel_l2(x[key], y[key]) < 10 * TOL, (fname, key)
+    la = rd.read_log_maxima(os.path.join(da, "log.txt"))
+    lb = rd.read_log_maxima(os.path.join(db, "log.txt"))
+    assert len(la) == len(lb)
+    np.testing.assert_allclose([float(v) for v in la], [float(v) for v in lb], rtol=1e-3, atol=1e-30)
+
+
+FP32_CASES = sorted(n for n in CASES if n != "lk_general")
+
+
+@pytest.mark.parametrize("name", FP32_CASES)
+def test_fp32_matches_oracle(built, tmp_path, name):
+    case = CASES[name]
+    da = H.fresh_dir(tmp_path, name + "_f32", case)
+    db = H.fresh_dir(tmp_path, name + "_orc", case)
+    E.run_rundir(da, form=E.FORM_FP32_FUSED)
+    H.run_oracle(db)
+    compare_fp32(da, db, case[0])
+
+
+def test_fp32_rejects_per_cell_collision_tables(built, tmp_path):
+    case = CASES["lk_general"]
+    d = H.fresh_dir(tmp_path, "g", case)
+    with pytest.raises(E.MfdtdError) as ei:
+        E.run_rundir(d, form=E.FORM_FP32_FUSED)
+    assert E.STATUS[ei.value.code] == "EINVAL"
+
+
+def test_fp32_chunked_grid_and_long_run(built, tmp_path):
+    """A grid long in x (several x-chunks per tile column) and 200 steps."""
+    p, wp, nu, B0 = CASES["lk_trail"]
+    p = dataclasses.replace(p, Nx=160, Ny=48, Nz=64, tsteps=200, numfiles=5,
+                            probex=[80, 30], probey=[24, 20], probez=[32, 30])
+    wp = rd.gaussian_trail_wp(p, 1e14, 1.0)
+    nu = np.full((p.Nx, p.Ny), 5e4)
+    case = (p, wp, nu, B0)
+    da = H.fresh_dir(tmp_path, "f", case)
+    db = H.fresh_dir(tmp_path, "o", case)
+    E.run_rundir(da, form=E.FORM_FP32_FUSED)
+    H.run_oracle(db)
+    compare_fp32(da, db, p)
+
+
+def test_fp32_in_memory_matches_plain_fields(built):
+    """Field snapshots after 60 steps: FP32 vs FP64 plain form on the GPU."""
+    p, wp, nu, B0 = CASES["lk_trail"]
+    p = dataclasses.replace(p, tsteps=60)
+    wp2 = np.asarray(wp).reshape(-1, order="F").reshape(p.Nx, p.Ny)
+    nu2 = np.asarray(nu).reshape(-1, order="F").reshape(p.Nx, p.Ny)
+    pb = E.Problem.from_params(p, wp2, nu2, B0)
+    s64 = E.Simulation(pb, form=E.FORM_FP64_PLAIN)
+    s32 = E.Simulation(pb, form=E.FORM_FP32_FUSED)
+    s64.advance(60)
+    s32.advance(60)
+    for comp in range(6):
+        a, b = s32.read_field(comp), s64.read_field(comp)
+        if np.linalg.norm(b) > 0:
+            assert H.rel_l2(a, b) < TOL, comp
+    s64.close()
+    s32.close()
