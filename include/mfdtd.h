@@ -135,6 +135,17 @@ int mfdtd_sim_write_outputs(mfdtd_sim *s, const char *dir);
  * simulation's stream), and the number of kernels it launched. */
 int mfdtd_sim_last_timing(const mfdtd_sim *s, double *ms_per_step, int64_t *launches);
 
+/* Bistatic radar cross section from the simulation's near-to-far-field sums,
+ * replacing analysis/meteorNTF.m:236-332 (which handles only the backscatter
+ * direction theta = 90 deg, phi = 180 deg) for any list of directions
+ * (radians; theta from +z, phi from +x).  Uses the analysis constants of
+ * analysis/loadconstants.m and the incident power of the source DFT, as the
+ * MATLAB does.  out[(m * ndir + d) * 3 + {0, 1, 2}] = sigma, and its two
+ * polarisation parts |L_phi + eta0 N_theta|^2 and |L_theta - eta0 N_phi|^2
+ * terms, in m^2, for frequency m.  method 0: FP64 on the CUDA cores. */
+int mfdtd_sim_far_field(mfdtd_sim *s, int32_t ndir, const double *theta, const double *phi,
+                        int32_t method, double *out);
+
 /* Per-kernel-class device time of the last mfdtd_sim_advance when the
  * simulation was created with opts.profile set: for class `which` (0, 1, ...)
  * its name, mean duration of one launch in ms, and launch count.  Returns

@@ -36,6 +36,7 @@ CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-result",
 CUDA_UNITS = [
     ("plain_fp64.cu", ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]),
     ("fp32_fused.cu", []),
+    ("farfield.cu", []),
 ]
 CXX_UNITS = ["problem.cpp", "sim.cpp"]
 

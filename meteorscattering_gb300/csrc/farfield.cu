@@ -1,0 +1,255 @@
+// farfield.cu -- near-to-far-field projection of the Huygens-surface sums.
+//
+// Generalises analysis/meteorNTF.m:236-332 (backscatter only, observer along
+// -x) to any set of directions r_hat(theta, phi):
+//     L(r_hat) = sum over the 12 M arrays, N(r_hat) = sum over the 12 J arrays of
+//     w * dA * X(a,b) * exp(-j k r_hat . r'(a,b)),
+// where X = cos-sum + 1i * sin-sum is the phasor of one DFT accumulator
+// (analysis/meteorNTF.m:202-230), w the trapezoid edge weight and r' the Yee
+// position of the sample (the half-cell offsets of meteorNTF.m:236-246).
+//
+// The phase factor of a sample on a face with in-plane axes (a, b) separates,
+// exp(-jk r_n n0) * exp(-jk r_a pos_a) * exp(-jk r_b pos_b), so per face:
+//   stage 1 (complex GEMM): T[u][a] = sum_b P[u][b] X[a][b],
+//            P[u][b] = w_b exp(-jk s_u pos_b), s_u the distinct values of r_b
+//            over the direction set (a theta/phi grid has few of them);
+//   stage 2 (reduction):    L[d] += exp(-jk r_n n0) dA sum_a w_a exp(-jk r_a pos_a) T[u(d)][a].
+// Both stages run in FP64 on the CUDA cores.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "common.hpp"
+#include "farfield.hpp"
+
+namespace mfdtd {
+namespace {
+
+constexpr double kPI = 3.141592653589793;
+// analysis/loadconstants.m:3-10 (the RCS post-processing constants)
+const double kU0a = 4 * kPI * 1e-7, kE0a = 8.845e-12;
+
+void ck(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) throw Error(MFDTD_ECUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// P[u][b] = w_b * exp(-j k s_u pos_b)
+__global__ void k_ff_phase(double2 *P, const double *s, int U, int B, double k, double b_off,
+                           double hb, int halve_ends) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x, u = blockIdx.y;
+    if (b >= B || u >= U) return;
+    const double pos = (b + b_off) * hb;
+    double sn, cs;
+    sincos(-k * s[u] * pos, &sn, &cs);
+    const double w = (halve_ends && (b == 0 || b == B - 1)) ? 0.5 : 1.0;
+    P[(size_t)u * B + b] = make_double2(w * cs, w * sn);
+}
+
+// T[u][a] = sum_b P[u][b] * X(a, b); X(a,b) = src[((a0+a)*Bs + b0+b)*n2 + 2m + {1: re, 0: im}]
+constexpr int FT = 16;
+__global__ void __launch_bounds__(256) k_ff_gemm(double2 *T, const double2 *P, const double *src,
+                                                 int U, int A, int B, int a0, int b0, int Bs, int n2,
+                                                 int m) {
+    __shared__ double2 Ps[FT][FT + 1];
+    __shared__ double2 Xs[FT][FT + 1];
+    const int tx = threadIdx.x, ty = threadIdx.y;  // tx: a within tile, ty: u within tile
+    const int a = blockIdx.x * FT + tx, u = blockIdx.y * FT + ty;
+    double re = 0, im = 0;
+    for (int bb = 0; bb < B; bb += FT) {
+        // P tile: rows u, cols b ; X tile: rows a, cols b
+        {
+            const int uu = blockIdx.y * FT + ty, b = bb + tx;
+            Ps[ty][tx] = (uu < U && b < B) ? P[(size_t)uu * B + b] : make_double2(0, 0);
+            const int aa = blockIdx.x * FT + ty;
+            if (aa < A && b < B) {
+                const size_t o = ((size_t)(a0 + aa) * Bs + (b0 + b)) * n2 + 2 * m;
+                Xs[ty][tx] = make_double2(src[o + 1], src[o]);
+            } else {
+                Xs[ty][tx] = make_double2(0, 0);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int q = 0; q < FT; q++) {
+            const double2 p = Ps[ty][q], x = Xs[tx][q];
+            re += p.x * x.x - p.y * x.y;
+            im += p.x * x.y + p.y * x.x;
+        }
+        __syncthreads();
+    }
+    if (a < A && u < U) T[(size_t)u * A + a] = make_double2(re, im);
+}
+
+// out[d] += scale(d) * sum_a w_a exp(-jk r_a(d) pos_a) T[u(d)][a]
+__global__ void __launch_bounds__(256) k_ff_reduce(double2 *out, const double2 *T, const int *umap,
+                                                   const double *ra, const double *rn, int D, int A,
+                                                   double k, double a_off, double ha, int halve_ends,
+                                                   double n0, double area) {
+    const int d = blockIdx.x;
+    if (d >= D) return;
+    const double2 *row = T + (size_t)umap[d] * A;
+    const double kr = -k * ra[d];
+    double re = 0, im = 0;
+    for (int a = threadIdx.x; a < A; a += blockDim.x) {
+        double sn, cs;
+        sincos(kr * ((a + a_off) * ha), &sn, &cs);
+        const double w = (halve_ends && (a == 0 || a == A - 1)) ? 0.5 : 1.0;
+        const double2 t = row[a];
+        re += w * (cs * t.x - sn * t.y);
+        im += w * (cs * t.y + sn * t.x);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        re += __shfl_down_sync(0xffffffffu, re, off);
+        im += __shfl_down_sync(0xffffffffu, im, off);
+    }
+    __shared__ double sre[8], sim[8];
+    if ((threadIdx.x & 31) == 0) { sre[threadIdx.x >> 5] = re; sim[threadIdx.x >> 5] = im; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) { re += sre[w]; im += sim[w]; }
+        double sn, cs;
+        sincos(-k * rn[d] * n0, &sn, &cs);
+        const double xr = area * (cs * re - sn * im), xi = area * (cs * im + sn * re);
+        out[d].x += xr;
+        out[d].y += xi;
+    }
+}
+
+struct FaceDesc {
+    int n_ax, a_ax, b_ax;  // 0 = x, 1 = y, 2 = z
+    bool high;             // back / top / right
+};
+// face order in the NTF arrays: front, back, top, bot, left, right
+const FaceDesc kFaces[6] = {{0, 1, 2, false}, {0, 1, 2, true}, {1, 0, 2, true},
+                            {1, 0, 2, false}, {2, 0, 1, false}, {2, 0, 1, true}};
+// per face: (array offset within the face's 4, vector 0=M/1=J, field axis, kind 0=A/1=B)
+struct CompDesc {
+    int q, vec, axis, kind;
+};
+// arrays of one face in file order: front: My, Mz, Jy, Jz ; top: Mx, Mz, Jx, Jz ; left: Mx, My, Jx, Jy
+const CompDesc kComps[3][4] = {
+    {{0, 0, 1, 0}, {1, 0, 2, 1}, {2, 1, 1, 1}, {3, 1, 2, 0}},   // x faces
+    {{0, 0, 0, 0}, {1, 0, 2, 1}, {2, 1, 0, 1}, {3, 1, 2, 0}},   // y faces
+    {{0, 0, 0, 0}, {1, 0, 1, 1}, {2, 1, 0, 1}, {3, 1, 1, 0}}};  // z faces
+
+}  // namespace
+
+// Far-field of the 24 device arrays `ntf` (file layout) for the given directions.
+void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdft, int ndir,
+                    const double *theta, const double *phi, double *out, void *stream) {
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nf = P.nntf(), ntfb = P.ntfb, n2 = 2 * nf;
+    const int dims[3] = {P.Nx, P.Ny, P.Nz};
+    const double h[3] = {P.dx, P.dy, P.dz};
+    const double vp = std::sqrt(1.0 / (kU0a * kE0a)), eta0 = std::sqrt(kU0a / kE0a);
+    std::vector<double> r[3];
+    for (int q = 0; q < 3; q++) r[q].resize(ndir);
+    for (int d = 0; d < ndir; d++) {
+        r[0][d] = std::sin(theta[d]) * std::cos(phi[d]);
+        r[1][d] = std::sin(theta[d]) * std::sin(phi[d]);
+        r[2][d] = std::cos(theta[d]);
+    }
+    double *d_r[3];
+    std::vector<void *> tmp;
+    auto dmalloc = [&](size_t bytes) {
+        void *p = nullptr;
+        ck(cudaMallocAsync(&p, std::max<size_t>(bytes, 8), st), "cudaMallocAsync");
+        tmp.push_back(p);
+        return p;
+    };
+    for (int q = 0; q < 3; q++) {
+        d_r[q] = (double *)dmalloc(ndir * 8);
+        ck(cudaMemcpyAsync(d_r[q], r[q].data(), ndir * 8, cudaMemcpyHostToDevice, st), "H2D");
+    }
+    // accumulators [freq][vec][axis][dir]
+    double2 *acc = (double2 *)dmalloc((size_t)nf * 6 * ndir * sizeof(double2));
+    ck(cudaMemsetAsync(acc, 0, (size_t)nf * 6 * ndir * sizeof(double2), st), "memset");
+
+    for (int f = 0; f < 6; f++) {
+        const FaceDesc &F = kFaces[f];
+        const int Na = dims[F.a_ax], Nb = dims[F.b_ax];
+        // distinct direction cosines along b, and the map d -> u
+        std::map<double, int> uniq;
+        std::vector<int> umap(ndir);
+        for (int d = 0; d < ndir; d++) {
+            auto it = uniq.find(r[F.b_ax][d]);
+            if (it == uniq.end()) it = uniq.emplace(r[F.b_ax][d], (int)uniq.size()).first;
+            umap[d] = it->second;
+        }
+        std::vector<double> svals(uniq.size());
+        for (auto &kv : uniq) svals[kv.second] = kv.first;
+        const int U = (int)svals.size();
+        double *d_s = (double *)dmalloc(U * 8);
+        int *d_umap = (int *)dmalloc(ndir * 4);
+        ck(cudaMemcpyAsync(d_s, svals.data(), U * 8, cudaMemcpyHostToDevice, st), "H2D");
+        ck(cudaMemcpyAsync(d_umap, umap.data(), ndir * 4, cudaMemcpyHostToDevice, st), "H2D");
+        const double n0 = (F.high ? dims[F.n_ax] - ntfb : ntfb) * h[F.n_ax];
+        const double area = h[F.a_ax] * h[F.b_ax];
+        // trims (analysis/meteorNTF.m:66-196): type A keeps a in [ntfb, Na-ntfb]
+        // (ends halved) and b in [ntfb, Nb-ntfb-1] at half-integer positions;
+        // type B keeps a in [ntfb, Na-ntfb-1] at half-integer positions and b in
+        // [ntfb, Nb-ntfb] (ends halved).
+        for (int kind = 0; kind < 2; kind++) {
+            const int A = kind == 0 ? Na - 2 * ntfb + 1 : Na - 2 * ntfb;
+            const int B = kind == 0 ? Nb - 2 * ntfb : Nb - 2 * ntfb + 1;
+            if (A <= 0 || B <= 0) continue;
+            const double a_off = kind == 0 ? ntfb : ntfb + 0.5;
+            const double b_off = kind == 0 ? ntfb + 0.5 : ntfb;
+            double2 *Pm = (double2 *)dmalloc((size_t)U * B * sizeof(double2));
+            double2 *T = (double2 *)dmalloc((size_t)U * A * sizeof(double2));
+            for (int m = 0; m < nf; m++) {
+                const double k = 2 * kPI * P.fntf[m] / vp;
+                k_ff_phase<<<dim3((B + 127) / 128, U), 128, 0, st>>>(Pm, d_s, U, B, k, b_off, h[F.b_ax],
+                                                                     kind == 1);
+                for (int c = 0; c < 4; c++) {
+                    const CompDesc &C = kComps[F.n_ax][c];
+                    if (C.kind != kind) continue;
+                    const double *src = ntf[f * 4 + C.q];
+                    k_ff_gemm<<<dim3((A + FT - 1) / FT, (U + FT - 1) / FT), dim3(FT, FT), 0, st>>>(
+                        T, Pm, src, U, A, B, ntfb, ntfb, Nb, n2, m);
+                    double2 *o = acc + ((size_t)m * 6 + C.vec * 3 + C.axis) * ndir;
+                    k_ff_reduce<<<ndir, 256, 0, st>>>(o, T, d_umap, d_r[F.a_ax], d_r[F.n_ax], ndir, A, k,
+                                                      a_off, h[F.a_ax], kind == 0, n0, area);
+                }
+            }
+        }
+    }
+    std::vector<double2> h_acc((size_t)nf * 6 * ndir);
+    ck(cudaMemcpyAsync(h_acc.data(), acc, h_acc.size() * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H");
+    for (void *p : tmp) ck(cudaFreeAsync(p, st), "cudaFreeAsync");
+    ck(cudaStreamSynchronize(st), "far field");
+
+    // sigma: analysis/meteorNTF.m:311-332, generalised to (theta, phi)
+    const double *Eydft = srcdft, *Ezdft = srcdft + 2 * nf;
+    for (int m = 0; m < nf; m++) {
+        const double k = 2 * kPI * P.fntf[m] / vp;
+        const double ezr = Ezdft[2 * m + 1], ezi = Ezdft[2 * m];
+        const double eyr = Eydft[2 * m + 1], eyi = Eydft[2 * m];
+        const double Pinc = (ezr * ezr + ezi * ezi + eyr * eyr + eyi * eyi) / 2 / eta0;
+        const double c = k * k / (8 * kPI * eta0) / Pinc;
+        for (int d = 0; d < ndir; d++) {
+            auto g = [&](int vec, int ax) { return h_acc[((size_t)m * 6 + vec * 3 + ax) * ndir + d]; };
+            const double ct = std::cos(theta[d]), stt = std::sin(theta[d]);
+            const double cp = std::cos(phi[d]), sp = std::sin(phi[d]);
+            double2 Lx = g(0, 0), Ly = g(0, 1), Lz = g(0, 2), Nx = g(1, 0), Ny = g(1, 1), Nz = g(1, 2);
+            auto th = [&](double2 X, double2 Y, double2 Z) {
+                return make_double2(X.x * ct * cp + Y.x * ct * sp - Z.x * stt, X.y * ct * cp + Y.y * ct * sp - Z.y * stt);
+            };
+            auto phf = [&](double2 X, double2 Y) { return make_double2(-X.x * sp + Y.x * cp, -X.y * sp + Y.y * cp); };
+            const double2 Lth = th(Lx, Ly, Lz), Lph = phf(Lx, Ly), Nth = th(Nx, Ny, Nz), Nph = phf(Nx, Ny);
+            const double ar = Lph.x + eta0 * Nth.x, ai = Lph.y + eta0 * Nth.y;
+            const double br = Lth.x - eta0 * Nph.x, bi = Lth.y - eta0 * Nph.y;
+            const double sa = c * (ar * ar + ai * ai), sb = c * (br * br + bi * bi);
+            double *o = out + ((size_t)m * ndir + d) * 3;
+            o[0] = sa + sb;
+            o[1] = sa;
+            o[2] = sb;
+        }
+    }
+}
+
+}  // namespace mfdtd

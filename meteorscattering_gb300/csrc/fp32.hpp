@@ -24,6 +24,8 @@ public:
     void read_field(int comp, double *out, void *stream);
     // Throws if a kernel set the device error flag (a bounded wait ran out).
     void check(void *stream);
+    // Device pointers of the 24 DFT arrays (output_NTF.dat order).
+    double *const *ntf_arrays() const;
     ~Fp32Sim();
 
 private:

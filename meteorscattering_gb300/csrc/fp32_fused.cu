@@ -1045,6 +1045,8 @@ void Fp32Sim::read_field(int comp, double *out, void *stream) {
     ck(cudaFreeAsync(tmp, s), "cudaFreeAsync");
 }
 
+double *const *Fp32Sim::ntf_arrays() const { return impl_->a.ntf; }
+
 Fp32Sim::~Fp32Sim() { delete impl_; }
 
 }  // namespace mfdtd

@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "common.hpp"
+#include "farfield.hpp"
 #include "fp32.hpp"
 
 using mfdtd::Error;
@@ -348,11 +349,9 @@ struct mfdtd_sim {
                8 * ((int64_t)P.Nx * P.Ny * nf2);
     }
 
-    void read_ntf(double *out) {
-        flush();
-        const size_t nf2 = 2 * (size_t)P.nntf();
-        // Source DFT sums: a function of the injected waveform only.  They
-        // cover the steps run so far.
+    // Source DFT sums (source/meteor-2.1.cpp:1378-1383): a function of the
+    // injected waveform only, over the steps run so far.  Eydft then Ezdft.
+    std::vector<double> source_dft() const {
         std::vector<double> sd(4 * (size_t)P.nntf(), 0.0);
         {
             const double PI = 3.141592653589793;
@@ -367,6 +366,13 @@ struct mfdtd_sim {
                     sd[2 * m + 1] += P.src[2 * tt + 1] * c;
                 }
         }
+        return sd;
+    }
+
+    void read_ntf(double *out) {
+        flush();
+        const size_t nf2 = 2 * (size_t)P.nntf();
+        std::vector<double> sd = source_dft();
         std::memcpy(out, sd.data(), sd.size() * 8);
         double *o = out + sd.size();
         const size_t fb = (size_t)P.Ny * P.Nz * nf2, tb = (size_t)P.Nx * P.Nz * nf2, lr = (size_t)P.Nx * P.Ny * nf2;
@@ -615,6 +621,18 @@ int mfdtd_sim_last_timing(const mfdtd_sim *s, double *ms_per_step, int64_t *laun
         if (!s) throw Error(MFDTD_EINVAL, "NULL sim");
         if (ms_per_step) *ms_per_step = s->last_ms_per_step;
         if (launches) *launches = s->last_launches;
+    });
+}
+
+int mfdtd_sim_far_field(mfdtd_sim *s, int32_t ndir, const double *theta, const double *phi,
+                        int32_t method, double *out) {
+    return guarded([&] {
+        if (!s || !theta || !phi || !out || ndir <= 0) throw Error(MFDTD_EINVAL, "bad arguments");
+        if (method != 0) throw Error(MFDTD_EINVAL, "unknown far-field method");
+        s->flush();
+        std::vector<double> sd = s->source_dft();
+        double *const *ntf = s->form == MFDTD_FORM_FP64_PLAIN ? s->pa.ntf : s->f32->ntf_arrays();
+        mfdtd::far_field_fp64(s->P, ntf, sd.data(), ndir, theta, phi, out, s->stream);
     });
 }
 

@@ -32,7 +32,8 @@ EXPORTS = (
     "mfdtd_sim_create", "mfdtd_sim_destroy", "mfdtd_sim_advance", "mfdtd_sim_sync",
     "mfdtd_sim_step_index", "mfdtd_sim_ntf_size", "mfdtd_sim_read_ntf",
     "mfdtd_sim_read_probes", "mfdtd_sim_read_field", "mfdtd_sim_write_outputs",
-    "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_last_error", "mfdtd_version",
+    "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_sim_far_field",
+    "mfdtd_last_error", "mfdtd_version",
 )
 
 
@@ -95,6 +96,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_sim_last_timing": (C.c_int, [vp, dp, C.POINTER(i64)]),
         "mfdtd_sim_kernel_stats": (C.c_int, [vp, i32, C.c_char_p, C.c_size_t, dp,
                                              C.POINTER(i64)]),
+        "mfdtd_sim_far_field": (C.c_int, [vp, i32, dp, dp, i32, dp]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -244,6 +246,18 @@ class Simulation:
         ms, n = C.c_double(), C.c_int64()
         _check(load_library().mfdtd_sim_last_timing(self._h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def far_field(self, theta, phi, method: int = 0) -> np.ndarray:
+        """sigma[nntf, ndir, 3] (total, and the two polarisation parts) in m^2."""
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        ph = np.ascontiguousarray(phi, dtype=np.float64)
+        if th.shape != ph.shape:
+            raise ValueError("theta and phi must have the same shape")
+        nf = self.dims[4]
+        out = np.empty((nf, th.size, 3), dtype=np.float64)
+        _check(load_library().mfdtd_sim_far_field(self._h, th.size, _dp(th), _dp(ph), method,
+                                                  _dp(out)))
+        return out
 
     def kernel_stats(self):
         """[(name, mean ms per launch, launches)] of the last advance (profile=True)."""

