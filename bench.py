@@ -72,6 +72,14 @@ def workload(name: str, steps_total: int):
         desc = ("256x256x512 magnetized trail, dx=0.2 m, Lee-Kalluri J, 10-cell CPML, "
                 "plane wave along +x (Ez), z-uniform Gaussian trail n0=1e15 r0=0.8 m")
         n0, r0, nu = 1e15, 0.8, 3e4
+    elif name == "trailprof":
+        # Profiling case: same physics, 128x384x1024 (3 GB FP32 state, > L2),
+        # with an interior/boundary mix close to the 768x768x1536 trail's.
+        N = (128, 384, 1024)
+        f0, gf = 50e6, 30.0
+        desc = ("128x384x1024 magnetized trail (profiling size), dx=0.2 m, Lee-Kalluri J, "
+                "10-cell CPML, plane wave along +x (Ez), n0=1e15 r0=0.8 m")
+        n0, r0, nu = 1e15, 0.8, 3e4
     elif name == "cfg1":
         N = (96, 96, 192)
         f0, gf = 50e6, 24.0

@@ -46,7 +46,7 @@ constexpr int STAGE_B = 3 * E_B + 3 * H_B + 3 * J_B;
 constexpr int STAGE_TX = 3 * EJ * EK * 4 + 3 * HJ * HK * 4 + 3 * TJ * TK * 4;  // bytes per stage
 constexpr int HN_COLS = TK + 1;            // new-H plane: cols k0-1..k0+TK-1
 constexpr int HN_B = 3 * HJ * HN_COLS * 4;
-constexpr int SMEM_B = NS * STAGE_B + align128(HN_B) + NS * 8 + 128;
+constexpr int SMEM_B = NS * STAGE_B + align128(HN_B) + NS * 8 + 16 + 128;
 constexpr double kE0 = 8.85419e-12;
 
 struct Maps {
@@ -66,6 +66,7 @@ struct Args {
     double platesize;
     float Bh[2 * kMaxPml], Ahx[2 * kMaxPml], Ahy[2 * kMaxPml], Ahz[2 * kMaxPml];
     float Be[2 * kMaxPml], Aex[2 * kMaxPml], Aey[2 * kMaxPml], Aez[2 * kMaxPml];
+    float lku[18];       // Lee-Kalluri matrices when nu is uniform over the grid
     // state
     float *E[2][3], *H[2][3], *J[3];
     float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
@@ -165,104 +166,133 @@ struct HVal {
     float x, y, z;
 };
 
+__device__ __forceinline__ bool hits(int lo, int hi, int v) { return v >= lo && v <= hi; }
+
+// Per-tile facts that are uniform across the CTA.
+struct TileInfo {
+    bool clean;   // no y/z CPML, TF/SF, NTF, slice, plate or domain-edge rows/columns
+    bool tf_in;   // (clean tiles) the whole tile lies inside the TF/SF box in j and k
+};
+
+
+__device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
+    TileInfo ti;
+    const int jlo = j0 - 1, jhi = j0 + TJ, klo = k0 - 1, khi = k0 + TK;
+    const int Ny = a.Ny, Nz = a.Nz, L = a.dopml ? a.L : 0;
+    bool c = a.doplate == 0;
+    c = c && jlo >= L + 1 && jhi <= Ny - L - 2 && klo >= L + 1 && khi <= Nz - L - 2;
+    c = c && jlo >= 1 && jhi <= Ny - 2 && klo >= 1 && khi <= Nz - 2;
+    const int sy[6] = {a.by1 - 1, a.by1, a.by2 - 1, a.by2, a.ntfb, Ny - a.ntfb};
+    const int sz[6] = {a.bz1 - 1, a.bz1, a.bz2 - 1, a.bz2, a.ntfb, Nz - a.ntfb};
+    for (int q = 0; q < 6; q++) c = c && !hits(jlo, jhi, sy[q]) && !hits(klo, khi, sz[q]);
+    // slices are written on record steps only
+    c = c && !(record && (hits(jlo, jhi, a.ssy) || hits(klo, khi, a.ssz)));
+    ti.clean = c;
+    ti.tf_in = jlo > a.by1 && jhi < a.by2 - 1 && klo > a.bz1 && khi < a.bz2 - 1;
+    return ti;
+}
+
 // H half-step of one cell (source/meteor-2.1.cpp:656-937 in FP32).  `dj,dk`
-// are relative to the tile origin; the E box of the plane and of the next
+// are relative to the tile origin; the E box of this plane and of the next
 // plane, and the old H box, are in shared memory.  Components outside their
 // update domain keep their old value.  `store_psi` is false for halo cells
-// computed on behalf of a neighbouring tile.
-__device__ __forceinline__ HVal h_cell(const Args &a, int par, int i, int j, int k, int dj, int dk,
-                                       const Stage &s, const Stage &s1, bool has_next,
-                                       bool store_psi, bool want_x, bool want_y, bool want_z) {
+// computed on behalf of a neighbouring tile.  In a clean tile only the
+// x-dependent special cases (uniform across the CTA) can occur.
+template <int PAR, bool CLEAN>
+__device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int dj, int dk,
+                                       const Stage &s, const Stage &s1, bool store_psi,
+                                       bool want_y, bool want_z, bool tf_in, bool use_pf,
+                                       float pf_yx, float pf_zx) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
     HVal o;
     o.x = s.h[0][HIDX(dj, dk)];
     o.y = s.h[1][HIDX(dj, dk)];
     o.z = s.h[2][HIDX(dj, dk)];
     const float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
-    const float *rd[6];
-    float *wr[6];
-    for (int q = 0; q < 6; q++) { rd[q] = a.Ph[par][q]; wr[q] = a.Ph[par ^ 1][q]; }
-    const bool inbx = i >= a.bx1 && i < a.bx2, inby = j >= a.by1 && j < a.by2,
-               inbz = k >= a.bz1 && k < a.bz2;
-    if (want_x && j < Ny - 1 && k < Nz - 1) {
+    const bool xin = i < Nx - 1;
+    const int sx = a.dopml ? hslab(i, Nx, L, a.xshift) : -1;
+    const bool inbx = i >= a.bx1 && i < a.bx2;
+    const bool inby = CLEAN ? tf_in : (j >= a.by1 && j < a.by2);
+    const bool inbz = CLEAN ? tf_in : (k >= a.bz1 && k < a.bz2);
+    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
         const float dEz = s.e[2][EIDX(dj + 1, dk)] - ez;
         const float dEy = s.e[1][EIDX(dj, dk + 1)] - ey;
         float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
-        if (inbx && inbz) {
-            const float ezi = a.inc[par][1][i];
-            if (j == a.by1 - 1) h += a.chy * ezi;
-            if (j == a.by2 - 1) h -= a.chy * ezi;
-        }
-        if (inbx && inby) {
-            const float eyi = a.inc[par][0][i];
-            if (k == a.bz1 - 1) h -= a.chz * eyi;
-            if (k == a.bz2 - 1) h += a.chz * eyi;
-        }
-        if (a.dopml) {
-            const int sy = hslab(j, Ny, L, a.yshift);
-            if (sy >= 0) {
-                const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                const float p = a.Bh[sy] * rd[0][o2] + a.Ahy[sy] * dEz;
-                if (store_psi) wr[0][o2] = p;
-                h -= a.c2h * p;
+        if (!CLEAN) {
+            if (inbx && inbz) {
+                const float ezi = a.inc[PAR][1][i];
+                if (j == a.by1 - 1) h += a.chy * ezi;
+                if (j == a.by2 - 1) h -= a.chy * ezi;
             }
-            const int sz = hslab(k, Nz, L, a.zshift);
-            if (sz >= 0) {
-                const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                const float p = a.Bh[sz] * rd[1][o2] + a.Ahz[sz] * dEy;
-                if (store_psi) wr[1][o2] = p;
-                h += a.c2h * p;
+            if (inbx && inby) {
+                const float eyi = a.inc[PAR][0][i];
+                if (k == a.bz1 - 1) h -= a.chz * eyi;
+                if (k == a.bz2 - 1) h += a.chz * eyi;
+            }
+            if (a.dopml) {
+                const int sy = hslab(j, Ny, L, a.yshift);
+                if (sy >= 0) {
+                    const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                    const float p = a.Bh[sy] * a.Ph[PAR][0][o2] + a.Ahy[sy] * dEz;
+                    if (store_psi) a.Ph[PAR ^ 1][0][o2] = p;
+                    h -= a.c2h * p;
+                }
+                const int sz = hslab(k, Nz, L, a.zshift);
+                if (sz >= 0) {
+                    const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                    const float p = a.Bh[sz] * a.Ph[PAR][1][o2] + a.Ahz[sz] * dEy;
+                    if (store_psi) a.Ph[PAR ^ 1][1][o2] = p;
+                    h += a.c2h * p;
+                }
             }
         }
         o.x = h;
     }
-    if (want_y && i < Nx - 1 && k < Nz - 1 && has_next) {
+    if (want_y && xin && (CLEAN || k < Nz - 1)) {
         const float dEx = s.e[0][EIDX(dj, dk + 1)] - ex;
         const float dEz = s1.e[2][EIDX(dj, dk)] - ez;
         float h = a.c1h * o.y - (a.chz * dEx - a.chx * dEz);
         if (inby && inbz) {
-            if (i == a.bx1 - 1) h -= a.chx * a.inc[par][1][a.bx1];
-            if (i == a.bx2 - 1) h += a.chx * a.inc[par][1][a.bx2 - 1];
+            if (i == a.bx1 - 1) h -= a.chx * a.inc[PAR][1][a.bx1];
+            if (i == a.bx2 - 1) h += a.chx * a.inc[PAR][1][a.bx2 - 1];
         }
-        if (a.dopml) {
-            const int sx = hslab(i, Nx, L, a.xshift);
-            if (sx >= 0) {
-                const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-                const float p = a.Bh[sx] * rd[2][o2] + a.Ahx[sx] * dEz;
-                if (store_psi) wr[2][o2] = p;
-                h += a.c2h * p;
-            }
+        if (sx >= 0) {
+            const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
+            const float p = a.Bh[sx] * (use_pf ? pf_yx : a.Ph[PAR][2][o2]) + a.Ahx[sx] * dEz;
+            if (store_psi) a.Ph[PAR ^ 1][2][o2] = p;
+            h += a.c2h * p;
+        }
+        if (!CLEAN && a.dopml) {
             const int sz = hslab(k, Nz, L, a.zshift);
             if (sz >= 0) {
                 const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                const float p = a.Bh[sz] * rd[3][o2] + a.Ahz[sz] * dEx;
-                if (store_psi) wr[3][o2] = p;
+                const float p = a.Bh[sz] * a.Ph[PAR][3][o2] + a.Ahz[sz] * dEx;
+                if (store_psi) a.Ph[PAR ^ 1][3][o2] = p;
                 h -= a.c2h * p;
             }
         }
         o.y = h;
     }
-    if (want_z && i < Nx - 1 && j < Ny - 1 && has_next) {
+    if (want_z && xin && (CLEAN || j < Ny - 1)) {
         const float dEy = s1.e[1][EIDX(dj, dk)] - ey;
         const float dEx = s.e[0][EIDX(dj + 1, dk)] - ex;
         float h = a.c1h * o.z - (a.chx * dEy - a.chy * dEx);
         if (inby && inbz) {
-            if (i == a.bx1 - 1) h += a.chx * a.inc[par][0][a.bx1];
-            if (i == a.bx2 - 1) h -= a.chx * a.inc[par][0][a.bx2 - 1];
+            if (i == a.bx1 - 1) h += a.chx * a.inc[PAR][0][a.bx1];
+            if (i == a.bx2 - 1) h -= a.chx * a.inc[PAR][0][a.bx2 - 1];
         }
-        if (a.dopml) {
-            const int sx = hslab(i, Nx, L, a.xshift);
-            if (sx >= 0) {
-                const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-                const float p = a.Bh[sx] * rd[4][o2] + a.Ahx[sx] * dEy;
-                if (store_psi) wr[4][o2] = p;
-                h -= a.c2h * p;
-            }
+        if (sx >= 0) {
+            const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
+            const float p = a.Bh[sx] * (use_pf ? pf_zx : a.Ph[PAR][4][o2]) + a.Ahx[sx] * dEy;
+            if (store_psi) a.Ph[PAR ^ 1][4][o2] = p;
+            h -= a.c2h * p;
+        }
+        if (!CLEAN && a.dopml) {
             const int sy = hslab(j, Ny, L, a.yshift);
             if (sy >= 0) {
                 const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                const float p = a.Bh[sy] * rd[5][o2] + a.Ahy[sy] * dEx;
-                if (store_psi) wr[5][o2] = p;
+                const float p = a.Bh[sy] * a.Ph[PAR][5][o2] + a.Ahy[sy] * dEx;
+                if (store_psi) a.Ph[PAR ^ 1][5][o2] = p;
                 h += a.c2h * p;
             }
         }
@@ -274,21 +304,24 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int par, int i, int j, int
 // Incident-line H value of this step at index i (the 1-D update of
 // source/meteor-2.1.cpp:833, 892 without the +x CPML term, which never
 // reaches the TF/SF planes).
-__device__ __forceinline__ float hyinc_new(const Args &a, int par, int i) {
-    const float *ez = a.inc[par][1];
-    return a.c1h * a.inc[par][2][i] + a.chx * (ez[i + 1] - ez[i]);
+template <int PAR>
+__device__ __forceinline__ float hyinc_new(const Args &a, int i) {
+    const float *ez = a.inc[PAR][1];
+    return a.c1h * a.inc[PAR][2][i] + a.chx * (ez[i + 1] - ez[i]);
 }
-__device__ __forceinline__ float hzinc_new(const Args &a, int par, int i) {
-    const float *ey = a.inc[par][0];
-    return a.c1h * a.inc[par][3][i] - a.chx * (ey[i + 1] - ey[i]);
+template <int PAR>
+__device__ __forceinline__ float hzinc_new(const Args &a, int i) {
+    const float *ey = a.inc[PAR][0];
+    return a.c1h * a.inc[PAR][3][i] - a.chx * (ey[i + 1] - ey[i]);
 }
 
-// The whole 1-D incident line for this step, written to set par^1 (one CTA).
-__device__ void line_update(const Args &a, int par, int t) {
+// The whole 1-D incident line for this step, written to set PAR^1 (one CTA).
+template <int PAR>
+__device__ void line_update(const Args &a, int t) {
     const int Nx = a.Nx, L = a.L;
-    const float *ey = a.inc[par][0], *ez = a.inc[par][1], *hy = a.inc[par][2], *hz = a.inc[par][3];
-    float *ey2 = a.inc[par ^ 1][0], *ez2 = a.inc[par ^ 1][1], *hy2 = a.inc[par ^ 1][2],
-          *hz2 = a.inc[par ^ 1][3];
+    const float *ey = a.inc[PAR][0], *ez = a.inc[PAR][1], *hy = a.inc[PAR][2], *hz = a.inc[PAR][3];
+    float *ey2 = a.inc[PAR ^ 1][0], *ez2 = a.inc[PAR ^ 1][1], *hy2 = a.inc[PAR ^ 1][2],
+          *hz2 = a.inc[PAR ^ 1][3];
     for (int i = threadIdx.x; i < Nx; i += blockDim.x) {
         float vy = hy[i], vz = hz[i];
         if (i < Nx - 1) {
@@ -296,10 +329,10 @@ __device__ void line_update(const Args &a, int par, int t) {
             vz = a.c1h * hz[i] - a.chx * (ey[i + 1] - ey[i]);
             if (a.dopml && i >= Nx - L - 1) {
                 const int s = i - a.xshift;
-                const float py = a.Bh[s] * a.incP[par][2][s] + a.Ahx[s] * (ez[i + 1] - ez[i]);
-                const float pz = a.Bh[s] * a.incP[par][3][s] + a.Ahx[s] * (ey[i + 1] - ey[i]);
-                a.incP[par ^ 1][2][s] = py;
-                a.incP[par ^ 1][3][s] = pz;
+                const float py = a.Bh[s] * a.incP[PAR][2][s] + a.Ahx[s] * (ez[i + 1] - ez[i]);
+                const float pz = a.Bh[s] * a.incP[PAR][3][s] + a.Ahx[s] * (ey[i + 1] - ey[i]);
+                a.incP[PAR ^ 1][2][s] = py;
+                a.incP[PAR ^ 1][3][s] = pz;
                 vy += a.c2h * py;
                 vz -= a.c2h * pz;
             }
@@ -315,10 +348,10 @@ __device__ void line_update(const Args &a, int par, int t) {
             vz = a.c1e0 * ez[i] + a.cex * (hy2[i] - hy2[i - 1]);
             if (a.dopml && i >= Nx - L - 1) {
                 const int s = i - a.xshift;
-                const float py = a.Be[s] * a.incP[par][0][s] + a.Aex[s] * (hz2[i] - hz2[i - 1]);
-                const float pz = a.Be[s] * a.incP[par][1][s] + a.Aex[s] * (hy2[i] - hy2[i - 1]);
-                a.incP[par ^ 1][0][s] = py;
-                a.incP[par ^ 1][1][s] = pz;
+                const float py = a.Be[s] * a.incP[PAR][0][s] + a.Aex[s] * (hz2[i] - hz2[i - 1]);
+                const float pz = a.Be[s] * a.incP[PAR][1][s] + a.Aex[s] * (hy2[i] - hy2[i - 1]);
+                a.incP[PAR ^ 1][0][s] = py;
+                a.incP[PAR ^ 1][1][s] = pz;
                 vy -= a.c2e0 * py;
                 vz += a.c2e0 * pz;
             }
@@ -342,102 +375,191 @@ __device__ __forceinline__ void acc2(double *A, double *B, size_t base, double v
     }
 }
 
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(NTHREADS, 2)
-    k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    // TMA destinations must be 128-byte aligned; the launch reserves 128 spare bytes.
-    unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
-    float *hn = (float *)(smem + NS * STAGE_B);
-    uint64_t *bar = (uint64_t *)(smem + NS * STAGE_B + align128(HN_B));
+// Everything a marching CTA keeps between planes.
+struct MarchCtx {
+    unsigned char *smem;
+    float *hn;
+    uint64_t *bar;
+    int tid, warp, lane, j0, k0, i_begin, i_end, p0, q_last, dj, dk, j, k;
+    bool role_ok, in_grid, valid;
+    int issued;
+};
 
-    const int par = t & 1;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, Nzp = a.Nzp, L = a.L;
-    const int k0 = blockIdx.x * TK, j0 = blockIdx.y * TJ;
-    const int i_begin = blockIdx.z * a.chunk;
-    const int i_end = min(Nx, i_begin + a.chunk);
-    if (i_begin >= Nx) return;
-    const int p0 = max(i_begin - 1, 0);
-    const int q_last = min(i_end, Nx - 1);  // last plane loaded
-    const size_t plane = (size_t)Ny * Nzp;
-
-    const bool first_cta = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
-    if (first_cta) line_update(a, par, t);
-
-    // Probes of the previous step from the read set (source/meteor-2.1.cpp:1443-1455).
-    if (first_cta && t > 0 && warp == 9 && lane >= 8 && lane - 8 < a.nprobes) {
-        const int pidx = lane - 8;
-        const int ix = a.probe_ijk[3 * pidx], iy = a.probe_ijk[3 * pidx + 1], iz = a.probe_ijk[3 * pidx + 2];
-        const size_t sI = plane, sJ = Nzp;
-        const size_t c = ix * sI + iy * sJ + iz;
-        const float *E0 = a.E[par][0], *E1 = a.E[par][1], *E2 = a.E[par][2];
-        const float *H0 = a.H[par][0], *H1 = a.H[par][1], *H2 = a.H[par][2];
-        const size_t o = (size_t)(t - 1) * a.nprobes + pidx, T = (size_t)a.tsteps * a.nprobes;
-        a.probe[o] = 0.5 * ((double)E0[c] + E0[c - sI]);
-        a.probe[T + o] = 0.5 * ((double)E1[c] + E1[c - sJ]);
-        a.probe[2 * T + o] = 0.5 * ((double)E2[c] + E2[c - 1]);
-        a.probe[3 * T + o] = 0.25 * ((double)H0[c] + H0[c - sJ] + H0[c - 1] + H0[c - sJ - 1]);
-        a.probe[4 * T + o] = 0.25 * ((double)H1[c] + H1[c - sI] + H1[c - 1] + H1[c - sI - 1]);
-        a.probe[5 * T + o] = 0.25 * ((double)H2[c] + H2[c - sJ] + H2[c - sI] + H2[c - sI - sJ]);
+template <int PAR>
+__device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q) {
+    const int slot = (q - c.p0) % NS;
+    Stage st = stage_at(c.smem + slot * STAGE_B);
+    mbar_arm(&c.bar[slot], STAGE_TX);
+    for (int comp = 0; comp < 3; comp++) {
+        tma3(st.e[comp], &maps.E[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
+        tma3(st.h[comp], &maps.H[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
+        tma3(st.j[comp], &maps.J[comp], c.k0, c.j0, q, &c.bar[slot]);
     }
+}
 
-    if (tid == PROD) {
-        for (int s = 0; s < NS; s++) mbar_init(&bar[s], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
-    auto issue = [&](int q) {
-        const int slot = (q - p0) % NS;
-        unsigned char *base = smem + slot * STAGE_B;
-        Stage st = stage_at(base);
-        mbar_arm(&bar[slot], STAGE_TX);
-        for (int c = 0; c < 3; c++) {
-            tma3(st.e[c], &maps.E[par][c], k0 - 4, j0 - 1, q, &bar[slot]);
-            tma3(st.h[c], &maps.H[par][c], k0 - 4, j0 - 1, q, &bar[slot]);
-            tma3(st.j[c], &maps.J[c], k0, j0, q, &bar[slot]);
-        }
-    };
-    int issued = p0 - 1;  // last plane whose copies were issued (producer's view)
-    if (tid == PROD) {
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        for (int q = p0; q <= q_last && q < p0 + NS; q++) { issue(q); issued = q; }
-    }
-
-    // role of this thread
+// The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
+// or -1.
+template <int PAR, int JM, bool CLEAN>
+__device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &c, int t, int record,
+                                     bool tf_in) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
+    const size_t plane = (size_t)Ny * a.Nzp;
+    const int dj = c.dj, dk = c.dk, j = c.j, k = c.k, warp = c.warp;
     const bool tile = warp < TJ;
-    const int dj = tile ? warp : (warp == TJ ? -1 : lane);
-    const int dk = tile ? lane : (warp == TJ ? lane : -1);
-    const int j = j0 + dj, k = k0 + dk;
-    const bool role_ok = tile || warp == TJ || (warp == TJ + 1 && lane < TJ);
-    const bool in_grid = role_ok && j >= 0 && j < Ny && k >= 0 && k < Nz;
-    const bool valid = tile && in_grid;
+    const bool valid = c.valid, in_grid = c.in_grid;
+    float *hn = c.hn;
 
-    // Lee-Kalluri matrices for this k (LK_PER_K) in registers
-    float lkm[18];
-    if (a.doB0 && a.lk_mode == LK_PER_K && valid)
+    // J method: JM 0 = Young DI, 1 = Lee-Kalluri with one matrix pair for the
+    // whole grid (read from the constant bank), 2 = Lee-Kalluri table.
+    float lkm[JM == 2 ? 18 : 1];
+    if (JM == 2 && a.lk_mode == LK_PER_K && valid)
         for (int q = 0; q < 18; q++) lkm[q] = a.lk[(size_t)k * 18 + q];
     const float Gk = valid ? a.G[k] : 0.f, G2k = valid ? a.G2[k] : 0.f;
-
-    float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
-    bool failed = false;
-    int fail_q = 0;
     const int nf = a.nntf;
     const double *ph = a.phase + (size_t)t * nf * 2;
+    const size_t col = (size_t)(valid ? j : 0) * a.Nzp + (valid ? k : 0);
 
-    for (int q = p0; q < i_end; q++) {
+    // Per-plane values that live in global memory are prefetched one plane
+    // ahead into registers, so their latency overlaps the previous plane's
+    // work: the plasma weight (and collision frequency) of the thread's (i,j)
+    // column and, inside the x CPML slabs, the four x-normal psi values.
+    const int jj = valid ? j : 0, kk = valid ? k : 0;
+    auto pf_load = [&](int qq, float &wq, float &nu, float &hyx, float &hzx, float &eyx, float &ezx) {
+        if (!valid || qq >= Nx) return;
+        const size_t ij = (size_t)qq * Ny + jj;
+        wq = a.wq2[ij];
+        if (JM == 0) nu = a.nu2[ij];
+        if (a.dopml) {
+            const int sh = hslab(qq, Nx, L, a.xshift), se = eslab(qq, Nx, L, a.xshift);
+            if (sh >= 0) {
+                const size_t o2 = ((size_t)sh * Ny + jj) * Nz + kk;
+                hyx = a.Ph[PAR][2][o2];
+                hzx = a.Ph[PAR][4][o2];
+            }
+            if (se >= 0) {
+                const size_t o2 = ((size_t)se * Ny + jj) * Nz + kk;
+                eyx = a.Pe[2][o2];
+                ezx = a.Pe[4][o2];
+            }
+        }
+    };
+    float nwq = 0.f, nnu = 0.f, nhyx = 0.f, nhzx = 0.f, neyx = 0.f, nezx = 0.f;
+    pf_load(c.p0, nwq, nnu, nhyx, nhzx, neyx, nezx);
+
+    float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
+    for (int q = c.p0; q < c.i_end; q++) {
         const int i = q;
-        const int slot = (q - p0) % NS;
-        const unsigned parity = ((q - p0) / NS) & 1;
-        const bool has_next = q + 1 <= q_last;
-        bool ok = mbar_wait(&bar[slot], parity);
-        if (has_next) ok = ok && mbar_wait(&bar[(q + 1 - p0) % NS], ((q + 1 - p0) / NS) & 1);
-        if (__syncthreads_or(!ok)) { failed = true; fail_q = q; break; }
-        const Stage s = stage_at(smem + slot * STAGE_B);
-        const Stage s1 = stage_at(smem + ((q + 1 - p0) % NS) * STAGE_B);
-        const bool real = q >= i_begin;
-        const size_t cg = (size_t)i * plane + (size_t)j * Nzp + k;
+        const float cwq = nwq, cnu = nnu, chyx = nhyx, chzx = nhzx, ceyx = neyx, cezx = nezx;
+        pf_load(q + 1, nwq, nnu, nhyx, nhzx, neyx, nezx);
+        const int slot = (q - c.p0) % NS;
+        const bool has_next = q + 1 <= c.q_last;
+        // One thread polls the stage barriers; the rest of the CTA sleeps in
+        // the CTA barrier instead of spinning (the mbarrier acquire by the
+        // poller plus bar.sync makes the TMA data visible to every thread).
+        volatile int *okflag = (volatile int *)(c.bar + NS);
+        if (c.tid == PROD) {
+            bool w = mbar_wait(&c.bar[slot], ((q - c.p0) / NS) & 1);
+            if (has_next) w = mbar_wait(&c.bar[(q + 1 - c.p0) % NS], ((q + 1 - c.p0) / NS) & 1) && w;
+            *okflag = w ? 1 : 0;
+        }
+        __syncthreads();
+        const bool ok = *okflag != 0;
+        const Stage s = stage_at(c.smem + slot * STAGE_B);
+        const Stage s1 = stage_at(c.smem + ((q + 1 - c.p0) % NS) * STAGE_B);
+        const bool real = q >= c.i_begin;
+        const size_t cg = (size_t)i * plane + col;
+
+        // Interior fast path: a clean tile on a plane outside the x CPML slabs
+        // and away from every x-special plane (TF/SF faces when the tile is in
+        // the box, NTF faces, the x slice on record steps).  No conditionals
+        // per cell; the arithmetic is the same as the general path's.
+        const int xlo = a.dopml ? L + 1 : 1, xhi = a.dopml ? Nx - L - 2 : Nx - 2;
+        const bool fast = CLEAN && real && i >= xlo && i <= xhi && i != a.ntfb && i != Nx - a.ntfb &&
+                          !(record && i == a.ssx) &&
+                          !(tf_in && (i == a.bx1 - 1 || i == a.bx1 || i == a.bx2 - 1));
+        if (fast) {
+            float jx = 0.f, jy = 0.f, jz = 0.f, exo = 0.f, eyo = 0.f, ezo = 0.f;
+            if (tile) {
+                exo = s.e[0][EIDX(dj, dk)];
+                eyo = s.e[1][EIDX(dj, dk)];
+                ezo = s.e[2][EIDX(dj, dk)];
+                jx = s.j[0][dj * TK + dk];
+                jy = s.j[1][dj * TK + dk];
+                jz = s.j[2][dj * TK + dk];
+                if (t > 0) {
+                    const float wq = cwq * G2k;
+                    if (JM == 0) {
+                        const float nue = cnu * Gk;
+                        const float den = 2.f + nue * a.dtf;
+                        const float ca = (2.f - nue * a.dtf) / den;
+                        const float cb = (2.f * a.dtf) * wq / den;
+                        jx = ca * jx + cb * exo;
+                        jy = ca * jy + cb * eyo;
+                        jz = ca * jz + cb * ezo;
+                    } else {
+                        const float m0 = 0.5f * (exo + ex_prev);
+                        const float m1 = 0.5f * (eyo + s.e[1][EIDX(dj - 1, dk)]);
+                        const float m2 = 0.5f * (ezo + s.e[2][EIDX(dj, dk - 1)]);
+                        const float *m = JM == 1 ? a.lku : lkm;
+                        float tbl[JM == 2 ? 18 : 1];
+                        if (JM == 2 && a.lk_mode != LK_PER_K) {
+                            const size_t e = a.lk_mode == LK_PER_IJ ? (size_t)i * Ny + j : cg;
+                            for (int u = 0; u < 18; u++) tbl[u] = a.lk[e * 18 + u];
+                            m = tbl;
+                        }
+                        const float nx = m[0] * jx + m[1] * jy + m[2] * jz + wq * (m[9] * m0 + m[10] * m1 + m[11] * m2);
+                        const float ny = m[3] * jx + m[4] * jy + m[5] * jz + wq * (m[12] * m0 + m[13] * m1 + m[14] * m2);
+                        const float nz = m[6] * jx + m[7] * jy + m[8] * jz + wq * (m[15] * m0 + m[16] * m1 + m[17] * m2);
+                        jx = nx; jy = ny; jz = nz;
+                    }
+                }
+            }
+            HVal hv = {0.f, 0.f, 0.f};
+            if (c.role_ok) {
+                const float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
+                hv.x = a.c1h * s.h[0][HIDX(dj, dk)] -
+                       (a.chy * (s.e[2][EIDX(dj + 1, dk)] - ez) - a.chz * (s.e[1][EIDX(dj, dk + 1)] - ey));
+                HN(0, dj, dk) = hv.x;
+                if (warp != TJ) {
+                    hv.y = a.c1h * s.h[1][HIDX(dj, dk)] -
+                           (a.chz * (s.e[0][EIDX(dj, dk + 1)] - ex) - a.chx * (s1.e[2][EIDX(dj, dk)] - ez));
+                    HN(1, dj, dk) = hv.y;
+                }
+                if (warp != TJ + 1) {
+                    hv.z = a.c1h * s.h[2][HIDX(dj, dk)] -
+                           (a.chx * (s1.e[1][EIDX(dj, dk)] - ey) - a.chy * (s.e[0][EIDX(dj + 1, dk)] - ex));
+                    HN(2, dj, dk) = hv.z;
+                }
+            }
+            if (tile) {
+                a.H[PAR ^ 1][0][cg] = hv.x;
+                a.H[PAR ^ 1][1][cg] = hv.y;
+                a.H[PAR ^ 1][2][cg] = hv.z;
+            }
+            __syncthreads();
+            if (tile) {
+                const float c1 = a.c1e0, c2 = a.c2e0;
+                const float ex = c1 * exo + (a.cey * (hv.z - HN(2, dj - 1, dk)) - a.cez * (hv.y - HN(1, dj, dk - 1))) - c2 * jx;
+                const float ey = c1 * eyo + (a.cez * (hv.x - HN(0, dj, dk - 1)) - a.cex * (hv.z - hz_prev)) - c2 * jy;
+                const float ez = c1 * ezo + (a.cex * (hv.y - hy_prev) - a.cey * (hv.x - HN(0, dj - 1, dk))) - c2 * jz;
+                a.E[PAR ^ 1][0][cg] = ex;
+                a.E[PAR ^ 1][1][cg] = ey;
+                a.E[PAR ^ 1][2][cg] = ez;
+                a.J[0][cg] = jx;
+                a.J[1][cg] = jy;
+                a.J[2][cg] = jz;
+                ex_prev = exo;
+            }
+            hy_prev = hv.y;
+            hz_prev = hv.z;
+            if (__syncthreads_or(!ok)) return q;
+            if (c.tid == PROD && q + NS <= c.q_last) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_stage<PAR>(maps, c, q + NS);
+                c.issued = q + NS;
+            }
+            continue;
+        }
 
         // ---- J of the previous step (lagged), source/meteor-fork.cpp:1523-1595
         float jx = 0.f, jy = 0.f, jz = 0.f;
@@ -445,13 +567,15 @@ __global__ void __launch_bounds__(NTHREADS, 2)
             jx = s.j[0][dj * TK + dk];
             jy = s.j[1][dj * TK + dk];
             jz = s.j[2][dj * TK + dk];
-            if (t > 0 && i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1) {
+            const bool jdom = CLEAN ? (i >= 1 && i < Nx - 1)
+                                    : (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1);
+            if (t > 0 && jdom) {
                 const float exc = s.e[0][EIDX(dj, dk)], eyc = s.e[1][EIDX(dj, dk)],
                             ezc = s.e[2][EIDX(dj, dk)];
                 const size_t ij = (size_t)i * Ny + j;
-                if (!a.doB0) {
-                    const float nue = a.doplate ? 0.f : a.nu2[ij] * Gk;
-                    const float wq = a.doplate ? 0.f : a.wq2[ij] * G2k;
+                const float wq = cwq * G2k;
+                if (JM == 0) {
+                    const float nue = cnu * Gk;
                     const float den = 2.f + nue * a.dtf;
                     const float ca = (2.f - nue * a.dtf) / den;
                     const float cb = (2.f * a.dtf) * wq / den;
@@ -462,10 +586,9 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                     const float m0 = 0.5f * (exc + ex_prev);
                     const float m1 = 0.5f * (eyc + s.e[1][EIDX(dj - 1, dk)]);
                     const float m2 = 0.5f * (ezc + s.e[2][EIDX(dj, dk - 1)]);
-                    const float wq = a.doplate ? 0.f : a.wq2[ij] * G2k;
-                    const float *m = lkm;
-                    float tbl[18];
-                    if (a.lk_mode != LK_PER_K) {
+                    const float *m = JM == 1 ? a.lku : lkm;
+                    float tbl[JM == 2 ? 18 : 1];
+                    if (JM == 2 && a.lk_mode != LK_PER_K) {
                         const size_t e = a.lk_mode == LK_PER_IJ ? ij : cg;
                         for (int u = 0; u < 18; u++) tbl[u] = a.lk[e * 18 + u];
                         m = tbl;
@@ -480,89 +603,91 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 
         // ---- H of this plane: tile (all comps), halo row (Hx, Hz), halo column (Hx, Hy)
         HVal hv = {0.f, 0.f, 0.f};
-        if (in_grid) {
-            hv = h_cell(a, par, i, j, k, dj, dk, s, s1, has_next, tile && real,
-                        true, warp != TJ, warp != TJ + 1);
-        }
-        if (role_ok) {
+        if (in_grid)
+            hv = h_cell<PAR, CLEAN>(a, i, j, k, dj, dk, s, s1, tile && real, warp != TJ,
+                                    warp != TJ + 1, tf_in, tile, chyx, chzx);
+        if (c.role_ok) {
             HN(0, dj, dk) = hv.x;
             if (warp != TJ) HN(1, dj, dk) = hv.y;
             if (warp != TJ + 1) HN(2, dj, dk) = hv.z;
         }
         if (valid && real) {
-            a.H[par ^ 1][0][cg] = hv.x;
-            a.H[par ^ 1][1][cg] = hv.y;
-            a.H[par ^ 1][2][cg] = hv.z;
+            a.H[PAR ^ 1][0][cg] = hv.x;
+            a.H[PAR ^ 1][1][cg] = hv.y;
+            a.H[PAR ^ 1][2][cg] = hv.z;
         }
         __syncthreads();
 
         // ---- E of this plane (tile), source/meteor-2.1.cpp:1020-1374
         if (valid && real) {
-            const bool sphere = a.doplate == 2 && [&] {
+            bool sphere = false;
+            if (!CLEAN && a.doplate == 2) {
                 const double x = a.xc[i], y = a.yc[j], z = a.zc[k];
-                return sqrt(x * x + y * y + z * z) < a.platesize;
-            }();
+                sphere = sqrt(x * x + y * y + z * z) < a.platesize;
+            }
             const float c1 = sphere ? a.c1s : a.c1e0, c2 = sphere ? a.c2s : a.c2e0;
             const float cx = sphere ? a.csx : a.cex, cy = sphere ? a.csy : a.cey,
                         cz = sphere ? a.csz : a.cez;
-            const bool plate_row = a.doplate == 1 && i == a.ssx;
+            const bool plate_row = !CLEAN && a.doplate == 1 && i == a.ssx;
             float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
             const float ex_old = ex;
+            const int sxe = a.dopml ? eslab(i, Nx, L, a.xshift) : -1;
+            const bool inby = CLEAN ? tf_in : (j >= a.by1 && j < a.by2);
+            const bool inbz = CLEAN ? tf_in : (k >= a.bz1 && k < a.bz2);
             // Ex
-            if (i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1) {
+            if (i < Nx - 1 && (CLEAN || (j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1))) {
                 const float dHz = hv.z - HN(2, dj - 1, dk);
                 const float dHy = hv.y - HN(1, dj, dk - 1);
                 float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
-                if (i >= a.bx1 && i < a.bx2 - 1) {
-                    if (j >= a.by1 && j < a.by2) {
-                        if (k == a.bz1) e += a.cez * hyinc_new(a, par, i);
-                        if (k == a.bz2) e -= a.cez * hyinc_new(a, par, i);
+                if (!CLEAN) {
+                    if (i >= a.bx1 && i < a.bx2 - 1) {
+                        if (inby) {
+                            if (k == a.bz1) e += a.cez * hyinc_new<PAR>(a, i);
+                            if (k == a.bz2) e -= a.cez * hyinc_new<PAR>(a, i);
+                        }
+                        if (inbz) {
+                            if (j == a.by1) e -= a.cey * hzinc_new<PAR>(a, i);
+                            if (j == a.by2) e += a.cey * hzinc_new<PAR>(a, i);
+                        }
                     }
-                    if (k >= a.bz1 && k < a.bz2) {
-                        if (j == a.by1) e -= a.cey * hzinc_new(a, par, i);
-                        if (j == a.by2) e += a.cey * hzinc_new(a, par, i);
-                    }
-                }
-                if (a.dopml) {
-                    const int sy = eslab(j, Ny, L, a.yshift);
-                    if (sy >= 0) {
-                        const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                        const float p = a.Be[sy] * a.Pe[0][o2] + a.Aey[sy] * dHz;
-                        a.Pe[0][o2] = p;
-                        e += a.c2e0 * p;
-                    }
-                    const int sz = eslab(k, Nz, L, a.zshift);
-                    if (sz >= 0) {
-                        const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                        const float p = a.Be[sz] * a.Pe[1][o2] + a.Aez[sz] * dHy;
-                        a.Pe[1][o2] = p;
-                        e -= a.c2e0 * p;
+                    if (a.dopml) {
+                        const int sy = eslab(j, Ny, L, a.yshift);
+                        if (sy >= 0) {
+                            const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                            const float p = a.Be[sy] * a.Pe[0][o2] + a.Aey[sy] * dHz;
+                            a.Pe[0][o2] = p;
+                            e += a.c2e0 * p;
+                        }
+                        const int sz = eslab(k, Nz, L, a.zshift);
+                        if (sz >= 0) {
+                            const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                            const float p = a.Be[sz] * a.Pe[1][o2] + a.Aez[sz] * dHy;
+                            a.Pe[1][o2] = p;
+                            e -= a.c2e0 * p;
+                        }
                     }
                 }
                 ex = e;
             }
             // Ey
-            const bool ey_plate = plate_row && j >= a.plate_lo && j < a.plate_up - 1 &&
-                                  k >= a.plate_lo && k < a.plate_up;
-            if (i >= 1 && i < Nx - 1 && k >= 1) {
+            if (i >= 1 && i < Nx - 1 && (CLEAN || k >= 1)) {
                 const float dHx = hv.x - HN(0, dj, dk - 1);
                 const float dHz = hv.z - hz_prev;
                 float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
-                if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
-                    if (i == a.bx1) e += a.cex * hzinc_new(a, par, a.bx1 - 1);
-                    if (i == a.bx2 - 1) e -= a.cex * hzinc_new(a, par, a.bx2 - 1);
+                if (inby && inbz) {
+                    if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
+                    if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
                 }
-                if (a.dopml) {
-                    const int sx = eslab(i, Nx, L, a.xshift);
-                    if (sx >= 0) {
-                        float p = 0.f;
-                        if (j < Ny - 1 && k < Nz - 1) {
-                            const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-                            p = a.Be[sx] * a.Pe[2][o2] + a.Aex[sx] * dHz;
-                            a.Pe[2][o2] = p;
-                        }
-                        e -= a.c2e0 * p;
+                if (sxe >= 0) {
+                    float p = 0.f;
+                    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
+                        const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
+                        p = a.Be[sxe] * ceyx + a.Aex[sxe] * dHz;
+                        a.Pe[2][o2] = p;
                     }
+                    e -= a.c2e0 * p;
+                }
+                if (!CLEAN && a.dopml) {
                     const int sz = eslab(k, Nz, L, a.zshift);
                     if (sz >= 0) {
                         float p = 0.f;
@@ -576,32 +701,32 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                 }
                 ey = e;
             }
-            if (ey_plate) ey = 0.f;
+            if (plate_row && j >= a.plate_lo && j < a.plate_up - 1 && k >= a.plate_lo && k < a.plate_up)
+                ey = 0.f;
             // Ez
             const bool ez_plate = plate_row && j >= a.plate_lo && j < a.plate_up &&
                                   k >= a.plate_lo && k < a.plate_up - 1;
             float ez_slice = ez;
-            if (i >= 1 && i < Nx - 1 && j >= 1) {
+            if (i >= 1 && i < Nx - 1 && (CLEAN || j >= 1)) {
                 const float dHy = hv.y - hy_prev;
                 const float dHx = hv.x - HN(0, dj - 1, dk);
                 float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
-                if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
-                    if (i == a.bx1) e -= a.cex * hyinc_new(a, par, a.bx1 - 1);
-                    if (i == a.bx2 - 1) e += a.cex * hyinc_new(a, par, a.bx2 - 1);
+                if (inby && inbz) {
+                    if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
+                    if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
                 }
                 if (ez_plate) e = 0.f;
                 ez_slice = e;
-                if (a.dopml) {
-                    const int sx = eslab(i, Nx, L, a.xshift);
-                    if (sx >= 0) {
-                        float p = 0.f;
-                        if (j < Ny - 1 && k < Nz - 1) {
-                            const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-                            p = a.Be[sx] * a.Pe[4][o2] + a.Aex[sx] * dHy;
-                            a.Pe[4][o2] = p;
-                        }
-                        e += a.c2e0 * p;
+                if (sxe >= 0) {
+                    float p = 0.f;
+                    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
+                        const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
+                        p = a.Be[sxe] * cezx + a.Aex[sxe] * dHy;
+                        a.Pe[4][o2] = p;
                     }
+                    e += a.c2e0 * p;
+                }
+                if (!CLEAN && a.dopml) {
                     const int sy = eslab(j, Ny, L, a.yshift);
                     if (sy >= 0 && k < Nz - 1) {
                         const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
@@ -615,17 +740,18 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                 ez = 0.f;
                 ez_slice = 0.f;
             }
-            a.E[par ^ 1][0][cg] = ex;
-            a.E[par ^ 1][1][cg] = ey;
-            a.E[par ^ 1][2][cg] = ez;
+            a.E[PAR ^ 1][0][cg] = ex;
+            a.E[PAR ^ 1][1][cg] = ey;
+            a.E[PAR ^ 1][2][cg] = ez;
             a.J[0][cg] = jx;
             a.J[1][cg] = jy;
             a.J[2][cg] = jz;
 
             // ---- running DFT on the Huygens surface (FP64 sums)
             const int nb = a.ntfb;
-            const bool fr = i == nb, bk = i == Nx - nb, tp = j == Ny - nb, bt = j == nb,
-                       lf = k == nb, rt = k == Nz - nb;
+            const bool fr = i == nb, bk = i == Nx - nb;
+            const bool tp = !CLEAN && j == Ny - nb, bt = !CLEAN && j == nb;
+            const bool lf = !CLEAN && k == nb, rt = !CLEAN && k == Nz - nb;
             if (fr || bk || tp || bt || lf || rt) {
                 const size_t n2 = 2 * (size_t)nf;
                 if (fr || bk) {
@@ -634,14 +760,14 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                     if (fr) { acc2(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
                     if (bk) { acc2(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
                 }
-                if (tp || bt) {
+                if (!CLEAN && (tp || bt)) {
                     const size_t base = ((size_t)i * Nz + k) * n2;
                     const double hz = 0.5 * ((double)hv.z + HN(2, dj - 1, dk));
                     const double hx = 0.5 * ((double)hv.x + HN(0, dj - 1, dk));
                     if (tp) { acc2(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
                     if (bt) { acc2(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
                 }
-                if (lf || rt) {
+                if (!CLEAN && (lf || rt)) {
                     const size_t base = ((size_t)i * Ny + j) * n2;
                     const double hy = 0.5 * ((double)hv.y + HN(1, dj, dk - 1));
                     const double hx = 0.5 * ((double)hv.x + HN(0, dj, dk - 1));
@@ -653,7 +779,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
             // ---- slices on record steps
             if (record) {
                 const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
-                if (k == a.ssz) {
+                if (!CLEAN && k == a.ssz) {
                     a.slE[oz + (size_t)i * Ny + j] = ey;
                     a.slE[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] = ez_slice;
                     if (j < Ny - 1) {
@@ -661,7 +787,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                         a.slH[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] = hv.z;
                     }
                 }
-                if (j == a.ssy) {
+                if (!CLEAN && j == a.ssy) {
                     a.slE[oy + (size_t)i * Nz + k] = ey;
                     a.slE[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] = ez_slice;
                     if (k < Nz - 1) {
@@ -672,7 +798,7 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                 if (i == a.ssx) {
                     a.slE[ox + (size_t)j * Nz + k] = ey;
                     a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = ez_slice;
-                    if (j < Ny - 1 && k < Nz - 1) {
+                    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
                         a.slH[ox + (size_t)j * Nz + k] = hv.y;
                         a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = hv.z;
                     }
@@ -684,22 +810,95 @@ __global__ void __launch_bounds__(NTHREADS, 2)
         }
         hy_prev = hv.y;
         hz_prev = hv.z;
-        __syncthreads();
-        if (tid == PROD && q + NS <= q_last) {
+        if (__syncthreads_or(!ok)) return q;
+        if (c.tid == PROD && q + NS <= c.q_last) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(q + NS);
-            issued = q + NS;
+            issue_stage<PAR>(maps, c, q + NS);
+            c.issued = q + NS;
+        }
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------------------
+template <int PAR, int JM>
+__global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
+    k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    MarchCtx c;
+    // TMA destinations must be 128-byte aligned; the launch reserves 128 spare bytes.
+    c.smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+    c.hn = (float *)(c.smem + NS * STAGE_B);
+    c.bar = (uint64_t *)(c.smem + NS * STAGE_B + align128(HN_B));
+
+    c.tid = threadIdx.x;
+    c.warp = c.tid >> 5;
+    c.lane = c.tid & 31;
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
+    c.k0 = blockIdx.x * TK;
+    c.j0 = blockIdx.y * TJ;
+    c.i_begin = blockIdx.z * a.chunk;
+    c.i_end = min(Nx, c.i_begin + a.chunk);
+    if (c.i_begin >= Nx) return;
+    c.p0 = max(c.i_begin - 1, 0);
+    c.q_last = min(c.i_end, Nx - 1);  // last plane loaded
+    const size_t plane = (size_t)Ny * a.Nzp;
+
+    const bool first_cta = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
+    if (first_cta) line_update<PAR>(a, t);
+
+    // Probes of the previous step from the read set (source/meteor-2.1.cpp:1443-1455).
+    if (first_cta && t > 0 && c.warp == 9 && c.lane >= 8 && c.lane - 8 < a.nprobes) {
+        const int pidx = c.lane - 8;
+        const int ix = a.probe_ijk[3 * pidx], iy = a.probe_ijk[3 * pidx + 1], iz = a.probe_ijk[3 * pidx + 2];
+        const size_t sI = plane, sJ = a.Nzp;
+        const size_t cc = ix * sI + iy * sJ + iz;
+        const float *E0 = a.E[PAR][0], *E1 = a.E[PAR][1], *E2 = a.E[PAR][2];
+        const float *H0 = a.H[PAR][0], *H1 = a.H[PAR][1], *H2 = a.H[PAR][2];
+        const size_t o = (size_t)(t - 1) * a.nprobes + pidx, T = (size_t)a.tsteps * a.nprobes;
+        a.probe[o] = 0.5 * ((double)E0[cc] + E0[cc - sI]);
+        a.probe[T + o] = 0.5 * ((double)E1[cc] + E1[cc - sJ]);
+        a.probe[2 * T + o] = 0.5 * ((double)E2[cc] + E2[cc - 1]);
+        a.probe[3 * T + o] = 0.25 * ((double)H0[cc] + H0[cc - sJ] + H0[cc - 1] + H0[cc - sJ - 1]);
+        a.probe[4 * T + o] = 0.25 * ((double)H1[cc] + H1[cc - sI] + H1[cc - 1] + H1[cc - sI - 1]);
+        a.probe[5 * T + o] = 0.25 * ((double)H2[cc] + H2[cc - sJ] + H2[cc - sI] + H2[cc - sI - sJ]);
+    }
+
+    if (c.tid == PROD) {
+        for (int s = 0; s < NS; s++) mbar_init(&c.bar[s], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    c.issued = c.p0 - 1;
+    if (c.tid == PROD) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int q = c.p0; q <= c.q_last && q < c.p0 + NS; q++) {
+            issue_stage<PAR>(maps, c, q);
+            c.issued = q;
         }
     }
 
-    if (failed && tid == PROD) {
+    // role of this thread
+    const bool tile = c.warp < TJ;
+    c.dj = tile ? c.warp : (c.warp == TJ ? -1 : c.lane);
+    c.dk = tile ? c.lane : (c.warp == TJ ? c.lane : -1);
+    c.j = c.j0 + c.dj;
+    c.k = c.k0 + c.dk;
+    c.role_ok = tile || c.warp == TJ || (c.warp == TJ + 1 && c.lane < TJ);
+    c.in_grid = c.role_ok && c.j >= 0 && c.j < Ny && c.k >= 0 && c.k < Nz;
+    c.valid = tile && c.in_grid;
+
+    const TileInfo ti = classify(a, c.j0, c.k0, record);
+    const int fail_q = ti.clean ? march<PAR, JM, true>(maps, a, c, t, record, ti.tf_in)
+                                : march<PAR, JM, false>(maps, a, c, t, record, false);
+    if (fail_q >= 0 && c.tid == PROD) {
         atomicOr(a.err, 1u);
         // Let the copies already issued land (bounded) before the CTA exits.
-        for (int qq = fail_q; qq <= issued; qq++) {
-            const int sl = (qq - p0) % NS;
-            const unsigned pp = ((qq - p0) / NS) & 1;
+        for (int qq = fail_q; qq <= c.issued; qq++) {
+            const int sl = (qq - c.p0) % NS;
+            const unsigned pp = ((qq - c.p0) / NS) & 1;
             const uint64_t t0 = globaltimer();
-            while (!mbar_test(&bar[sl], pp) && globaltimer() - t0 < 200000000ull) {
+            while (!mbar_test(&c.bar[sl], pp) && globaltimer() - t0 < 200000000ull) {
             }
         }
     }
@@ -813,6 +1012,7 @@ struct Fp32Sim::Impl {
     double *dtmp = nullptr;      // FP64 staging for conversions
     size_t dtmp_len = 0;
     unsigned int *scan = nullptr;  // [0] max|Ex| bits, [1] bad flag
+    int jm = 0;  // J method of the kernel variant
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
         void *p = nullptr;
@@ -933,8 +1133,20 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         }
     for (int c = 0; c < 3; c++) make_map(&m.maps.J[c], a.J[c], P.Nx, P.Ny, P.Nz, m.Nzp, TK, TJ);
 
-    ck(cudaFuncSetAttribute(k_fp32_step, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B),
-       "cudaFuncSetAttribute");
+    ck(cudaFuncSetAttribute(k_fp32_step<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    ck(cudaFuncSetAttribute(k_fp32_step<1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    ck(cudaFuncSetAttribute(k_fp32_step<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    ck(cudaFuncSetAttribute(k_fp32_step<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    ck(cudaFuncSetAttribute(k_fp32_step<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    ck(cudaFuncSetAttribute(k_fp32_step<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    m.jm = 0;
+    if (P.doB0) {
+        bool uniform = !P.lk.empty();
+        for (size_t q = 18; q < P.lk.size() && uniform; q++) uniform = P.lk[q] == P.lk[q % 18];
+        m.jm = uniform ? 1 : 2;
+        if (uniform)
+            for (int q = 0; q < 18; q++) a.lku[q] = (float)P.lk[q];
+    }
     // Split x into chunks so that the grid fills the machine several times over.
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
@@ -955,7 +1167,17 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     cudaStream_t s = (cudaStream_t)stream;
     Impl &m = *impl_;
     if (ev) cudaEventRecord((cudaEvent_t)ev[0], s);
-    k_fp32_step<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t, record ? 1 : 0);
+    const int rec = record ? 1 : 0;
+    auto go = [&](auto kern) { kern<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t, rec); };
+    if ((t & 1) == 0) {
+        if (m.jm == 0) go(k_fp32_step<0, 0>);
+        else if (m.jm == 1) go(k_fp32_step<0, 1>);
+        else go(k_fp32_step<0, 2>);
+    } else {
+        if (m.jm == 0) go(k_fp32_step<1, 0>);
+        else if (m.jm == 1) go(k_fp32_step<1, 1>);
+        else go(k_fp32_step<1, 2>);
+    }
     if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
     m_cur_ = (t + 1) & 1;
     return 1;
