@@ -446,24 +446,38 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     float nwq = 0.f, nnu = 0.f, nhyx = 0.f, nhzx = 0.f, neyx = 0.f, nezx = 0.f;
     pf_load(c.p0, nwq, nnu, nhyx, nhzx, neyx, nezx);
 
+    // One thread polls the stage mbarriers; the rest of the CTA sleeps in the
+    // CTA barrier instead of spinning.  The poller's mbarrier acquire plus
+    // bar.sync make the TMA data visible to every thread.
+    volatile int *okflag = (volatile int *)(c.bar + NS);
+    auto stage_ready = [&](int qq) {
+        return qq > c.q_last || mbar_wait(&c.bar[(qq - c.p0) % NS], ((qq - c.p0) / NS) & 1);
+    };
+    if (c.tid == PROD) *okflag = (stage_ready(c.p0) && stage_ready(c.p0 + 1)) ? 1 : 0;
+    __syncthreads();
+    if (!*okflag) return c.p0;
+    // End of a plane: wait for the stage the next plane needs, release the
+    // CTA, then refill the slot this plane used.
+    auto end_plane = [&](int q) -> bool {
+        if (c.tid == PROD) *okflag = stage_ready(q + 2) ? 1 : 0;
+        __syncthreads();
+        if (!*okflag) return false;
+        if (c.tid == PROD && q + NS <= c.q_last) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_stage<PAR>(maps, c, q + NS);
+            c.issued = q + NS;
+        }
+        return true;
+    };
+
     float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
     for (int q = c.p0; q < c.i_end; q++) {
         const int i = q;
         const float cwq = nwq, cnu = nnu, chyx = nhyx, chzx = nhzx, ceyx = neyx, cezx = nezx;
         pf_load(q + 1, nwq, nnu, nhyx, nhzx, neyx, nezx);
         const int slot = (q - c.p0) % NS;
-        const bool has_next = q + 1 <= c.q_last;
-        // One thread polls the stage barriers; the rest of the CTA sleeps in
-        // the CTA barrier instead of spinning (the mbarrier acquire by the
-        // poller plus bar.sync makes the TMA data visible to every thread).
-        volatile int *okflag = (volatile int *)(c.bar + NS);
-        if (c.tid == PROD) {
-            bool w = mbar_wait(&c.bar[slot], ((q - c.p0) / NS) & 1);
-            if (has_next) w = mbar_wait(&c.bar[(q + 1 - c.p0) % NS], ((q + 1 - c.p0) / NS) & 1) && w;
-            *okflag = w ? 1 : 0;
-        }
-        __syncthreads();
-        const bool ok = *okflag != 0;
+        // Stages q and q+1 are resident: the end-of-plane barrier of the
+        // previous iteration (or the one before the loop) guarantees it.
         const Stage s = stage_at(c.smem + slot * STAGE_B);
         const Stage s1 = stage_at(c.smem + ((q + 1 - c.p0) % NS) * STAGE_B);
         const bool real = q >= c.i_begin;
@@ -552,12 +566,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             }
             hy_prev = hv.y;
             hz_prev = hv.z;
-            if (__syncthreads_or(!ok)) return q;
-            if (c.tid == PROD && q + NS <= c.q_last) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                issue_stage<PAR>(maps, c, q + NS);
-                c.issued = q + NS;
-            }
+            if (!end_plane(q)) return q + 2;
             continue;
         }
 
@@ -810,12 +819,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         }
         hy_prev = hv.y;
         hz_prev = hv.z;
-        if (__syncthreads_or(!ok)) return q;
-        if (c.tid == PROD && q + NS <= c.q_last) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_stage<PAR>(maps, c, q + NS);
-            c.issued = q + NS;
-        }
+        if (!end_plane(q)) return q + 2;
     }
     return -1;
 }
