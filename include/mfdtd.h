@@ -146,6 +146,28 @@ int mfdtd_sim_last_timing(const mfdtd_sim *s, double *ms_per_step, int64_t *laun
 int mfdtd_sim_far_field(mfdtd_sim *s, int32_t ndir, const double *theta, const double *phi,
                         int32_t method, double *out);
 
+/* Far field of caller-held DFT sums without allocating any device memory.
+ * No counterpart in the reference (which computes the far field in MATLAB,
+ * analysis/meteorNTF.m).  For callers that cannot call cudaMalloc while they
+ * run -- a plugin inside a host that owns all device memory, a service that
+ * reserves its memory at start-up and forbids allocation afterwards.  The
+ * working memory is one fixed array of about 17 MB inside the library, held
+ * on every GPU the process uses until it exits.  Limits: each face of the
+ * Huygens box at most 2048 cells along either in-plane axis (larger grids:
+ * mfdtd_sim_far_field).  All calls share that array, so calls whose GPU work
+ * overlaps race and must be serialised by the caller.  The first call on a
+ * device looks up the array's device address; make that first call before
+ * any stream capture.
+ * ntf_dev: the 24 face arrays on the current device, output_NTF.dat order and
+ * layout ([a][b][2*nntf] doubles).  fntf[nntf], srcdft (Eydft[2n] then
+ * Ezdft[2n]), theta/phi[ndir] and out[nntf*ndir*3] are host arrays; out has the
+ * layout of mfdtd_sim_far_field.  stream may be NULL (legacy stream); the
+ * call returns after its GPU work finished. */
+int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t Nx, int32_t Ny, int32_t Nz,
+                           int32_t ntfb, int32_t nntf, const double *fntf, double dx, double dy,
+                           double dz, const double *srcdft, int32_t ndir, const double *theta,
+                           const double *phi, double *out, void *stream);
+
 /* Per-kernel-class device time of the last mfdtd_sim_advance when the
  * simulation was created with opts.profile set: for class `which` (0, 1, ...)
  * its name, mean duration of one launch in ms, and launch count.  Returns

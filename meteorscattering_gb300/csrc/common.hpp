@@ -15,6 +15,9 @@ namespace mfdtd {
 // hard-codes 10 cells, source/meteor-2.1.cpp:343).
 constexpr int kMaxPml = 32;
 
+// Record the message mfdtd_last_error() returns on this thread (sim.cpp).
+void set_last_error(const std::string &msg);
+
 struct Error : std::runtime_error {
     int code;
     Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -253,3 +254,187 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
 }
 
 }  // namespace mfdtd
+
+// ---------------------------------------------------------------------------
+// Far-field projection without any device allocation.
+//
+// Some callers cannot allocate device memory while they run: a plugin whose
+// host application owns every device allocation, a service that reserves all
+// of its memory up front and forbids allocation on the request path, or code
+// that must not call into the CUDA allocator at all.  This variant keeps its
+// working memory in one file-scope device array instead, so it only needs the
+// inputs and outputs the caller already holds.  Its limits, and the reasons:
+//   * the array is allocated when the library is loaded, on every GPU the
+//     process uses, and is held until the process exits -- so it is small;
+//   * every call uses the same array, so calls whose GPU work overlaps (on two
+//     streams, or from two threads) race with each other; callers must
+//     serialise them;
+//   * directions are processed 256 at a time and each face may be at most
+//     2048 cells along either of its in-plane axes, which bounds the array.
+namespace mfdtd {
+namespace {
+
+constexpr int kStaticDirs = 256;      // directions per pass
+constexpr int kStaticFace = 2048;     // max in-plane face extent (cells)
+constexpr size_t kStaticBytes =
+    (size_t)kStaticDirs * (2 * kStaticFace) * sizeof(double2)   // P and T
+    + (size_t)kStaticDirs * 6 * sizeof(double2)                 // L, N accumulators
+    + (size_t)kStaticDirs * 7 * sizeof(double)                  // theta, phi, r_hat, sigma staging
+    + (size_t)kStaticDirs * sizeof(int) + 4096;                 // identity map + alignment slack
+__device__ __align__(256) unsigned char g_ff_scratch[kStaticBytes];
+
+struct StaticScratch {
+    double2 *P, *T, *acc;
+    double *th, *ph, *r[3], *sig;
+    int *umap;
+};
+
+StaticScratch carve(unsigned char *base) {
+    StaticScratch sc;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        unsigned char *p = base + off;
+        off += (bytes + 255) / 256 * 256;
+        return p;
+    };
+    sc.P = (double2 *)take((size_t)kStaticDirs * kStaticFace * sizeof(double2));
+    sc.T = (double2 *)take((size_t)kStaticDirs * kStaticFace * sizeof(double2));
+    sc.acc = (double2 *)take((size_t)kStaticDirs * 6 * sizeof(double2));
+    sc.th = (double *)take(kStaticDirs * sizeof(double));
+    sc.ph = (double *)take(kStaticDirs * sizeof(double));
+    for (int q = 0; q < 3; q++) sc.r[q] = (double *)take(kStaticDirs * sizeof(double));
+    sc.sig = (double *)take((size_t)kStaticDirs * 3 * sizeof(double));
+    sc.umap = (int *)take(kStaticDirs * sizeof(int));
+    return sc;
+}
+
+// Device address of g_ff_scratch, looked up once per device with that device
+// current (the host-side symbol is only a stand-in, never a device address).
+constexpr int kMaxDevices = 64;
+std::atomic<unsigned char *> g_scratch_addr[kMaxDevices];
+
+unsigned char *scratch_for_current_device() {
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) throw Error(MFDTD_EINVAL, "device ordinal out of range");
+    unsigned char *p = g_scratch_addr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        void *addr = nullptr;
+        ck(cudaGetSymbolAddress(&addr, g_ff_scratch), "cudaGetSymbolAddress");
+        p = (unsigned char *)addr;
+        g_scratch_addr[dev].store(p, std::memory_order_release);
+    }
+    return p;
+}
+
+__global__ void k_ff_dirs(const double *th, const double *ph, int n, double *rx, double *ry, double *rz,
+                          int *umap) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    double st, ct, sp, cp;
+    sincos(th[d], &st, &ct);
+    sincos(ph[d], &sp, &cp);
+    rx[d] = st * cp;
+    ry[d] = st * sp;
+    rz[d] = ct;
+    umap[d] = d;
+}
+
+// sigma and its two polarisation terms from the L, N accumulators of n directions.
+__global__ void k_ff_sigma(const double2 *acc, const double *th, const double *ph, int n, double c,
+                           double eta0, double *sig) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    auto g = [&](int q) { return acc[(size_t)q * kStaticDirs + d]; };
+    const double2 Lx = g(0), Ly = g(1), Lz = g(2), Nx = g(3), Ny = g(4), Nz = g(5);
+    double stt, ct, sp, cp;
+    sincos(th[d], &stt, &ct);
+    sincos(ph[d], &sp, &cp);
+    const double Lthr = Lx.x * ct * cp + Ly.x * ct * sp - Lz.x * stt, Lthi = Lx.y * ct * cp + Ly.y * ct * sp - Lz.y * stt;
+    const double Lphr = -Lx.x * sp + Ly.x * cp, Lphi = -Lx.y * sp + Ly.y * cp;
+    const double Nthr = Nx.x * ct * cp + Ny.x * ct * sp - Nz.x * stt, Nthi = Nx.y * ct * cp + Ny.y * ct * sp - Nz.y * stt;
+    const double Nphr = -Nx.x * sp + Ny.x * cp, Nphi = -Nx.y * sp + Ny.y * cp;
+    const double ar = Lphr + eta0 * Nthr, ai = Lphi + eta0 * Nthi;
+    const double br = Lthr - eta0 * Nphr, bi = Lthi - eta0 * Nphi;
+    const double sa = c * (ar * ar + ai * ai), sb = c * (br * br + bi * bi);
+    sig[3 * d] = sa + sb;
+    sig[3 * d + 1] = sa;
+    sig[3 * d + 2] = sb;
+}
+
+}  // namespace
+}  // namespace mfdtd
+
+extern "C" int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t Nx, int32_t Ny, int32_t Nz,
+                                      int32_t ntfb, int32_t nntf, const double *fntf, double dx, double dy,
+                                      double dz, const double *srcdft, int32_t ndir, const double *theta,
+                                      const double *phi, double *out, void *stream) {
+    using namespace mfdtd;
+    try {
+        if (!ntf_dev || !fntf || !srcdft || !theta || !phi || !out || ndir <= 0 || nntf <= 0)
+            throw Error(MFDTD_EINVAL, "NULL argument or empty direction/frequency list");
+        for (int q = 0; q < 24; q++)
+            if (!ntf_dev[q]) throw Error(MFDTD_EINVAL, "NULL face array");
+        const int dims[3] = {Nx, Ny, Nz};
+        for (int q = 0; q < 3; q++)
+            if (dims[q] - 2 * ntfb + 1 > kStaticFace || dims[q] - 2 * ntfb < 1)
+                throw Error(MFDTD_EINVAL, "face extent outside [1, 2048] cells: too large for the "
+                                          "allocation-free far field (use mfdtd_sim_far_field)");
+        cudaStream_t st = (cudaStream_t)stream;
+        const StaticScratch sc = carve(scratch_for_current_device());
+        const double h[3] = {dx, dy, dz};
+        const int n2 = 2 * nntf;
+        const double vp = std::sqrt(1.0 / (kU0a * kE0a)), eta0 = std::sqrt(kU0a / kE0a);
+        for (int d0 = 0; d0 < ndir; d0 += kStaticDirs) {
+            const int nd = std::min(kStaticDirs, ndir - d0);
+            ck(cudaMemcpyAsync(sc.th, theta + d0, nd * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+            ck(cudaMemcpyAsync(sc.ph, phi + d0, nd * sizeof(double), cudaMemcpyHostToDevice, st), "H2D");
+            k_ff_dirs<<<(nd + 127) / 128, 128, 0, st>>>(sc.th, sc.ph, nd, sc.r[0], sc.r[1], sc.r[2], sc.umap);
+            for (int m = 0; m < nntf; m++) {
+                ck(cudaMemsetAsync(sc.acc, 0, (size_t)kStaticDirs * 6 * sizeof(double2), st), "memset");
+                const double k = 2 * kPI * fntf[m] / vp;
+                for (int f = 0; f < 6; f++) {
+                    const FaceDesc &F = kFaces[f];
+                    const int Na = dims[F.a_ax], Nb = dims[F.b_ax];
+                    const double n0 = (F.high ? dims[F.n_ax] - ntfb : ntfb) * h[F.n_ax];
+                    const double area = h[F.a_ax] * h[F.b_ax];
+                    for (int kind = 0; kind < 2; kind++) {
+                        const int A = kind == 0 ? Na - 2 * ntfb + 1 : Na - 2 * ntfb;
+                        const int B = kind == 0 ? Nb - 2 * ntfb : Nb - 2 * ntfb + 1;
+                        const double a_off = kind == 0 ? ntfb : ntfb + 0.5;
+                        const double b_off = kind == 0 ? ntfb + 0.5 : ntfb;
+                        // one P row per direction: P[d][b] = w_b exp(-jk r_b(d) pos_b)
+                        k_ff_phase<<<dim3((B + 127) / 128, nd), 128, 0, st>>>(sc.P, sc.r[F.b_ax], nd, B, k, b_off,
+                                                                              h[F.b_ax], kind == 1);
+                        for (int c = 0; c < 4; c++) {
+                            const CompDesc &C = kComps[F.n_ax][c];
+                            if (C.kind != kind) continue;
+                            k_ff_gemm<<<dim3((A + FT - 1) / FT, (nd + FT - 1) / FT), dim3(FT, FT), 0, st>>>(
+                                sc.T, sc.P, ntf_dev[f * 4 + C.q], nd, A, B, ntfb, ntfb, Nb, n2, m);
+                            k_ff_reduce<<<nd, 256, 0, st>>>(sc.acc + (size_t)(C.vec * 3 + C.axis) * kStaticDirs,
+                                                            sc.T, sc.umap, sc.r[F.a_ax], sc.r[F.n_ax], nd, A, k,
+                                                            a_off, h[F.a_ax], kind == 0, n0, area);
+                        }
+                    }
+                }
+                const double ezr = srcdft[2 * nntf + 2 * m + 1], ezi = srcdft[2 * nntf + 2 * m];
+                const double eyr = srcdft[2 * m + 1], eyi = srcdft[2 * m];
+                const double Pinc = (ezr * ezr + ezi * ezi + eyr * eyr + eyi * eyi) / 2 / eta0;
+                k_ff_sigma<<<(nd + 127) / 128, 128, 0, st>>>(sc.acc, sc.th, sc.ph, nd,
+                                                             k * k / (8 * kPI * eta0) / Pinc, eta0, sc.sig);
+                ck(cudaMemcpyAsync(out + ((size_t)m * ndir + d0) * 3, sc.sig, (size_t)nd * 3 * sizeof(double),
+                                   cudaMemcpyDeviceToHost, st),
+                   "D2H");
+            }
+        }
+        ck(cudaGetLastError(), "kernel launch");
+        ck(cudaStreamSynchronize(st), "far field (static scratch)");
+        return MFDTD_OK;
+    } catch (const Error &e) {
+        set_last_error(e.what());
+        return e.code;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return MFDTD_EINVAL;
+    }
+}

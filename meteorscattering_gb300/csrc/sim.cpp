@@ -73,6 +73,9 @@ std::string fmt_g(double v) {
 }
 
 }  // namespace
+
+void set_last_error(const std::string &msg) { g_last_error = msg; }
+
 }  // namespace mfdtd
 
 struct mfdtd_sim {

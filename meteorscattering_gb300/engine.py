@@ -33,7 +33,7 @@ EXPORTS = (
     "mfdtd_sim_step_index", "mfdtd_sim_ntf_size", "mfdtd_sim_read_ntf",
     "mfdtd_sim_read_probes", "mfdtd_sim_read_field", "mfdtd_sim_write_outputs",
     "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_sim_far_field",
-    "mfdtd_last_error", "mfdtd_version",
+    "mfdtd_far_field_static", "mfdtd_last_error", "mfdtd_version",
 )
 
 
@@ -97,6 +97,9 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_sim_kernel_stats": (C.c_int, [vp, i32, C.c_char_p, C.c_size_t, dp,
                                              C.POINTER(i64)]),
         "mfdtd_sim_far_field": (C.c_int, [vp, i32, dp, dp, i32, dp]),
+        "mfdtd_far_field_static": (C.c_int, [C.POINTER(C.c_void_p), i32, i32, i32, i32, i32, dp,
+                                             C.c_double, C.c_double, C.c_double, dp, i32, dp, dp,
+                                             dp, vp]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }

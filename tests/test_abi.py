@@ -100,3 +100,18 @@ def test_drop_in_executable_reports_errors(built, tmp_path):
     import subprocess
     r = subprocess.run([E.EXE_PATH], cwd=str(tmp_path), capture_output=True, text=True)
     assert r.returncode == 1 and "inputs.dat" in r.stderr
+
+
+def test_static_far_field_rejects_oversize_faces(built):
+    """The allocation-free far field refuses faces larger than its fixed
+    working array before touching the device."""
+    import ctypes as C
+    lib = E.load_library()
+    fake = (C.c_void_p * 24)(*range(4096, 4096 + 24 * 64, 64))
+    one = np.ones(4)
+    dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))
+    out = np.zeros(3)
+    rc = lib.mfdtd_far_field_static(fake, 3000, 64, 64, 15, 1, dp(one), 0.2, 0.2, 0.2, dp(one), 1,
+                                    dp(one), dp(one), dp(out), None)
+    assert E.STATUS[rc] == "EINVAL"
+    assert "2048" in E.last_error()
