@@ -79,6 +79,45 @@ typedef struct {
                               on the simulation's stream (mfdtd_sim_kernel_stats) */
 } mfdtd_run_opts;
 
+/* Extended inputs.  The reference hard-codes every one of these
+ * (source/meteor-2.1.cpp:343 pmllen = 10, :413-415 grading m = 4, kappa = 1,
+ * alpha = 0, :539-552 TF/SF box 10 cells and Huygens surface 5 cells inside
+ * the CPML, :1278-1304 a plane wave along +x, :134-138 coordinates filled
+ * for index < Nx only, :319-334 a 2-D plasma map times a Gaussian in z).
+ * mfdtd_ext_defaults() fills the reference's values; a problem that never
+ * receives an mfdtd_ext behaves exactly like the reference.
+ * In a run directory the same content is the optional file ext.dat
+ * (written by meteorscattering_gb300.rundir.write_ext), with wp3.dat/nu3.dat
+ * beside it when the per-cell maps are used. */
+typedef struct {
+    int32_t pmllen;       /* CPML thickness in cells (1..32)                   */
+    int32_t tfsf_gap;     /* cells between the CPML and the TF/SF box          */
+    int32_t ntf_gap;      /* cells between the CPML and the Huygens surface;
+                             must be <= tfsf_gap - 2 (surface outside the box)  */
+    int32_t oblique;      /* 1: plane wave along inc_theta/inc_phi through a
+                             dispersion-matched auxiliary line; the waveform
+                             is the sourcetype's first column; sourcepol is
+                             ignored                                           */
+    int32_t exact_coords; /* 1: cell coordinates -(N-1)/2*d + i*d along every
+                             axis with real division                           */
+    int32_t lk_colocated; /* 1: the Lee-Kalluri current update is driven by E
+                             at the current's own node.  0 (the reference,
+                             source/meteor-fork.cpp:1574-1576) averages E over
+                             two nodes but applies J at one; that asymmetric
+                             coupling grows without bound in magnetized
+                             plasma, faster at higher density               */
+    double pml_m;         /* polynomial grading order                           */
+    double kappa_max;     /* CPML kappa at the outer face (>= 1)                */
+    double alpha_max;     /* CPML alpha in the units of the reference's sigma
+                             (S/m): the recursion decays as
+                             exp(-(sigma/kappa + alpha) dt / E0)               */
+    double inc_theta;     /* direction of k: polar angle from +z (radians)      */
+    double inc_phi;       /* azimuth from +x (radians)                          */
+    double inc_psi;       /* polarisation: E along cos(psi)(-theta_hat) +
+                             sin(psi) phi_hat; psi = 0 is TM (E in the plane of
+                             k and z), psi = pi/2 is TE                         */
+} mfdtd_ext;
+
 typedef struct mfdtd_problem mfdtd_problem; /* parsed inputs + derived tables */
 typedef struct mfdtd_sim mfdtd_sim;         /* device-resident state          */
 
@@ -102,6 +141,15 @@ int mfdtd_problem_from_rundir(const char *dir, mfdtd_problem **out);
 int mfdtd_problem_create(const mfdtd_params *p, const double *wp2, const double *nu2,
                          const double B0[3], mfdtd_problem **out);
 void mfdtd_problem_destroy(mfdtd_problem *pb);
+/* The reference's values of every extended input. */
+void mfdtd_ext_defaults(mfdtd_ext *ext);
+/* Apply extended inputs to a problem and re-derive its tables.  ext may be
+ * NULL (reference values).  wp3/nu3 (may be NULL) are per-cell plasma
+ * frequency (rad/s) and collision frequency (1/s) maps [Nx][Ny][Nz] in C
+ * order; wp3 replaces wp2 * G(z), nu3 replaces nu2 * G(z).  No counterpart in
+ * the reference, which cannot express these inputs. */
+int mfdtd_problem_set_ext(mfdtd_problem *pb, const mfdtd_ext *ext, const double *wp3,
+                          const double *nu3);
 /* Grid and run sizes: out[0..5] = Nx, Ny, Nz, tsteps, nntf, nprobes. */
 int mfdtd_problem_dims(const mfdtd_problem *pb, int64_t out[6]);
 /* Device bytes a simulation of this problem in `form` will hold. */

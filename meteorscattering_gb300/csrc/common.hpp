@@ -62,11 +62,32 @@ struct Problem {
     std::vector<double> lk;            // L&K matrices, kLkStride per entry
     std::vector<double> srcdft;        // Eydft[2n] then Ezdft[2n] (full run)
 
+    // Extended inputs (no counterpart in the reference's inputs.dat): CPML
+    // thickness and grading, TF/SF and Huygens-surface offsets, oblique
+    // plane-wave incidence, exact coordinates, per-cell plasma maps.  With
+    // ext_present == 0 every derived table is the reference's.
+    mfdtd_ext ext{};
+    int ext_present = 0;
+    std::vector<double> wp3, nu3;      // [Nx][Ny][Nz] omega_p and nu, when given
+
+    // derived, extended
+    int kappa_on = 0;
+    std::vector<double> Ke, Kh;        // [2L] 1/kappa - 1 at E and H grading
+    int oblique = 0;
+    double inc_k[3] = {1, 0, 0}, inc_e[3] = {0, 0, 1}, inc_h[3] = {0, -1, 0};
+    double dl = 0;                     // auxiliary-line cell size (dispersion matched)
+    double kr[3] = {0, 0, 0}, s0 = 0;  // s(r) = kr . r_cells + s0, in line cells
+    int M = 0, ashift = 0;             // line nodes; psi index = n - ashift at the far end
+    std::vector<double> Be1, Ae1, Bh1, Ah1;  // [2L] line CPML (high half used)
+
     int nprobes() const { return (int)probex.size(); }
     int nntf() const { return (int)fntf.size(); }
     size_t cells() const { return (size_t)Nx * Ny * Nz; }
     void derive();  // fills every derived member; throws Error on bad input
 };
+
+// The reference's values of every extended input (problem.cpp).
+void ext_defaults(mfdtd_ext &e);
 
 Problem problem_from_rundir(const std::string &dir);
 Problem problem_from_params(const mfdtd_params &p, const double *wp2, const double *nu2,
@@ -85,6 +106,12 @@ struct PlainArgs {
     double *Eyinc, *Ezinc, *Hyinc, *Hzinc, *PeyxI, *PezxI, *PhyxI, *PhzxI;
     const double *wp2, *nu2, *G, *xc, *yc, *zc, *lk, *src, *phase;
     double *ntf[24];
+    // extended inputs
+    int kappa_on, oblique, M, ashift, lk_colocated;
+    double Ke[2 * kMaxPml], Kh[2 * kMaxPml];
+    double ke[3], kh[3], kr[3], s0, dl;
+    double Be1[2 * kMaxPml], Ae1[2 * kMaxPml], Bh1[2 * kMaxPml], Ah1[2 * kMaxPml];
+    const double *wp3, *nu3;  // per-cell maps or null
     double *probe;            // [6][tsteps][nprobes]
     const int *probe_ijk;     // [nprobes][3]
     double *slE, *slH;        // slice records (z, y, x planes, 2 comps each)

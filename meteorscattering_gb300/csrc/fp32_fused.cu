@@ -67,6 +67,14 @@ struct Args {
     float Bh[2 * kMaxPml], Ahx[2 * kMaxPml], Ahy[2 * kMaxPml], Ahz[2 * kMaxPml];
     float Be[2 * kMaxPml], Aex[2 * kMaxPml], Aey[2 * kMaxPml], Aez[2 * kMaxPml];
     float lku[18];       // Lee-Kalluri matrices when nu is uniform over the grid
+    // extended inputs: kappa != 1 derivative terms (1/kappa - 1)/d per slab index
+    int kappa_on;
+    float Khx[2 * kMaxPml], Khy[2 * kMaxPml], Khz[2 * kMaxPml];
+    float Kex[2 * kMaxPml], Key[2 * kMaxPml], Kez[2 * kMaxPml];
+    // oblique incidence: auxiliary line (E in inc[][1], H in inc[][2])
+    int oblique, M, ashift, lk_colocated;
+    float kr[3], s0, ke[3], kh[3], chl, cel;   // chl = c2h/dl, cel = c2e0/dl
+    float Bh1[2 * kMaxPml], Ah1[2 * kMaxPml], Be1[2 * kMaxPml], Ae1[2 * kMaxPml];  // A/dl
     // state
     float *E[2][3], *H[2][3], *J[3];
     float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
@@ -75,6 +83,8 @@ struct Args {
     float *incP[2][4];   // 1-D psi: PeyxI, PezxI, PhyxI, PhzxI
     const float *wq2;    // E0 * wp2^2 per (i,j)
     const float *nu2;    // nu2 per (i,j)
+    const float *wq3;    // E0 * wp3^2 per cell (padded layout) or null
+    const float *nu3;    // nu3 per cell (padded layout) or null
     const float *G, *G2; // z-Gaussian and its square per k
     const float *lk;     // Lee-Kalluri table (18 per entry)
     const float *src;    // [tsteps][2]
@@ -170,6 +180,69 @@ struct HVal {
 
 __device__ __forceinline__ bool hits(int lo, int hi, int v) { return v >= lo && v <= hi; }
 
+// ---- oblique incidence (extended inputs) ----------------------------------
+// Same construction as the FP64 plain form: a node with doubled coordinates P
+// sees the auxiliary line at s = kr . P/2 + s0; every curl term whose
+// neighbour lies across the TF/SF box surface gets the neighbour's incident
+// value.  H targets use the line's E of this pass's start; E targets use the
+// line's H of this step, computed here from the start-of-pass line (the line
+// itself is advanced by the first CTA into the other buffer).
+__device__ __forceinline__ bool obl_in(const Args &a, int p0, int p1, int p2) {
+    return p0 >= 2 * a.bx1 && p0 <= 2 * (a.bx2 - 1) && p1 >= 2 * a.by1 && p1 <= 2 * (a.by2 - 1) &&
+           p2 >= 2 * a.bz1 && p2 <= 2 * (a.bz2 - 1);
+}
+__device__ __forceinline__ bool obl_shell(const Args &a, int i, int j, int k) {
+    return i >= a.bx1 - 1 && i <= a.bx2 && j >= a.by1 - 1 && j <= a.by2 && k >= a.bz1 - 1 &&
+           k <= a.bz2 &&
+           !(i > a.bx1 && i < a.bx2 - 2 && j > a.by1 && j < a.by2 - 2 && k > a.bz1 && k < a.bz2 - 2);
+}
+template <int PAR>
+__device__ __forceinline__ float obl_e_at(const Args &a, float s) {
+    const float *e = a.inc[PAR][1];
+    const float fl = floorf(s);
+    const int n = (int)fl;
+    return e[n] + (s - fl) * (e[n + 1] - e[n]);
+}
+template <int PAR>
+__device__ __forceinline__ float obl_h_new_at(const Args &a, float s) {
+    const float *e = a.inc[PAR][1], *h = a.inc[PAR][2];
+    const float fl = floorf(s);
+    const int n = (int)fl;
+    const float h0 = a.c1h * h[n] - a.chl * (e[n + 1] - e[n]);
+    const float h1 = a.c1h * h[n + 1] - a.chl * (e[n + 2] - e[n + 1]);
+    return h0 + (s - fl) * (h1 - h0);
+}
+// Correction to add to component C of E (IS_E) or H at cell (i,j,k), already
+// scaled by c2/d.  Zero when no curl-term neighbour crosses the surface.
+template <int PAR, bool IS_E, int C>
+__device__ __noinline__ float obl_corr(const Args &a, int i, int j, int k) {
+    int P[3] = {2 * i, 2 * j, 2 * k};
+#pragma unroll
+    for (int q = 0; q < 3; q++)
+        if (IS_E ? q == C : q != C) P[q] += 1;
+    const int T = obl_in(a, P[0], P[1], P[2]);
+    constexpr int ax[2] = {(C + 1) % 3, (C + 2) % 3};
+    constexpr int comp[2] = {(C + 2) % 3, (C + 1) % 3};
+    constexpr int sg[2] = {IS_E ? 1 : -1, IS_E ? -1 : 1};
+    const float cd[3] = {IS_E ? a.cex : a.chx, IS_E ? a.cey : a.chy, IS_E ? a.cez : a.chz};
+    float acc = 0.f;
+#pragma unroll
+    for (int term = 0; term < 2; term++)
+#pragma unroll
+        for (int side = 1; side >= -1; side -= 2) {
+            int Q[3] = {P[0], P[1], P[2]};
+            Q[ax[term]] += side;
+            const int Tn = obl_in(a, Q[0], Q[1], Q[2]);
+            if (Tn == T) continue;
+            const float sp = a.kr[0] * (0.5f * Q[0]) + a.kr[1] * (0.5f * Q[1]) + a.kr[2] * (0.5f * Q[2]) + a.s0;
+            const float inc = IS_E ? a.kh[comp[term]] * obl_h_new_at<PAR>(a, sp - 0.5f)
+                                   : a.ke[comp[term]] * obl_e_at<PAR>(a, sp);
+            const float v = inc * cd[ax[term]];
+            acc += sg[term] * side * (T - Tn) > 0 ? v : -v;
+        }
+    return acc;
+}
+
 // Per-tile facts that are uniform across the CTA.
 struct TileInfo {
     bool clean;   // no y/z CPML, TF/SF, NTF, slice, plate or domain-edge rows/columns
@@ -221,15 +294,19 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         const float dEy = s.e[1][EIDX(dj, dk + 1)] - ey;
         float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
         if (!CLEAN) {
-            if (inbx && inbz) {
-                const float ezi = a.inc[PAR][1][i];
-                if (j == a.by1 - 1) h += a.chy * ezi;
-                if (j == a.by2 - 1) h -= a.chy * ezi;
-            }
-            if (inbx && inby) {
-                const float eyi = a.inc[PAR][0][i];
-                if (k == a.bz1 - 1) h -= a.chz * eyi;
-                if (k == a.bz2 - 1) h += a.chz * eyi;
+            if (!a.oblique) {
+                if (inbx && inbz) {
+                    const float ezi = a.inc[PAR][1][i];
+                    if (j == a.by1 - 1) h += a.chy * ezi;
+                    if (j == a.by2 - 1) h -= a.chy * ezi;
+                }
+                if (inbx && inby) {
+                    const float eyi = a.inc[PAR][0][i];
+                    if (k == a.bz1 - 1) h -= a.chz * eyi;
+                    if (k == a.bz2 - 1) h += a.chz * eyi;
+                }
+            } else if (obl_shell(a, i, j, k)) {
+                h += obl_corr<PAR, false, 0>(a, i, j, k);
             }
             if (a.dopml) {
                 const int sy = hslab(j, Ny, L, a.yshift);
@@ -238,6 +315,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                     const float p = a.Bh[sy] * a.Ph[PAR][0][o2] + a.Ahy[sy] * dEz;
                     if (store_psi) a.Ph[PAR ^ 1][0][o2] = p;
                     h -= a.c2h * p;
+                    if (a.kappa_on) h -= a.c2h * (a.Khy[sy] * dEz);
                 }
                 const int sz = hslab(k, Nz, L, a.zshift);
                 if (sz >= 0) {
@@ -245,6 +323,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                     const float p = a.Bh[sz] * a.Ph[PAR][1][o2] + a.Ahz[sz] * dEy;
                     if (store_psi) a.Ph[PAR ^ 1][1][o2] = p;
                     h += a.c2h * p;
+                    if (a.kappa_on) h += a.c2h * (a.Khz[sz] * dEy);
                 }
             }
         }
@@ -254,15 +333,20 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         const float dEx = s.e[0][EIDX(dj, dk + 1)] - ex;
         const float dEz = s1.e[2][EIDX(dj, dk)] - ez;
         float h = a.c1h * o.y - (a.chz * dEx - a.chx * dEz);
-        if (inby && inbz) {
-            if (i == a.bx1 - 1) h -= a.chx * a.inc[PAR][1][a.bx1];
-            if (i == a.bx2 - 1) h += a.chx * a.inc[PAR][1][a.bx2 - 1];
+        if (!a.oblique) {
+            if (inby && inbz) {
+                if (i == a.bx1 - 1) h -= a.chx * a.inc[PAR][1][a.bx1];
+                if (i == a.bx2 - 1) h += a.chx * a.inc[PAR][1][a.bx2 - 1];
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            h += obl_corr<PAR, false, 1>(a, i, j, k);
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
             const float p = a.Bh[sx] * (use_pf ? pf_yx : a.Ph[PAR][2][o2]) + a.Ahx[sx] * dEz;
             if (store_psi) a.Ph[PAR ^ 1][2][o2] = p;
             h += a.c2h * p;
+            if (a.kappa_on) h += a.c2h * (a.Khx[sx] * dEz);
         }
         if (!CLEAN && a.dopml) {
             const int sz = hslab(k, Nz, L, a.zshift);
@@ -271,6 +355,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                 const float p = a.Bh[sz] * a.Ph[PAR][3][o2] + a.Ahz[sz] * dEx;
                 if (store_psi) a.Ph[PAR ^ 1][3][o2] = p;
                 h -= a.c2h * p;
+                if (a.kappa_on) h -= a.c2h * (a.Khz[sz] * dEx);
             }
         }
         o.y = h;
@@ -279,15 +364,20 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         const float dEy = s1.e[1][EIDX(dj, dk)] - ey;
         const float dEx = s.e[0][EIDX(dj + 1, dk)] - ex;
         float h = a.c1h * o.z - (a.chx * dEy - a.chy * dEx);
-        if (inby && inbz) {
-            if (i == a.bx1 - 1) h += a.chx * a.inc[PAR][0][a.bx1];
-            if (i == a.bx2 - 1) h -= a.chx * a.inc[PAR][0][a.bx2 - 1];
+        if (!a.oblique) {
+            if (inby && inbz) {
+                if (i == a.bx1 - 1) h += a.chx * a.inc[PAR][0][a.bx1];
+                if (i == a.bx2 - 1) h -= a.chx * a.inc[PAR][0][a.bx2 - 1];
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            h += obl_corr<PAR, false, 2>(a, i, j, k);
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
             const float p = a.Bh[sx] * (use_pf ? pf_zx : a.Ph[PAR][4][o2]) + a.Ahx[sx] * dEy;
             if (store_psi) a.Ph[PAR ^ 1][4][o2] = p;
             h -= a.c2h * p;
+            if (a.kappa_on) h -= a.c2h * (a.Khx[sx] * dEy);
         }
         if (!CLEAN && a.dopml) {
             const int sy = hslab(j, Ny, L, a.yshift);
@@ -296,6 +386,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                 const float p = a.Bh[sy] * a.Ph[PAR][5][o2] + a.Ahy[sy] * dEx;
                 if (store_psi) a.Ph[PAR ^ 1][5][o2] = p;
                 h += a.c2h * p;
+                if (a.kappa_on) h += a.c2h * (a.Khy[sy] * dEx);
             }
         }
         o.z = h;
@@ -321,6 +412,41 @@ __device__ __forceinline__ float hzinc_new(const Args &a, int i) {
 template <int PAR>
 __device__ void line_update(const Args &a, int t) {
     const int Nx = a.Nx, L = a.L;
+    if (a.oblique) {  // auxiliary line along k: E in slot 1, H in slot 2, CPML at the far end
+        const int M = a.M;
+        const float *e = a.inc[PAR][1], *h = a.inc[PAR][2];
+        float *e2 = a.inc[PAR ^ 1][1], *h2 = a.inc[PAR ^ 1][2];
+        for (int n = threadIdx.x; n < M; n += blockDim.x) {
+            float v = h[n];
+            if (n < M - 1) {
+                v = a.c1h * h[n] - a.chl * (e[n + 1] - e[n]);
+                if (n >= M - L - 1) {
+                    const int s = n - a.ashift;
+                    const float p = a.Bh1[s] * a.incP[PAR][2][s] + a.Ah1[s] * (e[n + 1] - e[n]);
+                    a.incP[PAR ^ 1][2][s] = p;
+                    v -= a.c2h * p;
+                }
+            }
+            h2[n] = v;
+        }
+        __syncthreads();
+        for (int n = threadIdx.x; n < M; n += blockDim.x) {
+            float v = e[n];
+            if (n >= 1 && n < M - 1) {
+                v = a.c1e0 * e[n] - a.cel * (h2[n] - h2[n - 1]);
+                if (n >= M - L - 1) {
+                    const int s = n - a.ashift;
+                    const float p = a.Be1[s] * a.incP[PAR][1][s] + a.Ae1[s] * (h2[n] - h2[n - 1]);
+                    a.incP[PAR ^ 1][1][s] = p;
+                    v -= a.c2e0 * p;
+                }
+            } else if (n == 0) {
+                v = a.src[2 * t];
+            }
+            e2[n] = v;
+        }
+        return;
+    }
     const float *ey = a.inc[PAR][0], *ez = a.inc[PAR][1], *hy = a.inc[PAR][2], *hz = a.inc[PAR][3];
     float *ey2 = a.inc[PAR ^ 1][0], *ez2 = a.inc[PAR ^ 1][1], *hy2 = a.inc[PAR ^ 1][2],
           *hz2 = a.inc[PAR ^ 1][3];
@@ -429,8 +555,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     auto pf_load = [&](int qq, float &wq, float &nu, float &hyx, float &hzx, float &eyx, float &ezx) {
         if (!valid || qq >= Nx) return;
         const size_t ij = (size_t)qq * Ny + jj;
-        wq = a.wq2[ij];
-        if (JM == 0) nu = a.nu2[ij];
+        const size_t cq = (size_t)qq * plane + (size_t)jj * a.Nzp + kk;
+        wq = a.wq3 ? a.wq3[cq] : a.wq2[ij];
+        if (JM == 0) nu = a.nu3 ? a.nu3[cq] : a.nu2[ij];
         if (a.dopml) {
             const int sh = hslab(qq, Nx, L, a.xshift), se = eslab(qq, Nx, L, a.xshift);
             if (sh >= 0) {
@@ -513,9 +640,10 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         jy = ca * jy + cb * eyo;
                         jz = ca * jz + cb * ezo;
                     } else {
-                        const float m0 = 0.5f * (exo + ex_prev);
-                        const float m1 = 0.5f * (eyo + s.e[1][EIDX(dj - 1, dk)]);
-                        const float m2 = 0.5f * (ezo + s.e[2][EIDX(dj, dk - 1)]);
+                        const bool co = a.lk_colocated;
+                        const float m0 = co ? exo : 0.5f * (exo + ex_prev);
+                        const float m1 = co ? eyo : 0.5f * (eyo + s.e[1][EIDX(dj - 1, dk)]);
+                        const float m2 = co ? ezo : 0.5f * (ezo + s.e[2][EIDX(dj, dk - 1)]);
                         const float *m = JM == 1 ? a.lku : lkm;
                         float tbl[JM == 2 ? 18 : 1];
                         if (JM == 2 && a.lk_mode != LK_PER_K) {
@@ -594,9 +722,10 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                     jy = ca * jy + cb * eyc;
                     jz = ca * jz + cb * ezc;
                 } else {
-                    const float m0 = 0.5f * (exc + ex_prev);
-                    const float m1 = 0.5f * (eyc + s.e[1][EIDX(dj - 1, dk)]);
-                    const float m2 = 0.5f * (ezc + s.e[2][EIDX(dj, dk - 1)]);
+                    const bool co = a.lk_colocated;
+                    const float m0 = co ? exc : 0.5f * (exc + ex_prev);
+                    const float m1 = co ? eyc : 0.5f * (eyc + s.e[1][EIDX(dj - 1, dk)]);
+                    const float m2 = co ? ezc : 0.5f * (ezc + s.e[2][EIDX(dj, dk - 1)]);
                     const float *m = JM == 1 ? a.lku : lkm;
                     float tbl[JM == 2 ? 18 : 1];
                     if (JM == 2 && a.lk_mode != LK_PER_K) {
@@ -651,7 +780,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 const float dHy = hv.y - HN(1, dj, dk - 1);
                 float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
                 if (!CLEAN) {
-                    if (i >= a.bx1 && i < a.bx2 - 1) {
+                    if (a.oblique) {
+                        if (obl_shell(a, i, j, k)) e += obl_corr<PAR, true, 0>(a, i, j, k);
+                    } else if (i >= a.bx1 && i < a.bx2 - 1) {
                         if (inby) {
                             if (k == a.bz1) e += a.cez * hyinc_new<PAR>(a, i);
                             if (k == a.bz2) e -= a.cez * hyinc_new<PAR>(a, i);
@@ -668,6 +799,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                             const float p = a.Be[sy] * a.Pe[0][o2] + a.Aey[sy] * dHz;
                             a.Pe[0][o2] = p;
                             e += a.c2e0 * p;
+                            if (a.kappa_on) e += a.c2e0 * (a.Key[sy] * dHz);
                         }
                         const int sz = eslab(k, Nz, L, a.zshift);
                         if (sz >= 0) {
@@ -675,6 +807,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                             const float p = a.Be[sz] * a.Pe[1][o2] + a.Aez[sz] * dHy;
                             a.Pe[1][o2] = p;
                             e -= a.c2e0 * p;
+                            if (a.kappa_on) e -= a.c2e0 * (a.Kez[sz] * dHy);
                         }
                     }
                 }
@@ -685,9 +818,13 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 const float dHx = hv.x - HN(0, dj, dk - 1);
                 const float dHz = hv.z - hz_prev;
                 float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
-                if (inby && inbz) {
-                    if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
-                    if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
+                if (!a.oblique) {
+                    if (inby && inbz) {
+                        if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
+                        if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
+                    }
+                } else if (obl_shell(a, i, j, k)) {
+                    e += obl_corr<PAR, true, 1>(a, i, j, k);
                 }
                 if (sxe >= 0) {
                     float p = 0.f;
@@ -697,6 +834,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         a.Pe[2][o2] = p;
                     }
                     e -= a.c2e0 * p;
+                    if (a.kappa_on) e -= a.c2e0 * (a.Kex[sxe] * dHz);
                 }
                 if (!CLEAN && a.dopml) {
                     const int sz = eslab(k, Nz, L, a.zshift);
@@ -708,6 +846,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                             a.Pe[3][o2] = p;
                         }
                         e += a.c2e0 * p;
+                        if (a.kappa_on) e += a.c2e0 * (a.Kez[sz] * dHx);
                     }
                 }
                 ey = e;
@@ -722,9 +861,13 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 const float dHy = hv.y - hy_prev;
                 const float dHx = hv.x - HN(0, dj - 1, dk);
                 float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
-                if (inby && inbz) {
-                    if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
-                    if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
+                if (!a.oblique) {
+                    if (inby && inbz) {
+                        if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
+                        if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
+                    }
+                } else if (obl_shell(a, i, j, k)) {
+                    e += obl_corr<PAR, true, 2>(a, i, j, k);
                 }
                 if (ez_plate) e = 0.f;
                 ez_slice = e;
@@ -736,6 +879,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         a.Pe[4][o2] = p;
                     }
                     e += a.c2e0 * p;
+                    if (a.kappa_on) e += a.c2e0 * (a.Kex[sxe] * dHy);
                 }
                 if (!CLEAN && a.dopml) {
                     const int sy = eslab(j, Ny, L, a.yshift);
@@ -744,6 +888,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         const float p = a.Be[sy] * a.Pe[5][o2] + a.Aey[sy] * dHx;
                         a.Pe[5][o2] = p;
                         e -= a.c2e0 * p;
+                        if (a.kappa_on) e -= a.c2e0 * (a.Key[sy] * dHx);
                     }
                 }
                 ez = e;
@@ -1050,7 +1195,8 @@ int64_t Fp32Sim::footprint(const Problem &P) {
     const int64_t psi = P.dopml ? (L2 * P.Ny * P.Nz + (int64_t)P.Nx * L2 * P.Nz + (int64_t)P.Nx * P.Ny * L2) * 2 : 0;
     const int64_t nf2 = 2 * P.nntf();
     const int64_t ntf = 8 * nf2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz + (int64_t)P.Nx * P.Ny);
-    return cells * 4 * 15 + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2);
+    const int64_t maps = cells * 4 * ((P.wp3.empty() ? 0 : 1) + (P.nu3.empty() ? 0 : 1));
+    return cells * 4 * 15 + maps + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2);
 }
 
 void Fp32Sim::init(const Problem &P, void *stream) {
@@ -1080,7 +1226,23 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     a.csx = (float)(P.c2s / P.dx); a.csy = (float)(P.c2s / P.dy); a.csz = (float)(P.c2s / P.dz);
     a.dtf = (float)P.dt; a.c0di = (float)(2 * kE0 * P.dt);
     a.platesize = P.platesize;
+    a.kappa_on = P.kappa_on;
+    a.oblique = P.oblique;
+    a.lk_colocated = P.ext.lk_colocated;
+    if (P.oblique) {
+        a.M = P.M; a.ashift = P.ashift; a.s0 = (float)P.s0;
+        for (int q = 0; q < 3; q++) {
+            a.kr[q] = (float)P.kr[q]; a.ke[q] = (float)P.inc_e[q]; a.kh[q] = (float)P.inc_h[q];
+        }
+        a.chl = (float)(P.c2h / P.dl); a.cel = (float)(P.c2e0 / P.dl);
+        for (int q = 0; q < 2 * P.L; q++) {
+            a.Bh1[q] = (float)P.Bh1[q]; a.Ah1[q] = (float)(P.Ah1[q] / P.dl);
+            a.Be1[q] = (float)P.Be1[q]; a.Ae1[q] = (float)(P.Ae1[q] / P.dl);
+        }
+    }
     for (int q = 0; q < 2 * P.L; q++) {
+        a.Khx[q] = (float)(P.Kh[q] / P.dx); a.Khy[q] = (float)(P.Kh[q] / P.dy); a.Khz[q] = (float)(P.Kh[q] / P.dz);
+        a.Kex[q] = (float)(P.Ke[q] / P.dx); a.Key[q] = (float)(P.Ke[q] / P.dy); a.Kez[q] = (float)(P.Ke[q] / P.dz);
         a.Bh[q] = (float)P.Bh[q];
         a.Ahx[q] = (float)(P.Ah[q] / P.dx); a.Ahy[q] = (float)(P.Ah[q] / P.dy); a.Ahz[q] = (float)(P.Ah[q] / P.dz);
         a.Be[q] = (float)P.Be[q];
@@ -1103,16 +1265,33 @@ void Fp32Sim::init(const Problem &P, void *stream) {
             a.Pe[q] = m.alloc<float>(psz[q], s);
         }
     }
+    const size_t nline = std::max<size_t>(P.Nx, P.oblique ? (size_t)P.M : 0) + 1;
     for (int b = 0; b < 2; b++)
         for (int q = 0; q < 4; q++) {
-            a.inc[b][q] = m.alloc<float>(P.Nx + 1, s);
+            a.inc[b][q] = m.alloc<float>(nline, s);
             a.incP[b][q] = m.alloc<float>(L2, s);
         }
     {
         std::vector<float> wq2(P.wp2e.size()), nu2(P.nu2e.size()), G(P.Nz), G2(P.Nz);
         for (size_t q = 0; q < wq2.size(); q++) wq2[q] = (float)(kE0 * P.wp2e[q] * P.wp2e[q]);
         for (size_t q = 0; q < nu2.size(); q++) nu2[q] = (float)P.nu2e[q];
-        for (int k = 0; k < P.Nz; k++) { G[k] = (float)P.G[k]; G2[k] = (float)(P.G[k] * P.G[k]); }
+        // A per-cell map replaces the 2-D map times the z profile: its G factor is 1.
+        const bool w3 = !P.wp3.empty() && !P.doplate, n3 = !P.nu3.empty() && !P.doplate;
+        for (int k = 0; k < P.Nz; k++) {
+            G[k] = n3 ? 1.f : (float)P.G[k];
+            G2[k] = w3 ? 1.f : (float)(P.G[k] * P.G[k]);
+        }
+        auto per_cell = [&](const std::vector<double> &v, bool square) {
+            std::vector<float> out((size_t)P.Nx * P.Ny * m.Nzp, 0.f);
+            for (size_t ij = 0; ij < (size_t)P.Nx * P.Ny; ij++)
+                for (int k = 0; k < P.Nz; k++) {
+                    const double x = v[ij * P.Nz + k];
+                    out[ij * m.Nzp + k] = (float)(square ? kE0 * x * x : x);
+                }
+            return out;
+        };
+        a.wq3 = w3 ? m.upload(per_cell(P.wp3, true), s) : nullptr;
+        a.nu3 = n3 ? m.upload(per_cell(P.nu3, false), s) : nullptr;
         a.wq2 = m.upload(wq2, s); a.nu2 = m.upload(nu2, s); a.G = m.upload(G, s); a.G2 = m.upload(G2, s);
         std::vector<float> lk(P.lk.begin(), P.lk.end());
         a.lk = m.upload(lk, s);

@@ -57,6 +57,60 @@ __device__ __forceinline__ int eslab(int n, int N, int L, int shift) {
     return -1;
 }
 
+// ---- oblique incidence (extended inputs) ----------------------------------
+// The incident field comes from a 1-D auxiliary line along k (E in Ezinc, H in
+// Hyinc).  A node with doubled coordinates P sees the line at
+// s = kr . P/2 + s0, E nodes at s and H nodes at s - 1/2, interpolated
+// linearly.  Every curl term whose neighbour lies on the other side of the
+// TF/SF box surface is corrected with the neighbour's incident value.  Same
+// expression trees as the oracle, so the FP64 results are bit-identical.
+__device__ __forceinline__ bool obl_in(const PlainArgs &a, const int P[3]) {
+    return P[0] >= 2 * a.bx1 && P[0] <= 2 * (a.bx2 - 1) && P[1] >= 2 * a.by1 &&
+           P[1] <= 2 * (a.by2 - 1) && P[2] >= 2 * a.bz1 && P[2] <= 2 * (a.bz2 - 1);
+}
+__device__ __forceinline__ double obl_line(const double *line, double s) {
+    const double fl = floor(s);
+    const int n = (int)fl;
+    const double w = s - fl;
+    return line[n] + w * (line[n + 1] - line[n]);
+}
+__device__ __forceinline__ bool obl_shell(const PlainArgs &a, int i, int j, int k) {
+    return i >= a.bx1 - 1 && i <= a.bx2 && j >= a.by1 - 1 && j <= a.by2 && k >= a.bz1 - 1 &&
+           k <= a.bz2 &&
+           !(i > a.bx1 && i < a.bx2 - 2 && j > a.by1 && j < a.by2 - 2 && k > a.bz1 && k < a.bz2 - 2);
+}
+// Correction of component c of the target field (E when is_e) at (i,j,k);
+// returns false when no curl-term neighbour crosses the box surface.
+__device__ bool obl_corr(const PlainArgs &a, bool is_e, int c, int i, int j, int k, double *corr) {
+    int P[3] = {2 * i, 2 * j, 2 * k};
+    for (int q = 0; q < 3; q++)
+        if (is_e ? q == c : q != c) P[q] += 1;
+    const bool T = obl_in(a, P);
+    const int ax[2] = {(c + 1) % 3, (c + 2) % 3};
+    const int comp[2] = {(c + 2) % 3, (c + 1) % 3};
+    const int sg[2] = {is_e ? 1 : -1, is_e ? -1 : 1};
+    const double d[3] = {a.dx, a.dy, a.dz};
+    const double *line = is_e ? a.Hyinc : a.Ezinc;  // the neighbour field's line
+    double acc = 0;
+    bool any = false;
+    for (int term = 0; term < 2; term++)
+        for (int side = 1; side >= -1; side -= 2) {
+            int Q[3] = {P[0], P[1], P[2]};
+            Q[ax[term]] += side;
+            const bool Tn = obl_in(a, Q);
+            if (Tn == T) continue;
+            const double sp = ((a.kr[0] * (0.5 * Q[0]) + a.kr[1] * (0.5 * Q[1])) + a.kr[2] * (0.5 * Q[2])) + a.s0;
+            const double inc = is_e ? a.kh[comp[term]] * obl_line(line, sp - 0.5)
+                                    : a.ke[comp[term]] * obl_line(line, sp);
+            const double v = inc / d[ax[term]];
+            if (sg[term] * side * ((int)T - (int)Tn) > 0) acc = acc + v;
+            else acc = acc - v;
+            any = true;
+        }
+    *corr = acc;
+    return any;
+}
+
 __device__ __forceinline__ bool in_sphere(const PlainArgs &a, int i, int j, int k) {
     double x = a.xc[i], y = a.yc[j], z = a.zc[k];
     double dist = sqrt(x * x + y * y + z * z);
@@ -76,9 +130,9 @@ __global__ void __launch_bounds__(256) k_plain_h(PlainArgs a, int t) {
     // ---- J update of step t-1 (source/meteor-fork.cpp:1523-1595) ----
     if (t > 0 && i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1) {
         const size_t ij = (size_t)i * Ny + j;
-        const double wpe = a.doplate ? 0.0 : a.wp2[ij] * a.G[k];
+        const double wpe = a.doplate ? 0.0 : a.wp3 ? a.wp3[c] : a.wp2[ij] * a.G[k];
         if (!a.doB0) {
-            const double nue = a.doplate ? 0.0 : a.nu2[ij] * a.G[k];
+            const double nue = a.doplate ? 0.0 : a.nu3 ? a.nu3[c] : a.nu2[ij] * a.G[k];
             const double dt = a.dt;
             const double ca = (2 - nue * dt) / (2 + nue * dt);
             const double cb = 2 * ((kE0 * wpe * wpe * dt) / (2 + nue * dt));
@@ -88,9 +142,11 @@ __global__ void __launch_bounds__(256) k_plain_h(PlainArgs a, int t) {
         } else {
             size_t e = a.lk_mode == LK_PER_K ? (size_t)k : a.lk_mode == LK_PER_IJ ? ij : c;
             const double *m = a.lk + e * kLkStride;
-            const double m0 = (a.Ex[c] + a.Ex[c - sI]) / 2;
-            const double m1 = (a.Ey[c] + a.Ey[c - sJ]) / 2;
-            const double m2 = (a.Ez[c] + a.Ez[c - 1]) / 2;
+            // E averaged over two nodes as the reference does, or (extended
+            // input) E at the current's own node.
+            const double m0 = a.lk_colocated ? a.Ex[c] : (a.Ex[c] + a.Ex[c - sI]) / 2;
+            const double m1 = a.lk_colocated ? a.Ey[c] : (a.Ey[c] + a.Ey[c - sJ]) / 2;
+            const double m2 = a.lk_colocated ? a.Ez[c] : (a.Ez[c] + a.Ez[c - 1]) / 2;
             const double jx = a.Jx[c], jy = a.Jy[c], jz = a.Jz[c];
             const double q = kE0 * wpe * wpe;
             a.Jx[c] = m[0] * jx + m[1] * jy + m[2] * jz + q * (m[9] * m0 + m[10] * m1 + m[11] * m2);
@@ -124,16 +180,21 @@ __global__ void __launch_bounds__(256) k_plain_h(PlainArgs a, int t) {
             }
         }
         double h = a.c1h * a.Hx[c] - a.c2h * (dEz / a.dy - dEy / a.dz);
-        if (inbx && inbz) {
-            if (j == a.by1 - 1) h = h + a.c2h * a.Ezinc[i] / a.dy;
-            if (j == a.by2 - 1) h = h - a.c2h * a.Ezinc[i] / a.dy;
+        if (!a.oblique) {
+            if (inbx && inbz) {
+                if (j == a.by1 - 1) h = h + a.c2h * a.Ezinc[i] / a.dy;
+                if (j == a.by2 - 1) h = h - a.c2h * a.Ezinc[i] / a.dy;
+            }
+            if (inbx && inby) {
+                if (k == a.bz1 - 1) h = h - a.c2h * a.Eyinc[i] / a.dz;
+                if (k == a.bz2 - 1) h = h + a.c2h * a.Eyinc[i] / a.dz;
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            double corr;
+            if (obl_corr(a, false, 0, i, j, k, &corr)) h = h + a.c2h * corr;
         }
-        if (inbx && inby) {
-            if (k == a.bz1 - 1) h = h - a.c2h * a.Eyinc[i] / a.dz;
-            if (k == a.bz2 - 1) h = h + a.c2h * a.Eyinc[i] / a.dz;
-        }
-        if (sy >= 0) h = h - a.c2h * py;
-        if (sz >= 0) h = h + a.c2h * pz;
+        if (sy >= 0) h = h - a.c2h * (a.kappa_on ? py + a.Kh[sy] * dEz / a.dy : py);
+        if (sz >= 0) h = h + a.c2h * (a.kappa_on ? pz + a.Kh[sz] * dEy / a.dz : pz);
         a.Hx[c] = h;
     }
 
@@ -158,12 +219,17 @@ __global__ void __launch_bounds__(256) k_plain_h(PlainArgs a, int t) {
             }
         }
         double h = a.c1h * a.Hy[c] - a.c2h * (dEx / a.dz - dEz / a.dx);
-        if (inby && inbz) {
-            if (i == a.bx1 - 1) h = h - a.c2h * a.Ezinc[a.bx1] / a.dx;
-            if (i == a.bx2 - 1) h = h + a.c2h * a.Ezinc[a.bx2 - 1] / a.dx;
+        if (!a.oblique) {
+            if (inby && inbz) {
+                if (i == a.bx1 - 1) h = h - a.c2h * a.Ezinc[a.bx1] / a.dx;
+                if (i == a.bx2 - 1) h = h + a.c2h * a.Ezinc[a.bx2 - 1] / a.dx;
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            double corr;
+            if (obl_corr(a, false, 1, i, j, k, &corr)) h = h + a.c2h * corr;
         }
-        if (sx >= 0) h = h + a.c2h * px;
-        if (sz >= 0) h = h - a.c2h * pz;
+        if (sx >= 0) h = h + a.c2h * (a.kappa_on ? px + a.Kh[sx] * dEz / a.dx : px);
+        if (sz >= 0) h = h - a.c2h * (a.kappa_on ? pz + a.Kh[sz] * dEx / a.dz : pz);
         a.Hy[c] = h;
     }
 
@@ -188,17 +254,37 @@ __global__ void __launch_bounds__(256) k_plain_h(PlainArgs a, int t) {
             }
         }
         double h = a.c1h * a.Hz[c] - a.c2h * (dEy / a.dx - dEx / a.dy);
-        if (inby && inbz) {
-            if (i == a.bx1 - 1) h = h + a.c2h * a.Eyinc[a.bx1] / a.dx;
-            if (i == a.bx2 - 1) h = h - a.c2h * a.Eyinc[a.bx2 - 1] / a.dx;
+        if (!a.oblique) {
+            if (inby && inbz) {
+                if (i == a.bx1 - 1) h = h + a.c2h * a.Eyinc[a.bx1] / a.dx;
+                if (i == a.bx2 - 1) h = h - a.c2h * a.Eyinc[a.bx2 - 1] / a.dx;
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            double corr;
+            if (obl_corr(a, false, 2, i, j, k, &corr)) h = h + a.c2h * corr;
         }
-        if (sx >= 0) h = h - a.c2h * px;
-        if (sy >= 0) h = h + a.c2h * py;
+        if (sx >= 0) h = h - a.c2h * (a.kappa_on ? px + a.Kh[sx] * dEy / a.dx : px);
+        if (sy >= 0) h = h + a.c2h * (a.kappa_on ? py + a.Kh[sy] * dEx / a.dy : py);
         a.Hz[c] = h;
     }
 
+    // ---- oblique incidence: auxiliary line, H part (nodes n = i, i + Nx, ...)
+    if (a.oblique && j == 0 && k == 0) {
+        const int M = a.M;
+        for (int n = i; n < M - 1; n += Nx) {
+            double h = a.c1h * a.Hyinc[n] - a.c2h * (a.Ezinc[n + 1] - a.Ezinc[n]) / a.dl;
+            if (n >= M - L - 1) {
+                const int s = n - a.ashift;
+                const double p = a.Bh1[s] * a.PhyxI[s] + a.Ah1[s] * (a.Ezinc[n + 1] - a.Ezinc[n]) / a.dl;
+                a.PhyxI[s] = p;
+                h = h - a.c2h * p;
+            }
+            a.Hyinc[n] = h;
+        }
+    }
+
     // ---- 1-D incident line, H part (:705-706, 741-742, 833, 892, 863, 923)
-    if (j == 0 && k == 0 && i < Nx - 1) {
+    if (!a.oblique && j == 0 && k == 0 && i < Nx - 1) {
         const int s = (a.dopml && i >= Nx - L - 1) ? i - a.xshift : -1;
         double pyI = 0, pzI = 0;
         if (s >= 0) {
@@ -266,18 +352,23 @@ __global__ void __launch_bounds__(256) k_plain_e(PlainArgs a, int t, int record)
             }
         }
         double e = c1e * ex + c2e * (dHz / a.dy - dHy / a.dz) - c2e * a.Jx[c];
-        if (i >= a.bx1 && i < a.bx2 - 1) {
-            if (j >= a.by1 && j < a.by2) {
-                if (k == a.bz1) e = e + c2e0 * a.Hyinc[i] / a.dz;
-                if (k == a.bz2) e = e - c2e0 * a.Hyinc[i] / a.dz;
+        if (!a.oblique) {
+            if (i >= a.bx1 && i < a.bx2 - 1) {
+                if (j >= a.by1 && j < a.by2) {
+                    if (k == a.bz1) e = e + c2e0 * a.Hyinc[i] / a.dz;
+                    if (k == a.bz2) e = e - c2e0 * a.Hyinc[i] / a.dz;
+                }
+                if (k >= a.bz1 && k < a.bz2) {
+                    if (j == a.by1) e = e - c2e0 * a.Hzinc[i] / a.dy;
+                    if (j == a.by2) e = e + c2e0 * a.Hzinc[i] / a.dy;
+                }
             }
-            if (k >= a.bz1 && k < a.bz2) {
-                if (j == a.by1) e = e - c2e0 * a.Hzinc[i] / a.dy;
-                if (j == a.by2) e = e + c2e0 * a.Hzinc[i] / a.dy;
-            }
+        } else if (obl_shell(a, i, j, k)) {
+            double corr;
+            if (obl_corr(a, true, 0, i, j, k, &corr)) e = e + c2e0 * corr;
         }
-        if (sy >= 0) e = e + c2e0 * py;
-        if (sz >= 0) e = e - c2e0 * pz;
+        if (sy >= 0) e = e + c2e0 * (a.kappa_on ? py + a.Ke[sy] * dHz / a.dy : py);
+        if (sz >= 0) e = e - c2e0 * (a.kappa_on ? pz + a.Ke[sz] * dHy / a.dz : pz);
         ex = e;
         a.Ex[c] = e;
     }
@@ -303,12 +394,17 @@ __global__ void __launch_bounds__(256) k_plain_e(PlainArgs a, int t, int record)
             a.Peyz[o] = pz;
         }
         double e = c1e * ey + c2e * (dHx / a.dz - dHz / a.dx) - c2e * a.Jy[c];
-        if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
-            if (i == a.bx1) e = e + c2e0 * a.Hzinc[a.bx1 - 1] / a.dx;
-            if (i == a.bx2 - 1) e = e - c2e0 * a.Hzinc[a.bx2 - 1] / a.dx;
+        if (!a.oblique) {
+            if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
+                if (i == a.bx1) e = e + c2e0 * a.Hzinc[a.bx1 - 1] / a.dx;
+                if (i == a.bx2 - 1) e = e - c2e0 * a.Hzinc[a.bx2 - 1] / a.dx;
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            double corr;
+            if (obl_corr(a, true, 1, i, j, k, &corr)) e = e + c2e0 * corr;
         }
-        if (sx >= 0) e = e - c2e0 * px;
-        if (sz >= 0) e = e + c2e0 * pz;
+        if (sx >= 0) e = e - c2e0 * (a.kappa_on ? px + a.Ke[sx] * dHz / a.dx : px);
+        if (sz >= 0) e = e + c2e0 * (a.kappa_on ? pz + a.Ke[sz] * dHx / a.dz : pz);
         if (plate_row && j >= a.plate_lo && j < a.plate_up - 1 && k >= a.plate_lo && k < a.plate_up)
             e = 0;
         ey = e;
@@ -339,15 +435,20 @@ __global__ void __launch_bounds__(256) k_plain_e(PlainArgs a, int t, int record)
             a.Pezy[o] = py;
         }
         double e = c1e * ez + c2e * (dHy / a.dx - dHx / a.dy) - c2e * a.Jz[c];
-        if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
-            if (i == a.bx1) e = e - c2e0 * a.Hyinc[a.bx1 - 1] / a.dx;
-            if (i == a.bx2 - 1) e = e + c2e0 * a.Hyinc[a.bx2 - 1] / a.dx;
+        if (!a.oblique) {
+            if (j >= a.by1 && j < a.by2 && k >= a.bz1 && k < a.bz2) {
+                if (i == a.bx1) e = e - c2e0 * a.Hyinc[a.bx1 - 1] / a.dx;
+                if (i == a.bx2 - 1) e = e + c2e0 * a.Hyinc[a.bx2 - 1] / a.dx;
+            }
+        } else if (obl_shell(a, i, j, k)) {
+            double corr;
+            if (obl_corr(a, true, 2, i, j, k, &corr)) e = e + c2e0 * corr;
         }
         if (plate_row && j >= a.plate_lo && j < a.plate_up && k >= a.plate_lo && k < a.plate_up - 1)
             e = 0;
         ez_slice = e;  // slices see Ez before its CPML correction
-        if (sx >= 0) e = e + c2e0 * px;
-        if (sy >= 0 && k < Nz - 1) e = e - c2e0 * py;
+        if (sx >= 0) e = e + c2e0 * (a.kappa_on ? px + a.Ke[sx] * dHy / a.dx : px);
+        if (sy >= 0 && k < Nz - 1) e = e - c2e0 * (a.kappa_on ? py + a.Ke[sy] * dHx / a.dy : py);
         ez = e;
         a.Ez[c] = e;
     } else if (plate_row && j >= a.plate_lo && j < a.plate_up && k >= a.plate_lo &&
@@ -359,7 +460,24 @@ __global__ void __launch_bounds__(256) k_plain_e(PlainArgs a, int t, int record)
 
     // ---- 1-D incident line, E part and source (:1201, 1259, 1069-1071,
     //      1105-1107, 1227-1229, 1355-1357, 1278-1304)
-    if (j == 0 && k == 0) {
+    if (a.oblique && j == 0 && k == 0) {  // auxiliary line, E part, and the source
+        const int M = a.M;
+        for (int n = i; n < M - 1; n += Nx) {
+            if (n == 0) {
+                a.Ezinc[0] = a.src[2 * t];
+                continue;
+            }
+            double e = a.c1e0 * a.Ezinc[n] - c2e0 * (a.Hyinc[n] - a.Hyinc[n - 1]) / a.dl;
+            if (n >= M - L - 1) {
+                const int s = n - a.ashift;
+                const double p = a.Be1[s] * a.PezxI[s] + a.Ae1[s] * (a.Hyinc[n] - a.Hyinc[n - 1]) / a.dl;
+                a.PezxI[s] = p;
+                e = e - c2e0 * p;
+            }
+            a.Ezinc[n] = e;
+        }
+    }
+    if (!a.oblique && j == 0 && k == 0) {
         if (i >= 1 && i < Nx - 1) {
             const int s = (a.dopml && i >= Nx - L - 1) ? i - a.xshift : -1;
             double pyI = 0, pzI = 0;

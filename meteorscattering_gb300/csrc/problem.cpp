@@ -50,7 +50,131 @@ std::vector<unsigned char> slurp(const std::string &path) {
     return b;
 }
 
+bool file_exists(const std::string &path) {
+    FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) return false;
+    std::fclose(f);
+    return true;
+}
+
+// Optional extended inputs of a run directory: ext.dat (88 bytes, layout in
+// rundir.py write_ext) and the per-cell maps it announces.  The reference
+// never writes these files, so its run directories are unaffected.
+void read_ext_sidecars(const std::string &dir, Problem &P) {
+    const std::string path = dir + "/ext.dat";
+    if (!file_exists(path)) return;
+    Reader r;
+    r.name = path;
+    r.buf = slurp(path);
+    if (r.buf.size() < 8 || std::memcmp(r.buf.data(), "MFDTDX01", 8) != 0)
+        throw Error(MFDTD_EIO, path + ": not an extended-input file (bad magic)");
+    r.off = 8;
+    mfdtd_ext e;
+    e.pmllen = r.get<int32_t>();
+    e.tfsf_gap = r.get<int32_t>();
+    e.ntf_gap = r.get<int32_t>();
+    e.oblique = r.get<int32_t>();
+    e.exact_coords = r.get<int32_t>();
+    const int has_wp3 = r.get<int32_t>();
+    const int has_nu3 = r.get<int32_t>();
+    e.lk_colocated = r.get<int32_t>();
+    e.pml_m = r.get<double>();
+    e.kappa_max = r.get<double>();
+    e.alpha_max = r.get<double>();
+    e.inc_theta = r.get<double>();
+    e.inc_phi = r.get<double>();
+    e.inc_psi = r.get<double>();
+    P.ext = e;
+    P.ext_present = 1;
+    const size_t n3 = P.cells();
+    for (int q = 0; q < 2; q++) {
+        if (!(q == 0 ? has_wp3 : has_nu3)) continue;
+        Reader w;
+        w.name = dir + (q == 0 ? "/wp3.dat" : "/nu3.dat");
+        w.buf = slurp(w.name);
+        if (w.buf.size() < n3 * 8)
+            throw Error(MFDTD_EIO, w.name + ": expected " + std::to_string(n3 * 8) + " bytes");
+        std::vector<double> &dst = q == 0 ? P.wp3 : P.nu3;
+        dst.resize(n3);
+        std::memcpy(dst.data(), w.buf.data(), n3 * 8);
+    }
+}
+
+// Numerical wavenumber of the 3-D Yee grid along the unit vector u at angular
+// frequency w: the root of sum_q (sin(k u_q d_q / 2) / d_q)^2 =
+// (sin(w dt / 2) / (c dt))^2 (the Yee dispersion relation), by bisection.
+double yee3_wavenumber(double w, double dt, double c, const double d[3], const double u[3]) {
+    const double S = sin(w * dt / 2) / (c * dt);
+    const double S2 = S * S;
+    double lo = 0.5 * w / c, hi = 4 * w / c;
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        double f = 0;
+        for (int q = 0; q < 3; q++) {
+            const double v = sin(mid * u[q] * d[q] / 2) / d[q];
+            f = f + v * v;
+        }
+        if (f < S2) lo = mid;
+        else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// Cell size of a 1-D Yee line whose numerical wavenumber at w equals k:
+// the root of sin(k D / 2) / D = sin(w dt / 2) / (c dt), by bisection.
+double matched_line_cell(double k, double w, double dt, double c, double dmin, double dmax) {
+    const double S = sin(w * dt / 2) / (c * dt);
+    double lo = 0.25 * dmin, hi = 2 * dmax;
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (sin(k * mid / 2) / mid > S) lo = mid;
+        else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+// CPML recursion tables for slab index m in [L, 2L) (the low side mirrors
+// it), source/meteor-2.1.cpp:411-526 with the grading order, kappa_max and
+// alpha_max as parameters.  Ke/Kh (may be null) receive 1/kappa - 1.
+void cpml_tables(int pmllen, double pmlm, double kamax, double almax, double dx, double dt,
+                 double *Be, double *Ae, double *Bh, double *Ah, double *Ke, double *Kh) {
+    double simax = 1.5 * (double)(pmlm + 1) / (150 * kPI * dx);
+    for (int m = pmllen; m < 2 * pmllen; m++) {
+        int n = m - pmllen;
+        double mf = (double)n;
+        double s = simax * pow(((mf + 0.5) / pmllen), pmlm);
+        double sm = simax * pow(((mf + 1) / pmllen), pmlm);
+        double ka = 1 + (kamax - 1) * pow(((mf + 0.5) / pmllen), pmlm);
+        double kam = 1 + (kamax - 1) * pow(((mf + 1) / pmllen), pmlm);
+        double al = almax * pow(((pmllen - mf - 0.5) / pmllen), pmlm);
+        double alm = almax * pow(((pmllen - mf - 1) / pmllen), pmlm);
+        Be[m] = exp(-((s / ka) + al) * dt / kE0);
+        Ae[m] = s / (s * ka + pow(ka, 2) * al) * (Be[m] - 1);
+        Bh[m] = exp(-((sm / kam) + alm) * dt / kE0);
+        Ah[m] = sm / (sm * kam + pow(kam, 2) * alm) * (Bh[m] - 1);
+        if (Ke) Ke[m] = 1 / ka - 1;
+        if (Kh) Kh[m] = 1 / kam - 1;
+    }
+    for (int m = 0; m < pmllen; m++) {
+        Be[m] = Be[2 * pmllen - 1 - m]; Ae[m] = Ae[2 * pmllen - 1 - m];
+        Bh[m] = Bh[2 * pmllen - 1 - m]; Ah[m] = Ah[2 * pmllen - 1 - m];
+        if (Ke) Ke[m] = Ke[2 * pmllen - 1 - m];
+        if (Kh) Kh[m] = Kh[2 * pmllen - 1 - m];
+    }
+}
+
 }  // namespace
+
+void ext_defaults(mfdtd_ext &e) {
+    std::memset(&e, 0, sizeof e);
+    e.pmllen = 10;
+    e.tfsf_gap = 10;
+    e.ntf_gap = 5;
+    e.pml_m = 4;
+    e.kappa_max = 1;
+    e.alpha_max = 0;
+    e.inc_theta = kPI / 2;
+}
 
 // inputs.dat: source/meteor-2.1.cpp:84-112, doB0 source/meteor-fork.cpp:115.
 Problem problem_from_rundir(const std::string &dir) {
@@ -112,6 +236,7 @@ Problem problem_from_rundir(const std::string &dir) {
         dst.resize(n2);
         std::memcpy(dst.data(), w.buf.data(), n2 * 8);
     }
+    read_ext_sidecars(dir, P);
     P.derive();
     return P;
 }
@@ -145,7 +270,24 @@ Problem problem_from_params(const mfdtd_params &p, const double *wp2, const doub
 }
 
 void Problem::derive() {
-    L = 10;  // source/meteor-2.1.cpp:343
+    if (!ext_present) ext_defaults(ext);
+    L = ext.pmllen;  // source/meteor-2.1.cpp:343 (10)
+    if (ext_present) {
+        if (L < 1 || L > kMaxPml) throw Error(MFDTD_EINVAL, "pmllen must be in [1, 32]");
+        if (ext.tfsf_gap < 2 || ext.ntf_gap < 1 || ext.ntf_gap > ext.tfsf_gap - 2)
+            throw Error(MFDTD_EINVAL, "need tfsf_gap >= 2 and 1 <= ntf_gap <= tfsf_gap - 2 "
+                                      "(Huygens surface between the CPML and the TF/SF box)");
+        if (!(ext.pml_m >= 0) || !(ext.kappa_max >= 1) || !(ext.alpha_max >= 0))
+            throw Error(MFDTD_EINVAL, "need pml_m >= 0, kappa_max >= 1, alpha_max >= 0");
+        const int need = 2 * (L + ext.tfsf_gap) + 3;
+        if (Nx < need || Ny < need || Nz < need)
+            throw Error(MFDTD_EINVAL, "grid must be at least " + std::to_string(need) +
+                                          " cells along each axis for this CPML and TF/SF box");
+        if (!wp3.empty() && wp3.size() != cells())
+            throw Error(MFDTD_EINVAL, "wp3 must hold Nx*Ny*Nz values");
+        if (!nu3.empty() && nu3.size() != cells())
+            throw Error(MFDTD_EINVAL, "nu3 must hold Nx*Ny*Nz values");
+    }
     if (Nx < 2 * L + 2 || Ny < 2 * L + 2 || Nz < 2 * L + 2)
         throw Error(MFDTD_EINVAL, "grid must be at least 22 cells along each axis "
                                   "(two 10-cell CPML slabs that do not overlap)");
@@ -171,10 +313,16 @@ void Problem::derive() {
     dz = lambda / gridfactor;
     int nmax = std::max(Nx, std::max(Ny, Nz));
     x.assign(nmax, 0.0); y.assign(nmax, 0.0); z.assign(nmax, 0.0);
-    for (int i = 0; i < Nx; i++) {
-        x[i] = -(Nx - 1) / 2 * dx + dx * i;
-        y[i] = -(Ny - 1) / 2 * dy + dy * i;
-        z[i] = -(Nz - 1) / 2 * dz + dz * i;
+    if (ext.exact_coords) {
+        for (int i = 0; i < Nx; i++) x[i] = -(Nx - 1) / 2.0 * dx + dx * i;
+        for (int i = 0; i < Ny; i++) y[i] = -(Ny - 1) / 2.0 * dy + dy * i;
+        for (int i = 0; i < Nz; i++) z[i] = -(Nz - 1) / 2.0 * dz + dz * i;
+    } else {
+        for (int i = 0; i < Nx; i++) {
+            x[i] = -(Nx - 1) / 2 * dx + dx * i;
+            y[i] = -(Ny - 1) / 2 * dy + dy * i;
+            z[i] = -(Nz - 1) / 2 * dz + dz * i;
+        }
     }
     ssx = (Nx + 1) / 2;
     ssy = (Ny + 1) / 2;
@@ -199,6 +347,11 @@ void Problem::derive() {
                 B = cos(2 * PI * f0 * t * dt);
             }
             double ez, ey;
+            if (ext.oblique) {  // one waveform on the auxiliary line
+                src[2 * t] = A;
+                src[2 * t + 1] = 0;
+                continue;
+            }
             switch (sourcepol) {
             case 2: ez = 0; ey = A; break;
             case 3: ez = A; ey = A; break;
@@ -272,11 +425,16 @@ void Problem::derive() {
     // collision frequency, so they are tabulated once per distinct value.
     if (doB0) {
         bool nu_uniform = true;
-        for (size_t q = 1; q < nu2e.size(); q++)
-            if (std::memcmp(&nu2e[q], &nu2e[0], 8) != 0) { nu_uniform = false; break; }
         bool g_one = true;
-        for (int k = 0; k < Nz; k++)
-            if (!(G[k] == 1.0)) { g_one = false; break; }
+        if (!nu3.empty()) {  // per-cell map: uniform, or one entry per cell
+            for (size_t q = 1; q < nu3.size(); q++)
+                if (std::memcmp(&nu3[q], &nu3[0], 8) != 0) { nu_uniform = false; g_one = false; break; }
+        } else {
+            for (size_t q = 1; q < nu2e.size(); q++)
+                if (std::memcmp(&nu2e[q], &nu2e[0], 8) != 0) { nu_uniform = false; break; }
+            for (int k = 0; k < Nz; k++)
+                if (!(G[k] == 1.0)) { g_one = false; break; }
+        }
         if (doplate) nu_uniform = true;  // nue is exactly zero everywhere
         size_t entries;
         if (nu_uniform) { lk_mode = LK_PER_K; entries = Nz; }
@@ -317,7 +475,12 @@ void Problem::derive() {
         };
         // The cell value is nu2[i][j] * G[k] (one rounding), as in the reference;
         // with a plate or sphere scatterer it is exactly 0 (memset, :330-334).
-        auto nu_at = [&](size_t ij, int k) { return doplate ? 0.0 : nu2e[ij] * G[k]; };
+        // With a per-cell map the cell value is nu3 itself.
+        auto nu_at = [&](size_t ij, int k) {
+            if (doplate) return 0.0;
+            if (!nu3.empty()) return nu3[ij * Nz + k];
+            return nu2e[ij] * G[k];
+        };
         if (lk_mode == LK_PER_K) {
             for (int k = 0; k < Nz; k++) fill(&lk[(size_t)k * kLkStride], nu_at(0, k));
         } else if (lk_mode == LK_PER_IJ) {
@@ -331,41 +494,81 @@ void Problem::derive() {
         }
     }
 
-    // CPML, source/meteor-2.1.cpp:411-526 (m=4, kappa=1, alpha=0; the H
-    // tables also use E0, :478-496).
+    // CPML, source/meteor-2.1.cpp:411-526 (reference: m=4, kappa=1, alpha=0;
+    // the H tables also use E0, :478-496).  kappa != 1 adds a (1/kappa - 1)
+    // derivative term to each CPML correction (the reference's field update
+    // has no 1/kappa factor).
     Be.assign(2 * L, 0.0); Ae.assign(2 * L, 0.0); Bh.assign(2 * L, 0.0); Ah.assign(2 * L, 0.0);
-    if (dopml) {
-        const double pmlm = 4;
-        const int pmllen = L;
-        double simax = 1.5 * (double)(pmlm + 1) / (150 * kPI * dx);
-        double kamax = 1, almax = 0;
-        for (int m = pmllen; m < 2 * pmllen; m++) {
-            int n = m - pmllen;
-            double mf = (double)n;
-            double s = simax * pow(((mf + 0.5) / pmllen), pmlm);
-            double sm = simax * pow(((mf + 1) / pmllen), pmlm);
-            double ka = 1 + (kamax - 1) * pow(((mf + 0.5) / pmllen), pmlm);
-            double kam = 1 + (kamax - 1) * pow(((mf + 1) / pmllen), pmlm);
-            double al = almax * pow(((pmllen - mf - 0.5) / pmllen), pmlm);
-            double alm = almax * pow(((pmllen - mf - 1) / pmllen), pmlm);
-            Be[m] = exp(-((s / ka) + al) * dt / kE0);
-            Ae[m] = s / (s * ka + pow(ka, 2) * al) * (Be[m] - 1);
-            Bh[m] = exp(-((sm / kam) + alm) * dt / kE0);
-            Ah[m] = sm / (sm * kam + pow(kam, 2) * alm) * (Bh[m] - 1);
-        }
-        for (int m = 0; m < pmllen; m++) {
-            Be[m] = Be[2 * pmllen - 1 - m]; Ae[m] = Ae[2 * pmllen - 1 - m];
-            Bh[m] = Bh[2 * pmllen - 1 - m]; Ah[m] = Ah[2 * pmllen - 1 - m];
-        }
-    }
+    Ke.assign(2 * L, 0.0); Kh.assign(2 * L, 0.0);
+    kappa_on = dopml && ext.kappa_max != 1.0;
+    if (dopml)
+        cpml_tables(L, ext.pml_m, ext.kappa_max, ext.alpha_max, dx, dt, Be.data(), Ae.data(),
+                    Bh.data(), Ah.data(), Ke.data(), Kh.data());
     xshift = Nx - 2 * L - 1;
     yshift = Ny - 2 * L - 1;
     zshift = Nz - 2 * L - 1;
-    // TF/SF box and NTF surface, source/meteor-2.1.cpp:539-552.
-    bx1 = L + 10; bx2 = Nx - L - 10;
-    by1 = L + 10; by2 = Ny - L - 10;
-    bz1 = L + 10; bz2 = Nz - L - 10;
-    ntfb = L + 5;
+    // TF/SF box and NTF surface, source/meteor-2.1.cpp:539-552 (gaps 10, 5).
+    bx1 = L + ext.tfsf_gap; bx2 = Nx - L - ext.tfsf_gap;
+    by1 = L + ext.tfsf_gap; by2 = Ny - L - ext.tfsf_gap;
+    bz1 = L + ext.tfsf_gap; bz2 = Nz - L - ext.tfsf_gap;
+    ntfb = L + ext.ntf_gap;
+
+    // Oblique incidence: a 1-D auxiliary Yee line along k whose cell size dl
+    // matches the 3-D grid's numerical wavenumber along k at f0 (matched
+    // numerical dispersion), so the injected wave and the grid's own wave
+    // travel at the same speed.  The incident field at a node of doubled
+    // coordinates P is the line's value at s = kr . (P/2) + s0 (linear
+    // interpolation).  The line ends in an L-cell CPML.
+    oblique = ext.oblique ? 1 : 0;
+    if (oblique) {
+        const double th = ext.inc_theta, ph = ext.inc_phi, ps = ext.inc_psi;
+        inc_k[0] = sin(th) * cos(ph); inc_k[1] = sin(th) * sin(ph); inc_k[2] = cos(th);
+        const double tht[3] = {cos(th) * cos(ph), cos(th) * sin(ph), -sin(th)};
+        const double phh[3] = {-sin(ph), cos(ph), 0.0};
+        for (int q = 0; q < 3; q++) inc_e[q] = cos(ps) * (-tht[q]) + sin(ps) * phh[q];
+        inc_h[0] = inc_k[1] * inc_e[2] - inc_k[2] * inc_e[1];
+        inc_h[1] = inc_k[2] * inc_e[0] - inc_k[0] * inc_e[2];
+        inc_h[2] = inc_k[0] * inc_e[1] - inc_k[1] * inc_e[0];
+        const double c = 1 / sqrt(kU0 * kE0);
+        const double d3[3] = {dx, dy, dz};
+        const double w = 2 * kPI * f0;
+        const double k3 = yee3_wavenumber(w, dt, c, d3, inc_k);
+        dl = matched_line_cell(k3, w, dt, c, std::min(dx, std::min(dy, dz)), std::max(dx, std::max(dy, dz)));
+        if (!(c * dt < dl))
+            throw Error(MFDTD_EINVAL, "oblique incidence: the auxiliary line would be unstable "
+                                      "(grid too coarse for f0)");
+        for (int q = 0; q < 3; q++) kr[q] = inc_k[q] * d3[q] / dl;
+        // Line node 0 sits at the grid corner the wave enters first, so a wave
+        // along +x sees the line at s = x index, as the reference's line does.
+        const int gx[2] = {0, Nx - 1}, gy[2] = {0, Ny - 1}, gz[2] = {0, Nz - 1};
+        const int cx[2] = {bx1 - 1, bx2}, cy[2] = {by1 - 1, by2}, cz[2] = {bz1 - 1, bz2};
+        double gmin = 1e300, pmax = -1e300;
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                for (int e = 0; e < 2; e++) {
+                    gmin = std::min(gmin, kr[0] * gx[a] + kr[1] * gy[b] + kr[2] * gz[e]);
+                    pmax = std::max(pmax, kr[0] * cx[a] + kr[1] * cy[b] + kr[2] * cz[e]);
+                }
+        s0 = -gmin;
+        M = (int)ceil(pmax + s0) + 6 + L;
+        ashift = M - 2 * L - 1;
+        // Every node that can carry a correction lies in the box [b1-1, b2]^3,
+        // so its s lies between the extremes over that box's corners; the
+        // interpolation reads line nodes floor(s - 1/2) .. floor(s) + 2.
+        double smin = 1e300, smax = -1e300;
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                for (int e = 0; e < 2; e++) {
+                    const double sc = kr[0] * cx[a] + kr[1] * cy[b] + kr[2] * cz[e] + s0;
+                    smin = std::min(smin, sc);
+                    smax = std::max(smax, sc);
+                }
+        if (!(smin >= 1.0) || !(smax + 3 <= M - L - 2))
+            throw Error(MFDTD_EINVAL, "oblique incidence: TF/SF box outside the auxiliary line");
+        Be1.assign(2 * L, 0.0); Ae1.assign(2 * L, 0.0); Bh1.assign(2 * L, 0.0); Ah1.assign(2 * L, 0.0);
+        cpml_tables(L, ext.pml_m, 1.0, 0.0, dl, dt, Be1.data(), Ae1.data(), Bh1.data(), Ah1.data(),
+                    nullptr, nullptr);
+    }
     // Plate, source/meteor-2.1.cpp:1308-1309.
     plate_lo = (int)(ssy - platesize / 2 / dy);
     plate_up = (int)(ssy + platesize / 2 / dy);

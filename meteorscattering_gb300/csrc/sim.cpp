@@ -153,6 +153,17 @@ struct mfdtd_sim {
         a.platesize = P.platesize; a.dt = P.dt;
         for (int m = 0; m < 2 * P.L; m++) {
             a.Be[m] = P.Be[m]; a.Ae[m] = P.Ae[m]; a.Bh[m] = P.Bh[m]; a.Ah[m] = P.Ah[m];
+            a.Ke[m] = P.Ke[m]; a.Kh[m] = P.Kh[m];
+        }
+        a.kappa_on = P.kappa_on;
+        a.oblique = P.oblique;
+        a.lk_colocated = P.ext.lk_colocated;
+        if (P.oblique) {
+            a.M = P.M; a.ashift = P.ashift; a.s0 = P.s0; a.dl = P.dl;
+            for (int q = 0; q < 3; q++) { a.ke[q] = P.inc_e[q]; a.kh[q] = P.inc_h[q]; a.kr[q] = P.kr[q]; }
+            for (int m = 0; m < 2 * P.L; m++) {
+                a.Be1[m] = P.Be1[m]; a.Ae1[m] = P.Ae1[m]; a.Bh1[m] = P.Bh1[m]; a.Ah1[m] = P.Ah1[m];
+            }
         }
         double **f[9] = {&a.Ex, &a.Ey, &a.Ez, &a.Hx, &a.Hy, &a.Hz, &a.Jx, &a.Jy, &a.Jz};
         for (auto p : f) *p = dalloc<double>(NC);
@@ -164,11 +175,16 @@ struct mfdtd_sim {
             a.Pexy = dalloc<double>(nys); a.Pexz = dalloc<double>(nzs); a.Peyx = dalloc<double>(nxs);
             a.Peyz = dalloc<double>(nzs); a.Pezx = dalloc<double>(nxs); a.Pezy = dalloc<double>(nys);
         }
-        a.Eyinc = dalloc<double>(P.Nx); a.Ezinc = dalloc<double>(P.Nx);
-        a.Hyinc = dalloc<double>(P.Nx); a.Hzinc = dalloc<double>(P.Nx);
+        // Incident line: the reference's x-directed line has Nx nodes; the
+        // oblique auxiliary line keeps its E in Ezinc and its H in Hyinc.
+        const size_t nline = std::max<size_t>(P.Nx, P.oblique ? (size_t)P.M : 0);
+        a.Eyinc = dalloc<double>(nline); a.Ezinc = dalloc<double>(nline);
+        a.Hyinc = dalloc<double>(nline); a.Hzinc = dalloc<double>(nline);
         a.PeyxI = dalloc<double>(L2); a.PezxI = dalloc<double>(L2);
         a.PhyxI = dalloc<double>(L2); a.PhzxI = dalloc<double>(L2);
         a.wp2 = upload(P.wp2e); a.nu2 = upload(P.nu2e); a.G = upload(P.G);
+        a.wp3 = P.wp3.empty() ? nullptr : upload(P.wp3);
+        a.nu3 = P.nu3.empty() ? nullptr : upload(P.nu3);
         a.xc = upload(P.x); a.yc = upload(P.y); a.zc = upload(P.z);
         a.lk = upload(P.lk); a.src = upload(P.src); a.phase = upload(P.phase);
         const size_t nf2 = 2 * (size_t)P.nntf();
@@ -515,6 +531,28 @@ int mfdtd_problem_create(const mfdtd_params *prm, const double *wp2, const doubl
 }
 
 void mfdtd_problem_destroy(mfdtd_problem *pb) { delete pb; }
+
+void mfdtd_ext_defaults(mfdtd_ext *ext) {
+    if (ext) mfdtd::ext_defaults(*ext);
+}
+
+int mfdtd_problem_set_ext(mfdtd_problem *pb, const mfdtd_ext *ext, const double *wp3,
+                          const double *nu3) {
+    return guarded([&] {
+        if (!pb) throw Error(MFDTD_EINVAL, "NULL problem");
+        Problem P = pb->P;  // validate on a copy: a rejected call leaves pb unchanged
+        if (ext) P.ext = *ext;
+        else mfdtd::ext_defaults(P.ext);
+        P.ext_present = 1;
+        const size_t n3 = P.cells();
+        if (wp3) P.wp3.assign(wp3, wp3 + n3);
+        else P.wp3.clear();
+        if (nu3) P.nu3.assign(nu3, nu3 + n3);
+        else P.nu3.clear();
+        P.derive();
+        pb->P = std::move(P);
+    });
+}
 
 int mfdtd_problem_dims(const mfdtd_problem *pb, int64_t out[6]) {
     return guarded([&] {

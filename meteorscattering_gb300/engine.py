@@ -33,7 +33,8 @@ EXPORTS = (
     "mfdtd_sim_step_index", "mfdtd_sim_ntf_size", "mfdtd_sim_read_ntf",
     "mfdtd_sim_read_probes", "mfdtd_sim_read_field", "mfdtd_sim_write_outputs",
     "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_sim_far_field",
-    "mfdtd_far_field_static", "mfdtd_last_error", "mfdtd_version",
+    "mfdtd_far_field_static", "mfdtd_last_error", "mfdtd_version", "mfdtd_ext_defaults",
+    "mfdtd_problem_set_ext",
 )
 
 
@@ -60,6 +61,16 @@ class Params(C.Structure):
         ("probex", C.POINTER(C.c_int32)), ("probey", C.POINTER(C.c_int32)),
         ("probez", C.POINTER(C.c_int32)), ("nntf", C.c_int32), ("fntf", C.POINTER(C.c_double)),
         ("doplate", C.c_int32), ("platesize", C.c_double), ("doB0", C.c_int32),
+    ]
+
+
+class Ext(C.Structure):
+    """``mfdtd_ext`` -- extended inputs (reference values from mfdtd_ext_defaults)."""
+    _fields_ = [
+        ("pmllen", C.c_int32), ("tfsf_gap", C.c_int32), ("ntf_gap", C.c_int32),
+        ("oblique", C.c_int32), ("exact_coords", C.c_int32), ("lk_colocated", C.c_int32),
+        ("pml_m", C.c_double), ("kappa_max", C.c_double), ("alpha_max", C.c_double),
+        ("inc_theta", C.c_double), ("inc_phi", C.c_double), ("inc_psi", C.c_double),
     ]
 
 
@@ -100,6 +111,8 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_far_field_static": (C.c_int, [C.POINTER(C.c_void_p), i32, i32, i32, i32, i32, dp,
                                              C.c_double, C.c_double, C.c_double, dp, i32, dp, dp,
                                              dp, vp]),
+        "mfdtd_ext_defaults": (None, [C.POINTER(Ext)]),
+        "mfdtd_problem_set_ext": (C.c_int, [vp, C.POINTER(Ext), dp, dp]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -176,6 +189,31 @@ class Problem:
         h = C.c_void_p()
         _check(lib.mfdtd_problem_create(C.byref(prm), _dp(w), _dp(n), _dp(b), C.byref(h)))
         return cls(h)
+
+    def set_ext(self, ext=None, wp3: Optional[np.ndarray] = None,
+                nu3: Optional[np.ndarray] = None) -> "Problem":
+        """Apply extended inputs (a :class:`rundir.ExtParams`, or None for the
+        reference values) and optional per-cell ``[Nx][Ny][Nz]`` maps."""
+        lib = load_library()
+        e = Ext()
+        lib.mfdtd_ext_defaults(C.byref(e))
+        if ext is not None:
+            for f, _ in Ext._fields_:
+                setattr(e, f, getattr(ext, f))
+        Nx, Ny, Nz = self.dims()[:3]
+        keep = []
+
+        def arr(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != (Nx, Ny, Nz):
+                raise ValueError(f"per-cell maps must be (Nx, Ny, Nz) = ({Nx}, {Ny}, {Nz})")
+            keep.append(a)
+            return _dp(a)
+
+        _check(lib.mfdtd_problem_set_ext(self._h, C.byref(e), arr(wp3), arr(nu3)))
+        return self
 
     def dims(self):
         out = (C.c_int64 * 6)()

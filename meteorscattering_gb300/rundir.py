@@ -199,10 +199,113 @@ def write_rundir(path: str, p: RunParams, wp: np.ndarray, nu: np.ndarray,
     with open(os.path.join(path, "nu.dat"), "wb") as f:
         f.write(nu.tobytes(order="F"))
     for name in ("output_E.dat", "output_H.dat", "output_J.dat", "Probe.dat",
-                 "output_NTF.dat", "log.txt"):
+                 "output_NTF.dat", "log.txt", "ext.dat", "wp3.dat", "nu3.dat"):
         fp = os.path.join(path, name)
         if os.path.exists(fp):
             os.remove(fp)
+
+
+# --------------------------------------------------------------------------
+# Extended inputs (no counterpart in the reference, which hard-codes them)
+
+EXT_MAGIC = b"MFDTDX01"
+
+
+@dataclasses.dataclass
+class ExtParams:
+    """``mfdtd_ext`` of ``include/mfdtd.h``.  The defaults are the values the
+    reference hard-codes (``source/meteor-2.1.cpp:343, 413-415, 539-552``) and
+    its +x plane wave."""
+
+    pmllen: int = 10
+    tfsf_gap: int = 10
+    ntf_gap: int = 5
+    oblique: int = 0
+    exact_coords: int = 0
+    lk_colocated: int = 0
+    pml_m: float = 4.0
+    kappa_max: float = 1.0
+    alpha_max: float = 0.0
+    inc_theta: float = math.pi / 2
+    inc_phi: float = 0.0
+    inc_psi: float = 0.0
+
+    def k_hat(self) -> np.ndarray:
+        th, ph = self.inc_theta, self.inc_phi
+        return np.array([math.sin(th) * math.cos(ph), math.sin(th) * math.sin(ph), math.cos(th)])
+
+
+def pack_ext(e: ExtParams, has_wp3: bool, has_nu3: bool) -> bytes:
+    """``ext.dat``: 8-byte magic, 8 int32 (pmllen, tfsf_gap, ntf_gap, oblique,
+    exact_coords, has_wp3, has_nu3, lk_colocated), 6 float64 (pml_m, kappa_max, alpha_max,
+    inc_theta, inc_phi, inc_psi); 88 bytes."""
+    return (EXT_MAGIC
+            + struct.pack("<8i", e.pmllen, e.tfsf_gap, e.ntf_gap, e.oblique, e.exact_coords,
+                          1 if has_wp3 else 0, 1 if has_nu3 else 0, e.lk_colocated)
+            + struct.pack("<6d", e.pml_m, e.kappa_max, e.alpha_max, e.inc_theta, e.inc_phi,
+                          e.inc_psi))
+
+
+def unpack_ext(buf: bytes):
+    if buf[:8] != EXT_MAGIC or len(buf) < 88:
+        raise ValueError("not an ext.dat record")
+    iv = struct.unpack_from("<8i", buf, 8)
+    dv = struct.unpack_from("<6d", buf, 40)
+    e = ExtParams(pmllen=iv[0], tfsf_gap=iv[1], ntf_gap=iv[2], oblique=iv[3],
+                  exact_coords=iv[4], lk_colocated=iv[7], pml_m=dv[0], kappa_max=dv[1], alpha_max=dv[2],
+                  inc_theta=dv[3], inc_phi=dv[4], inc_psi=dv[5])
+    return e, bool(iv[5]), bool(iv[6])
+
+
+def write_ext(path: str, e: ExtParams, wp3: Optional[np.ndarray] = None,
+              nu3: Optional[np.ndarray] = None) -> None:
+    """Write ``ext.dat`` and, when given, the per-cell maps ``wp3.dat`` /
+    ``nu3.dat`` (``[Nx][Ny][Nz]`` float64, C order: these files are this
+    engine's own, so no MATLAB transposition applies)."""
+    with open(os.path.join(path, "ext.dat"), "wb") as f:
+        f.write(pack_ext(e, wp3 is not None, nu3 is not None))
+    for name, arr in (("wp3.dat", wp3), ("nu3.dat", nu3)):
+        fp = os.path.join(path, name)
+        if arr is not None:
+            np.ascontiguousarray(arr, dtype="<f8").tofile(fp)
+        elif os.path.exists(fp):
+            os.remove(fp)
+
+
+def tilted_trail_wp3(Nx: int, Ny: int, Nz: int, dx: float, tilt_deg: float, r0: float,
+                     log10n_lo: float, log10n_hi: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Per-cell plasma frequency of a straight trail whose axis is tilted by
+    ``tilt_deg`` from +z toward +x (staircased on the grid).  Density
+    n = n0(s) exp(-r^2 / r0^2), r the distance to the axis, s the position
+    along it; log10 n0 varies linearly from ``log10n_lo`` at the bottom of the
+    grid to ``log10n_hi`` at the top.  Cell-centred exact coordinates."""
+    x = grid_coords(Nx, dx)[:, None, None] - centre[0]
+    y = grid_coords(Ny, dx)[None, :, None] - centre[1]
+    z = grid_coords(Nz, dx)[None, None, :] - centre[2]
+    t = math.radians(tilt_deg)
+    ax = (math.sin(t), 0.0, math.cos(t))
+    out = np.empty((Nx, Ny, Nz))
+    half = 0.5 * (Nz - 1) * dx
+    for i in range(Nx):  # plane by plane keeps the temporaries small
+        xi = x[i]
+        s_ax = xi * ax[0] + z * ax[2]                       # [1, Nz]
+        r2 = xi * xi + y * y + z * z - s_ax * s_ax          # [Ny, Nz]
+        frac = np.clip((s_ax + half) / (2 * half), 0.0, 1.0)
+        n0 = 10.0 ** (log10n_lo + (log10n_hi - log10n_lo) * frac)
+        out[i] = plasma_frequency(n0 * np.exp(-np.maximum(r2, 0.0) / (r0 * r0)))[0]
+    return out
+
+
+def plasma_sphere_wp3(Nx: int, Ny: int, Nz: int, dx: float, radius: float,
+                      n_e: float) -> np.ndarray:
+    """Per-cell plasma frequency of a homogeneous sphere of ``radius`` (m)
+    and density ``n_e`` (m^-3) at the grid centre (cell-centred exact
+    coordinates, staircased)."""
+    x = grid_coords(Nx, dx)[:, None, None]
+    y = grid_coords(Ny, dx)[None, :, None]
+    z = grid_coords(Nz, dx)[None, None, :]
+    inside = (x * x + y * y + z * z) < radius * radius
+    return np.where(inside, plasma_frequency(n_e), 0.0)
 
 
 # --------------------------------------------------------------------------

@@ -50,11 +50,16 @@
 #define OR_ME 9.10939e-31
 #define OR_C 3.0000e8
 
-/* Hard-coded solver settings, R21:119, R21:342-343, R21:413-415, R21:539-552. */
-#define OR_PMLLEN 10
-#define OR_PMLM 4.0
-#define OR_TFSF_GAP 10
-#define OR_NTF_GAP 5
+/* Settings the reference hard-codes (R21:342-343 pmllen 10, R21:413-415 m = 4,
+ * kappa = 1, alpha = 0, R21:539-552 TF/SF gap 10 and NTF gap 5).  The optional
+ * ext.dat of a run directory (no counterpart in the reference) overrides
+ * them; without it every value is the reference's. */
+#define OR_MAXPML 32
+
+typedef struct {
+    int present, pmllen, tfsf_gap, ntf_gap, oblique, exact_coords, has_wp3, has_nu3, lk_colocated;
+    double pml_m, kappa_max, alpha_max, inc_theta, inc_phi, inc_psi;
+} or_ext;
 
 typedef struct {
     int dopml, savefields, sourcetype, sourcepol, tsteps, Nx, Ny, Nz;
@@ -65,6 +70,8 @@ typedef struct {
     double *fntf;
     double Bx, By, Bz;
     double *wp2, *nu2; /* [Nx][Ny], C order as read */
+    or_ext ext;
+    double *wp3, *nu3; /* [Nx][Ny][Nz] per-cell maps (extended inputs) or NULL */
 } or_in;
 
 static double now_s(void) {
@@ -127,8 +134,36 @@ static int read_inputs(const char *dir, or_in *p) {
     if (fread(&p->doB0, 4, 1, f) != 1) p->doB0 = 0; /* MATLAB-written file */
     fclose(f);
 
-    if (p->Nx < 2 * OR_PMLLEN + 2 || p->Ny < 2 * OR_PMLLEN + 2 || p->Nz < 2 * OR_PMLLEN + 2)
-        return -3;
+    /* ext.dat: magic, 8 int32, 6 doubles (88 bytes). */
+    p->ext.pmllen = 10; p->ext.tfsf_gap = 10; p->ext.ntf_gap = 5;
+    p->ext.pml_m = 4.0; p->ext.kappa_max = 1.0; p->ext.alpha_max = 0.0;
+    p->ext.inc_theta = OR_PI / 2;
+    f = open_in(dir, "ext.dat", "rb");
+    if (f) {
+        char magic[8];
+        int32_t iv[8];
+        double dv[6];
+        if (rd(magic, 1, 8, f) || memcmp(magic, "MFDTDX01", 8) || rd(iv, 4, 8, f) || rd(dv, 8, 6, f)) {
+            fclose(f);
+            return -2;
+        }
+        fclose(f);
+        or_ext *x = &p->ext;
+        x->present = 1;
+        x->pmllen = iv[0]; x->tfsf_gap = iv[1]; x->ntf_gap = iv[2]; x->oblique = iv[3];
+        x->exact_coords = iv[4]; x->has_wp3 = iv[5]; x->has_nu3 = iv[6]; x->lk_colocated = iv[7];
+        x->pml_m = dv[0]; x->kappa_max = dv[1]; x->alpha_max = dv[2];
+        x->inc_theta = dv[3]; x->inc_phi = dv[4]; x->inc_psi = dv[5];
+        if (x->pmllen < 1 || x->pmllen > OR_MAXPML || x->tfsf_gap < 2 || x->ntf_gap < 1 ||
+            x->ntf_gap > x->tfsf_gap - 2)
+            return -3;
+        int need = 2 * (x->pmllen + x->tfsf_gap) + 3;
+        if (p->Nx < need || p->Ny < need || p->Nz < need) return -3;
+    }
+    {
+        const int L = p->ext.pmllen;
+        if (p->Nx < 2 * L + 2 || p->Ny < 2 * L + 2 || p->Nz < 2 * L + 2) return -3;
+    }
     if (p->tsteps < 1 || p->numfiles < 1 || p->tsteps / p->numfiles < 1) return -3;
     for (int n = 0; n < p->nprobes; n++) {
         if (p->probex[n] < 1 || p->probex[n] >= p->Nx || p->probey[n] < 1 ||
@@ -157,12 +192,28 @@ static int read_inputs(const char *dir, or_in *p) {
     if (!f) return -1;
     e |= rd(p->nu2, 8, n2, f);
     fclose(f);
+    /* per-cell maps announced by ext.dat */
+    size_t n3 = n2 * (size_t)p->Nz;
+    if (p->ext.has_wp3) {
+        p->wp3 = malloc(n3 * sizeof(double));
+        f = open_in(dir, "wp3.dat", "rb");
+        if (!f) return -1;
+        e |= rd(p->wp3, 8, n3, f);
+        fclose(f);
+    }
+    if (p->ext.has_nu3) {
+        p->nu3 = malloc(n3 * sizeof(double));
+        f = open_in(dir, "nu3.dat", "rb");
+        if (!f) return -1;
+        e |= rd(p->nu3, 8, n3, f);
+        fclose(f);
+    }
     return e ? -2 : 0;
 }
 
 static void free_inputs(or_in *p) {
     free(p->probex); free(p->probey); free(p->probez);
-    free(p->fntf); free(p->wp2); free(p->nu2);
+    free(p->fntf); free(p->wp2); free(p->nu2); free(p->wp3); free(p->nu3);
 }
 
 static double *dalloc(size_t n) {
@@ -171,20 +222,21 @@ static double *dalloc(size_t n) {
     return a;
 }
 
-/* PML coefficient tables, R21:411-526.  Index m in [L, 2L) is the high side,
- * the low side mirrors it. */
+/* PML coefficient tables, R21:411-526, with the grading order, kappa_max and
+ * alpha_max as parameters (reference: 4, 1, 0).  Index m in [L, 2L) is the
+ * high side, the low side mirrors it.  Ke/Kh hold 1/kappa - 1 for the
+ * derivative term a kappa != 1 adds to the field update. */
 typedef struct {
-    double Be[2 * OR_PMLLEN], Ae[2 * OR_PMLLEN]; /* half-cell grading: E psi  */
-    double Bh[2 * OR_PMLLEN], Ah[2 * OR_PMLLEN]; /* full-cell grading: H psi  */
+    double Be[2 * OR_MAXPML], Ae[2 * OR_MAXPML]; /* half-cell grading: E psi  */
+    double Bh[2 * OR_MAXPML], Ah[2 * OR_MAXPML]; /* full-cell grading: H psi  */
+    double Ke[2 * OR_MAXPML], Kh[2 * OR_MAXPML];
 } or_pml;
 
-static void pml_tables(double dx, double dt, or_pml *t) {
-    const int L = OR_PMLLEN;
-    const double pmlm = OR_PMLM;
+static void pml_tables(int L, double pmlm, double kamax, double almax, double dx, double dt,
+                       or_pml *t) {
     double simax = 1.5 * (double)(pmlm + 1) / (150 * OR_PI * dx);
-    double kamax = 1, almax = 0;
-    double s[OR_PMLLEN], sm[OR_PMLLEN], ka[OR_PMLLEN], kam[OR_PMLLEN];
-    double al[OR_PMLLEN], alm[OR_PMLLEN];
+    double s[OR_MAXPML], sm[OR_MAXPML], ka[OR_MAXPML], kam[OR_MAXPML];
+    double al[OR_MAXPML], alm[OR_MAXPML];
     for (int m = 0; m < L; m++) {
         double mf = (double)m;
         s[m] = simax * pow(((mf + 0.5) / L), pmlm);
@@ -202,13 +254,114 @@ static void pml_tables(double dx, double dt, or_pml *t) {
         t->Ae[m] = s[n] / (s[n] * ka[n] + pow(ka[n], 2) * al[n]) * (t->Be[m] - 1);
         t->Bh[m] = exp(-((sm[n] / kam[n]) + alm[n]) * dt / OR_E0);
         t->Ah[m] = sm[n] / (sm[n] * kam[n] + pow(kam[n], 2) * alm[n]) * (t->Bh[m] - 1);
+        t->Ke[m] = 1 / ka[n] - 1;
+        t->Kh[m] = 1 / kam[n] - 1;
     }
     for (int m = 0; m < L; m++) {
         t->Be[m] = t->Be[2 * L - 1 - m];
         t->Ae[m] = t->Ae[2 * L - 1 - m];
         t->Bh[m] = t->Bh[2 * L - 1 - m];
         t->Ah[m] = t->Ah[2 * L - 1 - m];
+        t->Ke[m] = t->Ke[2 * L - 1 - m];
+        t->Kh[m] = t->Kh[2 * L - 1 - m];
     }
+}
+
+/* ---- oblique plane-wave incidence (extended inputs; the reference has only
+ * the +x line of R21:1278-1304) ----
+ * A 1-D auxiliary Yee line along k carries the incident wave.  Its cell size
+ * matches the 3-D grid's numerical wavenumber along k at f0 (matched
+ * numerical dispersion, Taflove & Hagness ch. 5): both dispersion relations
+ * are solved by bisection.  A node with doubled coordinates P sees the line
+ * at s = kr . P/2 + s0 (line cells; linear interpolation), E nodes at integer
+ * s, H nodes at s + 1/2.  TF/SF corrections are generic: every curl term whose
+ * neighbour lies on the other side of the box surface gets the neighbour's
+ * incident value, added on the total-field side and subtracted on the
+ * scattered-field side. */
+typedef struct {
+    double ke[3], kh[3], kr[3], s0, dl, d[3];
+    int b1[3], b2[3], M, ashift;
+} or_obl;
+
+static double yee3_wavenumber(double w, double dt, double c, const double d[3], const double u[3]) {
+    const double S = sin(w * dt / 2) / (c * dt);
+    const double S2 = S * S;
+    double lo = 0.5 * w / c, hi = 4 * w / c;
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        double f = 0;
+        for (int q = 0; q < 3; q++) {
+            const double v = sin(mid * u[q] * d[q] / 2) / d[q];
+            f = f + v * v;
+        }
+        if (f < S2) lo = mid;
+        else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+static double matched_line_cell(double k, double w, double dt, double c, double dmin, double dmax) {
+    const double S = sin(w * dt / 2) / (c * dt);
+    double lo = 0.25 * dmin, hi = 2 * dmax;
+    for (int it = 0; it < 200; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (sin(k * mid / 2) / mid > S) lo = mid;
+        else hi = mid;
+    }
+    return 0.5 * (lo + hi);
+}
+
+static int obl_in(const or_obl *o, const int P[3]) {
+    for (int q = 0; q < 3; q++)
+        if (P[q] < 2 * o->b1[q] || P[q] > 2 * (o->b2[q] - 1)) return 0;
+    return 1;
+}
+
+static double obl_line(const double *line, double s) {
+    double fl = floor(s);
+    int n = (int)fl;
+    double w = s - fl;
+    return line[n] + w * (line[n + 1] - line[n]);
+}
+
+/* Incident value of component q at doubled coordinates P: an E component when
+ * the neighbour field is E (line = E line), else an H component. */
+static double obl_inc(const or_obl *o, int nbr_is_e, int q, const int P[3], const double *line) {
+    double s = ((o->kr[0] * (0.5 * P[0]) + o->kr[1] * (0.5 * P[1])) + o->kr[2] * (0.5 * P[2])) + o->s0;
+    if (nbr_is_e) return o->ke[q] * obl_line(line, s);
+    return o->kh[q] * obl_line(line, s - 0.5);
+}
+
+/* TF/SF correction of component c of the target field (E when is_e) at cell
+ * (i,j,k).  Returns 1 and sets *corr when some curl-term neighbour lies on
+ * the other side of the box surface; the caller then adds c2 * corr.  `line`
+ * is the auxiliary line of the neighbour field (H line for E targets). */
+static int obl_corr(const or_obl *o, int is_e, int c, int i, int j, int k, const double *line,
+                    double *corr) {
+    int P[3] = {2 * i, 2 * j, 2 * k};
+    /* a target of either field is offset by half a cell along the axes other
+     * than its own component for H, along its own component for E */
+    for (int q = 0; q < 3; q++)
+        if (is_e ? q == c : q != c) P[q] += 1;
+    const int T = obl_in(o, P);
+    const int ax[2] = {(c + 1) % 3, (c + 2) % 3};
+    const int comp[2] = {(c + 2) % 3, (c + 1) % 3};
+    const int sg[2] = {is_e ? 1 : -1, is_e ? -1 : 1};
+    double acc = 0;
+    int any = 0;
+    for (int term = 0; term < 2; term++)
+        for (int side = 1; side >= -1; side -= 2) {
+            int Q[3] = {P[0], P[1], P[2]};
+            Q[ax[term]] += side;
+            const int Tn = obl_in(o, Q);
+            if (Tn == T) continue;
+            const double v = obl_inc(o, !is_e, comp[term], Q, line) / o->d[ax[term]];
+            if (sg[term] * side * (T - Tn) > 0) acc = acc + v;
+            else acc = acc - v;
+            any = 1;
+        }
+    *corr = acc;
+    return any;
 }
 
 static void write_all(FILE *f, const double *a, size_t n) {
@@ -228,7 +381,9 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
     if (rc) { free_inputs(&in); return rc; }
 
     const int Nx = in.Nx, Ny = in.Ny, Nz = in.Nz, tsteps = in.tsteps, nntf = in.nntf;
-    const int L = OR_PMLLEN;
+    const int L = in.ext.pmllen;
+    const int obl = in.ext.oblique != 0;
+    const int kappa_on = in.dopml && in.ext.kappa_max != 1.0;
     const double dt = in.dt;
     const size_t NC = (size_t)Nx * Ny * Nz;
 #define I3(i, j, k) ((((size_t)(i)) * Ny + (size_t)(j)) * Nz + (size_t)(k))
@@ -240,10 +395,16 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
     int nmax = Nx > Ny ? Nx : Ny;
     if (Nz > nmax) nmax = Nz;
     double *x = dalloc((size_t)nmax), *y = dalloc((size_t)nmax), *z = dalloc((size_t)nmax);
-    for (int i = 0; i < Nx; i++) {
-        x[i] = -(Nx - 1) / 2 * dx + dx * i;
-        if (i < nmax) y[i] = -(Ny - 1) / 2 * dy + dy * i;
-        if (i < nmax) z[i] = -(Nz - 1) / 2 * dz + dz * i;
+    if (in.ext.exact_coords) { /* extended input: every axis, real division */
+        for (int i = 0; i < Nx; i++) x[i] = -(Nx - 1) / 2.0 * dx + dx * i;
+        for (int i = 0; i < Ny; i++) y[i] = -(Ny - 1) / 2.0 * dy + dy * i;
+        for (int i = 0; i < Nz; i++) z[i] = -(Nz - 1) / 2.0 * dz + dz * i;
+    } else {
+        for (int i = 0; i < Nx; i++) {
+            x[i] = -(Nx - 1) / 2 * dx + dx * i;
+            if (i < nmax) y[i] = -(Ny - 1) / 2 * dy + dy * i;
+            if (i < nmax) z[i] = -(Nz - 1) / 2 * dz + dz * i;
+        }
     }
     const int ssx = (Nx + 1) / 2, ssy = (Ny + 1) / 2, ssz = (Nz + 1) / 2;
 
@@ -324,6 +485,8 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                         size_t c = I3(i, j, k);
                         wpe[c] = in.wp2[(size_t)i * Ny + j] * exp(-pow((z[k] - in.metloc[2]), 2) / (msig0 * msig0));
                         nue[c] = in.nu2[(size_t)i * Ny + j] * exp(-pow((z[k] - in.metloc[2]), 2) / (msig0 * msig0));
+                        if (in.wp3) wpe[c] = in.wp3[c]; /* per-cell maps (extended inputs) */
+                        if (in.nu3) nue[c] = in.nu3[c];
                     }
         }
     }
@@ -331,7 +494,8 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
     /* CPML, R21:342-535. */
     or_pml T;
     memset(&T, 0, sizeof T);
-    if (in.dopml) pml_tables(dx, dt, &T);
+    if (in.dopml)
+        pml_tables(L, in.ext.pml_m, in.ext.kappa_max, in.ext.alpha_max, dx, dt, &T);
     const int xshift = Nx - 2 * L - 1, yshift = Ny - 2 * L - 1, zshift = Nz - 2 * L - 1;
     /* psi slabs: x-normal [2L][Ny][Nz], y-normal [Nx][2L][Nz], z-normal [Nx][Ny][2L] */
     const size_t nxs = (size_t)2 * L * Ny * Nz, nys = (size_t)Nx * 2 * L * Nz, nzs = (size_t)Nx * Ny * 2 * L;
@@ -339,18 +503,89 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
     double *P_hyz = dalloc(nzs), *P_hzx = dalloc(nxs), *P_hzy = dalloc(nys);
     double *P_exy = dalloc(nys), *P_exz = dalloc(nzs), *P_eyx = dalloc(nxs);
     double *P_eyz = dalloc(nzs), *P_ezx = dalloc(nxs), *P_ezy = dalloc(nys);
-    double P_eyxI[2 * OR_PMLLEN] = {0}, P_ezxI[2 * OR_PMLLEN] = {0};
-    double P_hyxI[2 * OR_PMLLEN] = {0}, P_hzxI[2 * OR_PMLLEN] = {0};
+    double P_eyxI[2 * OR_MAXPML] = {0}, P_ezxI[2 * OR_MAXPML] = {0};
+    double P_hyxI[2 * OR_MAXPML] = {0}, P_hzxI[2 * OR_MAXPML] = {0};
 #define PX(i, j, k) ((((size_t)(i)) * Ny + (size_t)(j)) * Nz + (size_t)(k))        /* [2L][Ny][Nz] */
 #define PY(i, j, k) ((((size_t)(i)) * (2 * L) + (size_t)(j)) * Nz + (size_t)(k))   /* [Nx][2L][Nz] */
 #define PZ(i, j, k) ((((size_t)(i)) * Ny + (size_t)(j)) * (2 * L) + (size_t)(k))   /* [Nx][Ny][2L] */
-    const double *Bh = T.Bh, *Ah = T.Ah, *Be = T.Be, *Ae = T.Ae;
+    const double *Bh = T.Bh, *Ah = T.Ah, *Be = T.Be, *Ae = T.Ae, *Ke = T.Ke, *Kh = T.Kh;
+    /* A CPML correction with kappa != 1 also carries (1/kappa - 1) times the
+     * derivative the psi recursion uses (extended inputs). */
+#define KAP(p, K, s, diff, d) (kappa_on ? (p) + (K)[s] * (diff) / (d) : (p))
 
     /* TF/SF box and NTF surface, R21:539-552. */
-    const int bx1 = L + OR_TFSF_GAP, bx2 = Nx - L - OR_TFSF_GAP;
-    const int by1 = L + OR_TFSF_GAP, by2 = Ny - L - OR_TFSF_GAP;
-    const int bz1 = L + OR_TFSF_GAP, bz2 = Nz - L - OR_TFSF_GAP;
-    int ntfb = L + OR_NTF_GAP;
+    const int gap = in.ext.tfsf_gap;
+    const int bx1 = L + gap, bx2 = Nx - L - gap;
+    const int by1 = L + gap, by2 = Ny - L - gap;
+    const int bz1 = L + gap, bz2 = Nz - L - gap;
+    int ntfb = L + in.ext.ntf_gap;
+
+    /* Oblique incidence set-up (extended inputs).  E1d lives in Ezinc and H1d
+     * in Hyinc, which then hold M nodes; Eyinc and Hzinc stay zero. */
+    or_obl O;
+    memset(&O, 0, sizeof O);
+    or_pml T1;
+    memset(&T1, 0, sizeof T1);
+    double P_e1[2 * OR_MAXPML] = {0}, P_h1[2 * OR_MAXPML] = {0};
+    if (obl) {
+        const double th = in.ext.inc_theta, ph = in.ext.inc_phi, ps = in.ext.inc_psi;
+        double kk[3] = {sin(th) * cos(ph), sin(th) * sin(ph), cos(th)};
+        const double tht[3] = {cos(th) * cos(ph), cos(th) * sin(ph), -sin(th)};
+        const double phh[3] = {-sin(ph), cos(ph), 0.0};
+        for (int q = 0; q < 3; q++) O.ke[q] = cos(ps) * (-tht[q]) + sin(ps) * phh[q];
+        O.kh[0] = kk[1] * O.ke[2] - kk[2] * O.ke[1];
+        O.kh[1] = kk[2] * O.ke[0] - kk[0] * O.ke[2];
+        O.kh[2] = kk[0] * O.ke[1] - kk[1] * O.ke[0];
+        const double cl = 1 / sqrt(OR_U0 * OR_E0);
+        O.d[0] = dx; O.d[1] = dy; O.d[2] = dz;
+        const double w = 2 * OR_PI * in.f0;
+        const double k3 = yee3_wavenumber(w, dt, cl, O.d, kk);
+        double dmin = dx < dy ? dx : dy, dmax = dx > dy ? dx : dy;
+        if (dz < dmin) dmin = dz;
+        if (dz > dmax) dmax = dz;
+        O.dl = matched_line_cell(k3, w, dt, cl, dmin, dmax);
+        if (!(cl * dt < O.dl)) { free_inputs(&in); return -3; }
+        for (int q = 0; q < 3; q++) O.kr[q] = kk[q] * O.d[q] / O.dl;
+        /* line node 0 at the grid corner the wave enters first: a wave along +x
+         * sees the line at s = x index, like the reference's line */
+        const int gx[2] = {0, Nx - 1}, gy[2] = {0, Ny - 1}, gz[2] = {0, Nz - 1};
+        const int cx[2] = {bx1 - 1, bx2}, cy[2] = {by1 - 1, by2}, cz[2] = {bz1 - 1, bz2};
+        double gmin = 1e300, pmax = -1e300;
+        for (int a = 0; a < 2; a++)
+            for (int b = 0; b < 2; b++)
+                for (int e = 0; e < 2; e++) {
+                    const double g = O.kr[0] * gx[a] + O.kr[1] * gy[b] + O.kr[2] * gz[e];
+                    const double pp = O.kr[0] * cx[a] + O.kr[1] * cy[b] + O.kr[2] * cz[e];
+                    if (g < gmin) gmin = g;
+                    if (pp > pmax) pmax = pp;
+                }
+        O.s0 = -gmin;
+        O.M = (int)ceil(pmax + O.s0) + 6 + L;
+        O.ashift = O.M - 2 * L - 1;
+        {   /* the shell's line positions must sit inside the line */
+            double smin = 1e300, smax = -1e300;
+            for (int a = 0; a < 2; a++)
+                for (int b = 0; b < 2; b++)
+                    for (int e = 0; e < 2; e++) {
+                        const double sc = O.kr[0] * cx[a] + O.kr[1] * cy[b] + O.kr[2] * cz[e] + O.s0;
+                        if (sc < smin) smin = sc;
+                        if (sc > smax) smax = sc;
+                    }
+            if (!(smin >= 1.0) || !(smax + 3 <= O.M - L - 2)) { free_inputs(&in); return -3; }
+        }
+        O.b1[0] = bx1; O.b1[1] = by1; O.b1[2] = bz1;
+        O.b2[0] = bx2; O.b2[1] = by2; O.b2[2] = bz2;
+        pml_tables(L, in.ext.pml_m, 1.0, 0.0, O.dl, dt, &T1);
+        if (O.M > Nx) { /* the line outgrows the reference's Nx-node arrays */
+            free(Ezinc); free(Hyinc);
+            Ezinc = dalloc((size_t)O.M); Hyinc = dalloc((size_t)O.M);
+        }
+    }
+    /* the shell of cells that can carry a TF/SF correction */
+#define SHELL(i, j, k) ((i) >= bx1 - 1 && (i) <= bx2 && (j) >= by1 - 1 && (j) <= by2 && \
+                        (k) >= bz1 - 1 && (k) <= bz2 &&                                \
+                        !((i) > bx1 && (i) < bx2 - 2 && (j) > by1 && (j) < by2 - 2 &&    \
+                          (k) > bz1 && (k) < bz2 - 2))
 
     /* NTF running sums, R21:558-610. */
     double *Ezdft = dalloc(2 * (size_t)nntf), *Eydft = dalloc(2 * (size_t)nntf);
@@ -417,7 +652,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                 for (int j = 0; j < Ny; j++)
                     for (int k = 0; k < Nz - 1; k++)
                         P_hyx[PX(i - xshift, j, k)] = Bh[i - xshift] * P_hyx[PX(i - xshift, j, k)] + Ah[i - xshift] * (Ez[I3(i + 1, j, k)] - Ez[I3(i, j, k)]) / dx;
-                P_hyxI[i - xshift] = Bh[i - xshift] * P_hyxI[i - xshift] + Ah[i - xshift] * (Ezinc[i + 1] - Ezinc[i]) / dx;
+                if (!obl) P_hyxI[i - xshift] = Bh[i - xshift] * P_hyxI[i - xshift] + Ah[i - xshift] * (Ezinc[i + 1] - Ezinc[i]) / dx;
             }
             for (int i = 0; i < Nx - 1; i++)
                 for (int j = 0; j < Ny; j++) {
@@ -434,7 +669,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                 for (int j = 0; j < Ny - 1; j++)
                     for (int k = 0; k < Nz; k++)
                         P_hzx[PX(i - xshift, j, k)] = Bh[i - xshift] * P_hzx[PX(i - xshift, j, k)] + Ah[i - xshift] * (Ey[I3(i + 1, j, k)] - Ey[I3(i, j, k)]) / dx;
-                P_hzxI[i - xshift] = Bh[i - xshift] * P_hzxI[i - xshift] + Ah[i - xshift] * (Eyinc[i + 1] - Eyinc[i]) / dx;
+                if (!obl) P_hzxI[i - xshift] = Bh[i - xshift] * P_hzxI[i - xshift] + Ah[i - xshift] * (Eyinc[i + 1] - Eyinc[i]) / dx;
             }
             for (int i = 0; i < Nx - 1; i++) {
                 for (int j = 0; j < L; j++)
@@ -452,31 +687,41 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
             for (int j = 0; j < Ny - 1; j++)
                 for (int k = 0; k < Nz - 1; k++)
                     Hx[I3(i, j, k)] = c1h * Hx[I3(i, j, k)] - c2h * ((Ez[I3(i, j + 1, k)] - Ez[I3(i, j, k)]) / dy - (Ey[I3(i, j, k + 1)] - Ey[I3(i, j, k)]) / dz);
-        for (int i = bx1; i < bx2; i++)
-            for (int k = bz1; k < bz2; k++) {
-                Hx[I3(i, by1 - 1, k)] = Hx[I3(i, by1 - 1, k)] + c2h * Ezinc[i] / dy;
-                Hx[I3(i, by2 - 1, k)] = Hx[I3(i, by2 - 1, k)] - c2h * Ezinc[i] / dy;
-            }
-        for (int i = bx1; i < bx2; i++)
-            for (int j = by1; j < by2; j++) {
-                Hx[I3(i, j, bz1 - 1)] = Hx[I3(i, j, bz1 - 1)] - c2h * Eyinc[i] / dz;
-                Hx[I3(i, j, bz2 - 1)] = Hx[I3(i, j, bz2 - 1)] + c2h * Eyinc[i] / dz;
-            }
+        if (!obl) {
+            for (int i = bx1; i < bx2; i++)
+                for (int k = bz1; k < bz2; k++) {
+                    Hx[I3(i, by1 - 1, k)] = Hx[I3(i, by1 - 1, k)] + c2h * Ezinc[i] / dy;
+                    Hx[I3(i, by2 - 1, k)] = Hx[I3(i, by2 - 1, k)] - c2h * Ezinc[i] / dy;
+                }
+            for (int i = bx1; i < bx2; i++)
+                for (int j = by1; j < by2; j++) {
+                    Hx[I3(i, j, bz1 - 1)] = Hx[I3(i, j, bz1 - 1)] - c2h * Eyinc[i] / dz;
+                    Hx[I3(i, j, bz2 - 1)] = Hx[I3(i, j, bz2 - 1)] + c2h * Eyinc[i] / dz;
+                }
+        } else {
+            for (int i = bx1 - 1; i <= bx2; i++)
+                for (int j = by1 - 1; j <= by2; j++)
+                    for (int k = bz1 - 1; k <= bz2; k++) {
+                        double corr;
+                        if (SHELL(i, j, k) && obl_corr(&O, 0, 0, i, j, k, Ezinc, &corr))
+                            Hx[I3(i, j, k)] = Hx[I3(i, j, k)] + c2h * corr;
+                    }
+        }
         if (in.dopml) {
             for (int i = 0; i < Nx; i++) {
                 for (int j = 0; j < L; j++)
                     for (int k = 0; k < Nz - 1; k++)
-                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] - c2h * P_hxy[PY(i, j, k)];
+                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] - c2h * KAP(P_hxy[PY(i, j, k)], Kh, j, Ez[I3(i, j + 1, k)] - Ez[I3(i, j, k)], dy);
                 for (int j = Ny - L - 1; j < Ny - 1; j++)
                     for (int k = 0; k < Nz - 1; k++)
-                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] - c2h * P_hxy[PY(i, j - yshift, k)];
+                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] - c2h * KAP(P_hxy[PY(i, j - yshift, k)], Kh, j - yshift, Ez[I3(i, j + 1, k)] - Ez[I3(i, j, k)], dy);
             }
             for (int i = 0; i < Nx; i++)
                 for (int j = 0; j < Ny - 1; j++) {
                     for (int k = 0; k < L; k++)
-                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] + c2h * P_hxz[PZ(i, j, k)];
+                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] + c2h * KAP(P_hxz[PZ(i, j, k)], Kh, k, Ey[I3(i, j, k + 1)] - Ey[I3(i, j, k)], dz);
                     for (int k = Nz - L - 1; k < Nz - 1; k++)
-                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] + c2h * P_hxz[PZ(i, j, k - zshift)];
+                        Hx[I3(i, j, k)] = Hx[I3(i, j, k)] + c2h * KAP(P_hxz[PZ(i, j, k - zshift)], Kh, k - zshift, Ey[I3(i, j, k + 1)] - Ey[I3(i, j, k)], dz);
                 }
         }
 
@@ -486,30 +731,40 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
             for (int j = 0; j < Ny; j++)
                 for (int k = 0; k < Nz - 1; k++)
                     Hy[I3(i, j, k)] = c1h * Hy[I3(i, j, k)] - c2h * ((Ex[I3(i, j, k + 1)] - Ex[I3(i, j, k)]) / dz - (Ez[I3(i + 1, j, k)] - Ez[I3(i, j, k)]) / dx);
-            Hyinc[i] = c1h * Hyinc[i] + c2h * (Ezinc[i + 1] - Ezinc[i]) / dx;
+            if (!obl) Hyinc[i] = c1h * Hyinc[i] + c2h * (Ezinc[i + 1] - Ezinc[i]) / dx;
         }
-        for (int j = by1; j < by2; j++)
-            for (int k = bz1; k < bz2; k++) {
-                Hy[I3(bx1 - 1, j, k)] = Hy[I3(bx1 - 1, j, k)] - c2h * Ezinc[bx1] / dx;
-                Hy[I3(bx2 - 1, j, k)] = Hy[I3(bx2 - 1, j, k)] + c2h * Ezinc[bx2 - 1] / dx;
-            }
+        if (!obl) {
+            for (int j = by1; j < by2; j++)
+                for (int k = bz1; k < bz2; k++) {
+                    Hy[I3(bx1 - 1, j, k)] = Hy[I3(bx1 - 1, j, k)] - c2h * Ezinc[bx1] / dx;
+                    Hy[I3(bx2 - 1, j, k)] = Hy[I3(bx2 - 1, j, k)] + c2h * Ezinc[bx2 - 1] / dx;
+                }
+        } else {
+            for (int i = bx1 - 1; i <= bx2; i++)
+                for (int j = by1 - 1; j <= by2; j++)
+                    for (int k = bz1 - 1; k <= bz2; k++) {
+                        double corr;
+                        if (SHELL(i, j, k) && obl_corr(&O, 0, 1, i, j, k, Ezinc, &corr))
+                            Hy[I3(i, j, k)] = Hy[I3(i, j, k)] + c2h * corr;
+                    }
+        }
         if (in.dopml) {
             for (int i = 0; i < L; i++)
                 for (int j = 0; j < Ny; j++)
                     for (int k = 0; k < Nz - 1; k++)
-                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] + c2h * P_hyx[PX(i, j, k)];
+                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] + c2h * KAP(P_hyx[PX(i, j, k)], Kh, i, Ez[I3(i + 1, j, k)] - Ez[I3(i, j, k)], dx);
             for (int i = Nx - L - 1; i < Nx - 1; i++) {
                 for (int j = 0; j < Ny; j++)
                     for (int k = 0; k < Nz - 1; k++)
-                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] + c2h * P_hyx[PX(i - xshift, j, k)];
-                Hyinc[i] = Hyinc[i] + c2h * P_hyxI[i - xshift];
+                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] + c2h * KAP(P_hyx[PX(i - xshift, j, k)], Kh, i - xshift, Ez[I3(i + 1, j, k)] - Ez[I3(i, j, k)], dx);
+                if (!obl) Hyinc[i] = Hyinc[i] + c2h * P_hyxI[i - xshift];
             }
             for (int i = 0; i < Nx - 1; i++)
                 for (int j = 0; j < Ny; j++) {
                     for (int k = 0; k < L; k++)
-                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] - c2h * P_hyz[PZ(i, j, k)];
+                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] - c2h * KAP(P_hyz[PZ(i, j, k)], Kh, k, Ex[I3(i, j, k + 1)] - Ex[I3(i, j, k)], dz);
                     for (int k = Nz - L - 1; k < Nz - 1; k++)
-                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] - c2h * P_hyz[PZ(i, j, k - zshift)];
+                        Hy[I3(i, j, k)] = Hy[I3(i, j, k)] - c2h * KAP(P_hyz[PZ(i, j, k - zshift)], Kh, k - zshift, Ex[I3(i, j, k + 1)] - Ex[I3(i, j, k)], dz);
                 }
         }
 
@@ -519,31 +774,55 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
             for (int j = 0; j < Ny - 1; j++)
                 for (int k = 0; k < Nz; k++)
                     Hz[I3(i, j, k)] = c1h * Hz[I3(i, j, k)] - c2h * ((Ey[I3(i + 1, j, k)] - Ey[I3(i, j, k)]) / dx - (Ex[I3(i, j + 1, k)] - Ex[I3(i, j, k)]) / dy);
-            Hzinc[i] = c1h * Hzinc[i] - c2h * (Eyinc[i + 1] - Eyinc[i]) / dx;
+            if (!obl) Hzinc[i] = c1h * Hzinc[i] - c2h * (Eyinc[i + 1] - Eyinc[i]) / dx;
         }
-        for (int j = by1; j < by2; j++)
-            for (int k = bz1; k < bz2; k++) {
-                Hz[I3(bx1 - 1, j, k)] = Hz[I3(bx1 - 1, j, k)] + c2h * Eyinc[bx1] / dx;
-                Hz[I3(bx2 - 1, j, k)] = Hz[I3(bx2 - 1, j, k)] - c2h * Eyinc[bx2 - 1] / dx;
-            }
+        if (!obl) {
+            for (int j = by1; j < by2; j++)
+                for (int k = bz1; k < bz2; k++) {
+                    Hz[I3(bx1 - 1, j, k)] = Hz[I3(bx1 - 1, j, k)] + c2h * Eyinc[bx1] / dx;
+                    Hz[I3(bx2 - 1, j, k)] = Hz[I3(bx2 - 1, j, k)] - c2h * Eyinc[bx2 - 1] / dx;
+                }
+        } else {
+            for (int i = bx1 - 1; i <= bx2; i++)
+                for (int j = by1 - 1; j <= by2; j++)
+                    for (int k = bz1 - 1; k <= bz2; k++) {
+                        double corr;
+                        if (SHELL(i, j, k) && obl_corr(&O, 0, 2, i, j, k, Ezinc, &corr))
+                            Hz[I3(i, j, k)] = Hz[I3(i, j, k)] + c2h * corr;
+                    }
+        }
         if (in.dopml) {
             for (int i = 0; i < L; i++)
                 for (int j = 0; j < Ny - 1; j++)
                     for (int k = 0; k < Nz; k++)
-                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] - c2h * P_hzx[PX(i, j, k)];
+                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] - c2h * KAP(P_hzx[PX(i, j, k)], Kh, i, Ey[I3(i + 1, j, k)] - Ey[I3(i, j, k)], dx);
             for (int i = Nx - L - 1; i < Nx - 1; i++) {
                 for (int j = 0; j < Ny - 1; j++)
                     for (int k = 0; k < Nz; k++)
-                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] - c2h * P_hzx[PX(i - xshift, j, k)];
-                Hzinc[i] = Hzinc[i] - c2h * P_hzxI[i - xshift];
+                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] - c2h * KAP(P_hzx[PX(i - xshift, j, k)], Kh, i - xshift, Ey[I3(i + 1, j, k)] - Ey[I3(i, j, k)], dx);
+                if (!obl) Hzinc[i] = Hzinc[i] - c2h * P_hzxI[i - xshift];
             }
             for (int i = 0; i < Nx - 1; i++) {
                 for (int j = 0; j < L; j++)
                     for (int k = 0; k < Nz; k++)
-                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] + c2h * P_hzy[PY(i, j, k)];
+                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] + c2h * KAP(P_hzy[PY(i, j, k)], Kh, j, Ex[I3(i, j + 1, k)] - Ex[I3(i, j, k)], dy);
                 for (int j = Ny - L - 1; j < Ny - 1; j++)
                     for (int k = 0; k < Nz; k++)
-                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] + c2h * P_hzy[PY(i, j - yshift, k)];
+                        Hz[I3(i, j, k)] = Hz[I3(i, j, k)] + c2h * KAP(P_hzy[PY(i, j - yshift, k)], Kh, j - yshift, Ex[I3(i, j + 1, k)] - Ex[I3(i, j, k)], dy);
+            }
+        }
+
+        /* ---------------- auxiliary line, H part (oblique incidence) ------ */
+        if (obl) {
+            const int M = O.M;
+            for (int n = 0; n < M - 1; n++) {
+                double h = c1h * Hyinc[n] - c2h * (Ezinc[n + 1] - Ezinc[n]) / O.dl;
+                if (n >= M - L - 1) {
+                    const int sidx = n - O.ashift;
+                    P_h1[sidx] = T1.Bh[sidx] * P_h1[sidx] + T1.Ah[sidx] * (Ezinc[n + 1] - Ezinc[n]) / O.dl;
+                    h = h - c2h * P_h1[sidx];
+                }
+                Hyinc[n] = h;
             }
         }
 
@@ -642,7 +921,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                 for (int j = 0; j < Ny - 1; j++)
                     for (int k = 1; k < Nz - 1; k++)
                         P_eyx[PX(i - xshift, j, k)] = Be[i - xshift] * P_eyx[PX(i - xshift, j, k)] + Ae[i - xshift] * (Hz[I3(i, j, k)] - Hz[I3(i - 1, j, k)]) / dx;
-                P_eyxI[i - xshift] = Be[i - xshift] * P_eyxI[i - xshift] + Ae[i - xshift] * (Hzinc[i] - Hzinc[i - 1]) / dx;
+                if (!obl) P_eyxI[i - xshift] = Be[i - xshift] * P_eyxI[i - xshift] + Ae[i - xshift] * (Hzinc[i] - Hzinc[i - 1]) / dx;
             }
             for (int i = 1; i < Nx - 1; i++)
                 for (int j = 0; j < Ny - 1; j++) {
@@ -659,7 +938,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                 for (int j = 1; j < Ny - 1; j++)
                     for (int k = 0; k < Nz - 1; k++)
                         P_ezx[PX(i - xshift, j, k)] = Be[i - xshift] * P_ezx[PX(i - xshift, j, k)] + Ae[i - xshift] * (Hy[I3(i, j, k)] - Hy[I3(i - 1, j, k)]) / dx;
-                P_ezxI[i - xshift] = Be[i - xshift] * P_ezxI[i - xshift] + Ae[i - xshift] * (Hyinc[i] - Hyinc[i - 1]) / dx;
+                if (!obl) P_ezxI[i - xshift] = Be[i - xshift] * P_ezxI[i - xshift] + Ae[i - xshift] * (Hyinc[i] - Hyinc[i - 1]) / dx;
             }
             for (int i = 1; i < Nx - 1; i++) {
                 for (int j = 1; j < L + 1; j++)
@@ -679,31 +958,41 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                     size_t c = I3(i, j, k);
                     Ex[c] = c1e[c] * Ex[c] + c2e[c] * ((Hz[c] - Hz[I3(i, j - 1, k)]) / dy - (Hy[c] - Hy[I3(i, j, k - 1)]) / dz) - c2e[c] * Jx[c];
                 }
-        for (int i = bx1; i < bx2 - 1; i++)
-            for (int j = by1; j < by2; j++) {
-                Ex[I3(i, j, bz1)] = Ex[I3(i, j, bz1)] + c2e0 * Hyinc[i] / dz;
-                Ex[I3(i, j, bz2)] = Ex[I3(i, j, bz2)] - c2e0 * Hyinc[i] / dz;
-            }
-        for (int i = bx1; i < bx2 - 1; i++)
-            for (int k = bz1; k < bz2; k++) {
-                Ex[I3(i, by1, k)] = Ex[I3(i, by1, k)] - c2e0 * Hzinc[i] / dy;
-                Ex[I3(i, by2, k)] = Ex[I3(i, by2, k)] + c2e0 * Hzinc[i] / dy;
-            }
+        if (!obl) {
+            for (int i = bx1; i < bx2 - 1; i++)
+                for (int j = by1; j < by2; j++) {
+                    Ex[I3(i, j, bz1)] = Ex[I3(i, j, bz1)] + c2e0 * Hyinc[i] / dz;
+                    Ex[I3(i, j, bz2)] = Ex[I3(i, j, bz2)] - c2e0 * Hyinc[i] / dz;
+                }
+            for (int i = bx1; i < bx2 - 1; i++)
+                for (int k = bz1; k < bz2; k++) {
+                    Ex[I3(i, by1, k)] = Ex[I3(i, by1, k)] - c2e0 * Hzinc[i] / dy;
+                    Ex[I3(i, by2, k)] = Ex[I3(i, by2, k)] + c2e0 * Hzinc[i] / dy;
+                }
+        } else {
+            for (int i = bx1 - 1; i <= bx2; i++)
+                for (int j = by1 - 1; j <= by2; j++)
+                    for (int k = bz1 - 1; k <= bz2; k++) {
+                        double corr;
+                        if (SHELL(i, j, k) && obl_corr(&O, 1, 0, i, j, k, Hyinc, &corr))
+                            Ex[I3(i, j, k)] = Ex[I3(i, j, k)] + c2e0 * corr;
+                    }
+        }
         if (in.dopml) {
             for (int i = 0; i < Nx - 1; i++) {
                 for (int j = 1; j < L + 1; j++)
                     for (int k = 1; k < Nz - 1; k++)
-                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] + c2e0 * P_exy[PY(i, j - 1, k)];
+                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] + c2e0 * KAP(P_exy[PY(i, j - 1, k)], Ke, j - 1, Hz[I3(i, j, k)] - Hz[I3(i, j - 1, k)], dy);
                 for (int j = Ny - L - 1; j < Ny - 1; j++)
                     for (int k = 1; k < Nz - 1; k++)
-                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] + c2e0 * P_exy[PY(i, j - yshift, k)];
+                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] + c2e0 * KAP(P_exy[PY(i, j - yshift, k)], Ke, j - yshift, Hz[I3(i, j, k)] - Hz[I3(i, j - 1, k)], dy);
             }
             for (int i = 0; i < Nx - 1; i++)
                 for (int j = 1; j < Ny - 1; j++) {
                     for (int k = 1; k < L + 1; k++)
-                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] - c2e0 * P_exz[PZ(i, j, k - 1)];
+                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] - c2e0 * KAP(P_exz[PZ(i, j, k - 1)], Ke, k - 1, Hy[I3(i, j, k)] - Hy[I3(i, j, k - 1)], dz);
                     for (int k = Nz - L - 1; k < Nz - 1; k++)
-                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] - c2e0 * P_exz[PZ(i, j, k - zshift)];
+                        Ex[I3(i, j, k)] = Ex[I3(i, j, k)] - c2e0 * KAP(P_exz[PZ(i, j, k - zshift)], Ke, k - zshift, Hy[I3(i, j, k)] - Hy[I3(i, j, k - 1)], dz);
                 }
         }
 
@@ -715,30 +1004,40 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                     size_t c = I3(i, j, k);
                     Ey[c] = c1e[c] * Ey[c] + c2e[c] * ((Hx[c] - Hx[I3(i, j, k - 1)]) / dz - (Hz[c] - Hz[I3(i - 1, j, k)]) / dx) - c2e[c] * Jy[c];
                 }
-            Eyinc[i] = c1e0 * Eyinc[i] - c2e0 * (Hzinc[i] - Hzinc[i - 1]) / dx;
+            if (!obl) Eyinc[i] = c1e0 * Eyinc[i] - c2e0 * (Hzinc[i] - Hzinc[i - 1]) / dx;
         }
-        for (int j = by1; j < by2; j++)
-            for (int k = bz1; k < bz2; k++) {
-                Ey[I3(bx1, j, k)] = Ey[I3(bx1, j, k)] + c2e0 * Hzinc[bx1 - 1] / dx;
-                Ey[I3(bx2 - 1, j, k)] = Ey[I3(bx2 - 1, j, k)] - c2e0 * Hzinc[bx2 - 1] / dx;
-            }
+        if (!obl) {
+            for (int j = by1; j < by2; j++)
+                for (int k = bz1; k < bz2; k++) {
+                    Ey[I3(bx1, j, k)] = Ey[I3(bx1, j, k)] + c2e0 * Hzinc[bx1 - 1] / dx;
+                    Ey[I3(bx2 - 1, j, k)] = Ey[I3(bx2 - 1, j, k)] - c2e0 * Hzinc[bx2 - 1] / dx;
+                }
+        } else {
+            for (int i = bx1 - 1; i <= bx2; i++)
+                for (int j = by1 - 1; j <= by2; j++)
+                    for (int k = bz1 - 1; k <= bz2; k++) {
+                        double corr;
+                        if (SHELL(i, j, k) && obl_corr(&O, 1, 1, i, j, k, Hyinc, &corr))
+                            Ey[I3(i, j, k)] = Ey[I3(i, j, k)] + c2e0 * corr;
+                    }
+        }
         if (in.dopml) {
             for (int i = 1; i < L + 1; i++)
                 for (int j = 0; j < Ny; j++)
                     for (int k = 1; k < Nz; k++)
-                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] - c2e0 * P_eyx[PX(i - 1, j, k)];
+                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] - c2e0 * KAP(P_eyx[PX(i - 1, j, k)], Ke, i - 1, Hz[I3(i, j, k)] - Hz[I3(i - 1, j, k)], dx);
             for (int i = Nx - L - 1; i < Nx - 1; i++) {
                 for (int j = 0; j < Ny; j++)
                     for (int k = 1; k < Nz; k++)
-                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] - c2e0 * P_eyx[PX(i - xshift, j, k)];
-                Eyinc[i] = Eyinc[i] - c2e0 * P_eyxI[i - xshift];
+                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] - c2e0 * KAP(P_eyx[PX(i - xshift, j, k)], Ke, i - xshift, Hz[I3(i, j, k)] - Hz[I3(i - 1, j, k)], dx);
+                if (!obl) Eyinc[i] = Eyinc[i] - c2e0 * P_eyxI[i - xshift];
             }
             for (int i = 1; i < Nx - 1; i++)
                 for (int j = 0; j < Ny; j++) {
                     for (int k = 1; k < L + 1; k++)
-                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] + c2e0 * P_eyz[PZ(i, j, k - 1)];
+                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] + c2e0 * KAP(P_eyz[PZ(i, j, k - 1)], Ke, k - 1, Hx[I3(i, j, k)] - Hx[I3(i, j, k - 1)], dz);
                     for (int k = Nz - L - 1; k < Nz - 1; k++)
-                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] + c2e0 * P_eyz[PZ(i, j, k - zshift)];
+                        Ey[I3(i, j, k)] = Ey[I3(i, j, k)] + c2e0 * KAP(P_eyz[PZ(i, j, k - zshift)], Ke, k - zshift, Hx[I3(i, j, k)] - Hx[I3(i, j, k - 1)], dz);
                 }
         }
 
@@ -750,21 +1049,45 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                     size_t c = I3(i, j, k);
                     Ez[c] = c1e[c] * Ez[c] + c2e[c] * ((Hy[c] - Hy[I3(i - 1, j, k)]) / dx - (Hx[c] - Hx[I3(i, j - 1, k)]) / dy) - c2e[c] * Jz[c];
                 }
-            Ezinc[i] = c1e0 * Ezinc[i] + c2e0 * (Hyinc[i] - Hyinc[i - 1]) / dx;
+            if (!obl) Ezinc[i] = c1e0 * Ezinc[i] + c2e0 * (Hyinc[i] - Hyinc[i - 1]) / dx;
         }
-        for (int j = by1; j < by2; j++)
-            for (int k = bz1; k < bz2; k++) {
-                Ez[I3(bx1, j, k)] = Ez[I3(bx1, j, k)] - c2e0 * Hyinc[bx1 - 1] / dx;
-                Ez[I3(bx2 - 1, j, k)] = Ez[I3(bx2 - 1, j, k)] + c2e0 * Hyinc[bx2 - 1] / dx;
-            }
+        if (!obl) {
+            for (int j = by1; j < by2; j++)
+                for (int k = bz1; k < bz2; k++) {
+                    Ez[I3(bx1, j, k)] = Ez[I3(bx1, j, k)] - c2e0 * Hyinc[bx1 - 1] / dx;
+                    Ez[I3(bx2 - 1, j, k)] = Ez[I3(bx2 - 1, j, k)] + c2e0 * Hyinc[bx2 - 1] / dx;
+                }
+        } else {
+            for (int i = bx1 - 1; i <= bx2; i++)
+                for (int j = by1 - 1; j <= by2; j++)
+                    for (int k = bz1 - 1; k <= bz2; k++) {
+                        double corr;
+                        if (SHELL(i, j, k) && obl_corr(&O, 1, 2, i, j, k, Hyinc, &corr))
+                            Ez[I3(i, j, k)] = Ez[I3(i, j, k)] + c2e0 * corr;
+                    }
+        }
 
         /* ---------------- source, R21:1278-1304 ---------------- */
-        switch (in.sourcepol) {
-        case 2: Ezinc[0] = 0; Eyinc[0] = EsA[t]; break;
-        case 3: Ezinc[0] = EsA[t]; Eyinc[0] = EsA[t]; break;
-        case 4: Ezinc[0] = EsA[t]; Eyinc[0] = EsB[t]; break;
-        case 5: Ezinc[0] = EsB[t]; Eyinc[0] = EsA[t]; break;
-        default: Ezinc[0] = EsA[t]; Eyinc[0] = 0; break; /* 1 and others */
+        if (obl) { /* auxiliary line, E part, then the hard source at node 0 */
+            const int M = O.M;
+            for (int n = 1; n < M - 1; n++) {
+                double e = c1e0 * Ezinc[n] - c2e0 * (Hyinc[n] - Hyinc[n - 1]) / O.dl;
+                if (n >= M - L - 1) {
+                    const int sidx = n - O.ashift;
+                    P_e1[sidx] = T1.Be[sidx] * P_e1[sidx] + T1.Ae[sidx] * (Hyinc[n] - Hyinc[n - 1]) / O.dl;
+                    e = e - c2e0 * P_e1[sidx];
+                }
+                Ezinc[n] = e;
+            }
+            Ezinc[0] = EsA[t];
+        } else {
+            switch (in.sourcepol) {
+            case 2: Ezinc[0] = 0; Eyinc[0] = EsA[t]; break;
+            case 3: Ezinc[0] = EsA[t]; Eyinc[0] = EsA[t]; break;
+            case 4: Ezinc[0] = EsA[t]; Eyinc[0] = EsB[t]; break;
+            case 5: Ezinc[0] = EsB[t]; Eyinc[0] = EsA[t]; break;
+            default: Ezinc[0] = EsA[t]; Eyinc[0] = 0; break; /* 1 and others */
+            }
         }
 
         /* ---------------- plate, R21:1307-1320 ---------------- */
@@ -799,20 +1122,20 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
             for (int i = 1; i < L + 1; i++)
                 for (int j = 1; j < Ny; j++)
                     for (int k = 0; k < Nz; k++)
-                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] + c2e0 * P_ezx[PX(i - 1, j, k)];
+                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] + c2e0 * KAP(P_ezx[PX(i - 1, j, k)], Ke, i - 1, Hy[I3(i, j, k)] - Hy[I3(i - 1, j, k)], dx);
             for (int i = Nx - L - 1; i < Nx - 1; i++) {
                 for (int j = 1; j < Ny; j++)
                     for (int k = 0; k < Nz; k++)
-                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] + c2e0 * P_ezx[PX(i - xshift, j, k)];
-                Ezinc[i] = Ezinc[i] + c2e0 * P_ezxI[i - xshift];
+                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] + c2e0 * KAP(P_ezx[PX(i - xshift, j, k)], Ke, i - xshift, Hy[I3(i, j, k)] - Hy[I3(i - 1, j, k)], dx);
+                if (!obl) Ezinc[i] = Ezinc[i] + c2e0 * P_ezxI[i - xshift];
             }
             for (int i = 1; i < Nx - 1; i++) {
                 for (int j = 1; j < L + 1; j++)
                     for (int k = 0; k < Nz - 1; k++)
-                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] - c2e0 * P_ezy[PY(i, j - 1, k)];
+                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] - c2e0 * KAP(P_ezy[PY(i, j - 1, k)], Ke, j - 1, Hx[I3(i, j, k)] - Hx[I3(i, j - 1, k)], dy);
                 for (int j = Ny - L - 1; j < Ny - 1; j++)
                     for (int k = 0; k < Nz - 1; k++)
-                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] - c2e0 * P_ezy[PY(i, j - yshift, k)];
+                        Ez[I3(i, j, k)] = Ez[I3(i, j, k)] - c2e0 * KAP(P_ezy[PY(i, j - yshift, k)], Ke, j - yshift, Hx[I3(i, j, k)] - Hx[I3(i, j - 1, k)], dy);
             }
         }
 
@@ -935,9 +1258,11 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                         double K00 = Ee2 * (Ce2 * wcex * wcex + Ce3), K01 = Ee2 * (Ce2 * wcex * wcey - Ce4 * wcez), K02 = Ee2 * (Ce2 * wcex * wcez + Ce4 * wcey);
                         double K10 = Ee2 * (Ce2 * wcey * wcex + Ce4 * wcez), K11 = Ee2 * (Ce2 * wcey * wcey + Ce3), K12 = Ee2 * (Ce2 * wcey * wcez - Ce4 * wcex);
                         double K20 = Ee2 * (Ce2 * wcez * wcex - Ce4 * wcey), K21 = Ee2 * (Ce2 * wcez * wcey + Ce4 * wcex), K22 = Ee2 * (Ce2 * wcez * wcez + Ce3);
-                        double m0 = (Ex[c] + Ex[I3(i - 1, j, k)]) / 2;
-                        double m1 = (Ey[c] + Ey[I3(i, j - 1, k)]) / 2;
-                        double m2 = (Ez[c] + Ez[I3(i, j, k - 1)]) / 2;
+                        /* extended input lk_colocated: E at the current's own node */
+                        const int colo = in.ext.lk_colocated;
+                        double m0 = colo ? Ex[c] : (Ex[c] + Ex[I3(i - 1, j, k)]) / 2;
+                        double m1 = colo ? Ey[c] : (Ey[c] + Ey[I3(i, j - 1, k)]) / 2;
+                        double m2 = colo ? Ez[c] : (Ez[c] + Ez[I3(i, j, k - 1)]) / 2;
                         double jx = Jx[c], jy = Jy[c], jz = Jz[c];
                         Jx[c] = A00 * jx + A01 * jy + A02 * jz + OR_E0 * w * w * (K00 * m0 + K01 * m1 + K02 * m2);
                         Jy[c] = A10 * jx + A11 * jy + A12 * jz + OR_E0 * w * w * (K10 * m0 + K11 * m1 + K12 * m2);

@@ -61,3 +61,61 @@ def cases() -> Dict[str, Tuple[rd.RunParams, np.ndarray, np.ndarray, tuple]]:
         # no probes, no saved fields, one record step
         "quiet": _mk(probex=[], probey=[], probez=[], savefields=0, numfiles=1, doB0=1),
     }
+
+
+# ---------------------------------------------------------------------------
+# Extended inputs (ext.dat; no counterpart in the reference).  Each case is
+# (RunParams, wp, nu, B0, ExtParams, wp3 or None, nu3 or None).  The oracle is
+# the checker for these; its extensions are validated by physics tests
+# (TF/SF leakage, normal incidence through the oblique path, Mie series).
+
+def _ext_mk(N=(48, 48, 48), **kw):
+    # Courant 0.9 and 160+ steps: the pulse crosses the Huygens surface.
+    d = dict(dt=rd.stable_dt(0.25, 0.9), tsteps=160, fsig=20.0, numfiles=8)
+    d.update(kw)
+    return _mk(N=N, **d)
+
+
+def ext_cases():
+    out = {}
+    # CPML of the 96x96x192 benchmark configuration: m = 3, kappa_max = 5,
+    # alpha_max = 0.05, 12 cells; TF/SF box 8 cells and Huygens surface 4 cells
+    # inside the CPML; reference +x plane wave.
+    p, wp, nu, B0 = _ext_mk(doB0=1)
+    out["ext_cpml"] = (p, wp, nu, B0,
+                       rd.ExtParams(pmllen=12, tfsf_gap=8, ntf_gap=4, pml_m=3.0, kappa_max=5.0,
+                                    alpha_max=0.05), None, None)
+    # Tilted trail with log-varying density, magnetized (L&K, uniform nu), oblique
+    # TM incidence at theta = 70, phi = 20 degrees: the 768x768x1536 set-up in small.
+    p, wp, nu, B0 = _ext_mk(doB0=1, nu=3e4, metsize=(1e200, 1e200))
+    wp3 = rd.tilted_trail_wp3(p.Nx, p.Ny, p.Nz, p.dx, 30.0, 0.8, 13.0, 15.0)
+    out["ext_oblique_trail"] = (p, wp * 0, nu, B0,
+                                rd.ExtParams(pmllen=8, tfsf_gap=6, ntf_gap=3, pml_m=3.0,
+                                             kappa_max=5.0, alpha_max=0.05, oblique=1,
+                                             exact_coords=1, lk_colocated=1,
+                                             inc_theta=math.radians(70),
+                                             inc_phi=math.radians(20)), wp3, None)
+    # Unmagnetized collisional plasma sphere (per-cell maps), oblique TE incidence.
+    p, wp, nu, B0 = _ext_mk(doB0=0, fntf=[40e6, 50e6, 60e6], metsize=(1e200, 1e200))
+    wp3 = rd.plasma_sphere_wp3(p.Nx, p.Ny, p.Nz, p.dx, 2.0, 5e13)
+    nu3 = np.full((p.Nx, p.Ny, p.Nz), 1e5)
+    out["ext_sphere"] = (p, wp * 0, nu, (0.0, 0.0, 0.0),
+                         rd.ExtParams(oblique=1, exact_coords=1, inc_theta=math.radians(30),
+                                      inc_phi=math.radians(60), inc_psi=math.pi / 2),
+                         wp3, nu3)
+    # Collision frequency per cell with L&K (one matrix pair per cell), oblique.
+    p, wp, nu, B0 = _ext_mk(N=(44, 44, 44), doB0=1, tsteps=120, metsize=(1e200, 1e200))
+    rng = np.random.default_rng(11)
+    nu3 = 2e4 + 6e4 * rng.random((p.Nx, p.Ny, p.Nz))
+    wp3 = rd.tilted_trail_wp3(p.Nx, p.Ny, p.Nz, p.dx, 45.0, 1.0, 14.0, 15.0)
+    out["ext_lk_cell"] = (p, wp * 0, nu, B0,
+                          rd.ExtParams(oblique=1, inc_theta=math.radians(120),
+                                       inc_phi=math.radians(-35), inc_psi=0.3), wp3, nu3)
+    return out
+
+
+def write_ext_case(d, case):
+    """Write a full run directory (inputs + ext.dat + maps) for an ext case."""
+    p, wp, nu, B0, ext, wp3, nu3 = case
+    rd.write_rundir(d, p, wp, nu, B0)
+    rd.write_ext(d, ext, wp3, nu3)
