@@ -54,38 +54,52 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 def workload(name: str, steps_total: int):
-    """(RunParams, wp2 [Nx][Ny] C-order, nu2, B0, description)."""
-    if name == "trail768":
-        # Large single trail at 768 x 768 x 1536 cells, dx = 0.2 m (50 MHz radar,
-        # gridfactor 30), overdense Gaussian trail r0 = 0.8 m along z,
-        # nu = 3e4 1/s, B0 = 5e-5 T dipped 60 degrees, Lee-Kalluri current.
+    """(RunParams, wp2 [Nx][Ny] C-order, nu2, B0, description, MATLAB-shaped wp,
+    ExtParams or None, TrailParams or None)."""
+    B0 = (5e-5 * math.cos(math.pi / 3), 0.0, -5e-5 * math.sin(math.pi / 3))  # 60 deg dip
+    ext = trail = None
+    if name in ("trail768", "trailprof"):
+        # Large single trail: 768 x 768 x 1536 cells (trailprof: 128 x 384 x 1024,
+        # the profiling-size case with the same physics), dx = 0.2 m (50 MHz
+        # radar, gridfactor 30), 12-cell CPML graded m = 3, kappa_max = 5,
+        # alpha_max = 0.05; trail axis tilted 30 degrees from z in the x-z plane,
+        # log10 n0 rising linearly from 13 to 16 along it, r0 = 0.8 m; nu = 3e4;
+        # B0 = 5e-5 T dipped 60 degrees; oblique TM plane wave along
+        # (theta, phi) = (70, 20) degrees; Lee-Kalluri current driven by E at the
+        # current's node (the reference's two-node average diverges here).
+        N = (768, 768, 1536) if name == "trail768" else (128, 384, 1024)
+        f0, gf, nu = 50e6, 30.0, 3e4
+        desc = (f"{N[0]}x{N[1]}x{N[2]} tilted magnetized trail, dx=0.2 m, 12-cell CPML "
+                "(m=3, kappa_max=5, alpha_max=0.05), trail axis 30 deg from z in x-z, "
+                "log10 n0 13..16 along the axis, r0=0.8 m, nu=3e4, B0=5e-5 T at 60 deg dip, "
+                "oblique TM plane wave theta=70 phi=20 deg, Lee-Kalluri J (E at the J node)")
+        ext = rd.ExtParams(pmllen=12, pml_m=3.0, kappa_max=5.0, alpha_max=0.05, oblique=1,
+                           exact_coords=1, lk_colocated=1, inc_theta=math.radians(70),
+                           inc_phi=math.radians(20), inc_psi=0.0)
+        dx = rd.C0 / f0 / gf
+        trail = rd.TrailParams.tilted(30.0, 0.8, 13.0, 16.0, 0.5 * (N[2] - 1) * dx)
+        n0, r0 = 0.0, 0.8
+    elif name == "trail768_refinputs":
+        # What the reference's own input format can express at the same size:
+        # 10-cell CPML, plane wave along +x, z-uniform Gaussian trail.
         N = (768, 768, 1536)
         f0, gf = 50e6, 30.0
         desc = ("768x768x1536 magnetized trail, dx=0.2 m, Lee-Kalluri J, 10-cell CPML, "
                 "plane wave along +x (Ez), z-uniform Gaussian trail n0=1e15 r0=0.8 m, "
                 "nu=3e4, B0=5e-5 T at 60 deg dip")
         n0, r0, nu = 1e15, 0.8, 3e4
-    elif name == "trail256":
-        # Profiling-size version of trail768 (2 GB of FP32 state, > L2).
-        N = (256, 256, 512)
-        f0, gf = 50e6, 30.0
-        desc = ("256x256x512 magnetized trail, dx=0.2 m, Lee-Kalluri J, 10-cell CPML, "
-                "plane wave along +x (Ez), z-uniform Gaussian trail n0=1e15 r0=0.8 m")
-        n0, r0, nu = 1e15, 0.8, 3e4
-    elif name == "trailprof":
-        # Profiling case: same physics, 128x384x1024 (3 GB FP32 state, > L2),
-        # with an interior/boundary mix close to the 768x768x1536 trail's.
-        N = (128, 384, 1024)
-        f0, gf = 50e6, 30.0
-        desc = ("128x384x1024 magnetized trail (profiling size), dx=0.2 m, Lee-Kalluri J, "
-                "10-cell CPML, plane wave along +x (Ez), n0=1e15 r0=0.8 m")
-        n0, r0, nu = 1e15, 0.8, 3e4
     elif name == "cfg1":
+        # 96 x 96 x 192, dx = 0.25 m, 10-cell CPML graded m = 3, kappa_max = 5,
+        # alpha_max = 0.05, TF/SF box 8 and Huygens surface 4 cells inside it,
+        # plane wave along +x with E along z, overdense Gaussian trail along z.
         N = (96, 96, 192)
         f0, gf = 50e6, 24.0
-        desc = ("96x96x192 magnetized trail, dx=0.25 m, Lee-Kalluri J, n0=1e14 r0=1 m, "
-                "nu=5e4, B0=5e-5 T at 60 deg dip")
+        desc = ("96x96x192 magnetized trail, dx=0.25 m, CPML m=3 kappa_max=5 alpha_max=0.05, "
+                "TF/SF gap 8, NTF gap 4, Lee-Kalluri J, n0=1e14 r0=1 m, nu=5e4, "
+                "B0=5e-5 T at 60 deg dip")
         n0, r0, nu = 1e14, 1.0, 5e4
+        ext = rd.ExtParams(pmllen=10, tfsf_gap=8, ntf_gap=4, pml_m=3.0, kappa_max=5.0,
+                           alpha_max=0.05)
     else:
         raise SystemExit(f"unknown workload {name}")
     Nx, Ny, Nz = N
@@ -94,43 +108,58 @@ def workload(name: str, steps_total: int):
                      fsig=20.0, gridfactor=gf, numfiles=1, savefields=0, probex=[Nx // 2],
                      probey=[Ny // 2], probez=[Nz // 2], fntf=[f0], metsize=(1e200, 1e200),
                      doB0=1)
-    wp = rd.gaussian_trail_wp(p, n0, r0)
+    wp = rd.gaussian_trail_wp(p, n0, r0) if n0 > 0 else np.zeros((Nx, Ny))
     nu2 = np.full((Nx, Ny), nu)
-    B0 = (5e-5 * math.cos(math.pi / 3), 0.0, -5e-5 * math.sin(math.pi / 3))
     wp2 = np.asarray(wp).reshape(-1, order="F").reshape(Nx, Ny)
-    return p, wp2, nu2, B0, desc, wp
+    return p, wp2, nu2, B0, desc, wp, ext, trail
 
 
-def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams) -> float:
+def make_problem(E, p, wp2, nu2, B0, ext, trail):
+    """The public-API call sequence a user makes for this workload."""
+    pb = E.Problem.from_params(p, wp2, nu2, B0)
+    if ext is not None:
+        pb.set_ext(ext)
+    if trail is not None:
+        pb.set_trail(trail)
+    return pb
+
+
+def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
+                      per_cell_map: bool = False) -> float:
     """Compulsory DRAM bytes of one launch of `kernel` (per cell-update figure
     x cells, plus the CPML psi slabs each launch reads and writes)."""
     cells = p.Nx * p.Ny * p.Nz
-    L = 10
     psi = 2 * (2 * L * p.Ny * p.Nz + p.Nx * 2 * L * p.Nz + p.Nx * p.Ny * 2 * L)  # one half-step
     if form == "fp64":
-        if kernel == "k_plain_h":   # E r(3), H r/w(6), J r/w(6) ; psi r/w
-            return cells * 15 * 8 + psi * 16
+        m = 8 if per_cell_map else 0
+        if kernel == "k_plain_h":   # E r(3), H r/w(6), J r/w(6) ; psi r/w ; omega_p map
+            return cells * (15 * 8 + m) + psi * 16
         if kernel == "k_plain_e":   # H r(3), E r/w(6), J r(3) ; psi r/w
             return cells * 12 * 8 + psi * 16
     else:
-        # FP32 single pass: E, H, J read and written (18 x 4 B); the plasma
-        # weight comes from 2-D/1-D tables (no per-cell read); every psi cell
-        # of both half-steps read and written once.
-        return cells * 18 * 4 + 2 * psi * 8
+        # FP32 single pass: E, H, J read and written (18 x 4 B), plus the
+        # per-cell E0 wp^2 map when the plasma is 3-D (4 B); every psi cell of
+        # both half-steps read and written once.
+        return cells * (18 * 4 + (4 if per_cell_map else 0)) + 2 * psi * 8
     raise KeyError(kernel)
 
 
-def traffic_per_launch(form: str, workload: str, kernel: str, alg: float):
-    """DRAM traffic (read + write bytes) of one launch, from an ncu capture.
+# DRAM traffic / algorithmic bytes of k_fp32_step measured by ncu on the
+# profiling-size case of each workload (profiles/): the full-size grids are too
+# large for a multi-pass capture, and the halo overhead per cell is a property
+# of the tile geometry, so a full launch's traffic is the ratio times its
+# algorithmic bytes.
+TRAFFIC_RATIO = {
+    # profiles/k_fp32_step_trailprof_refinputs_full.md: 4.30 GB / 3.99 GB
+    "trail768_refinputs": 4.3015e9 / 3.9909e9,
+}
 
-    k_fp32_step: profiles/k_fp32_step_trailprof_full.md measured 4.30 GB of
-    DRAM traffic against 3.99 GB of algorithmic bytes (ratio 1.08) on the
-    128x384x1024 profiling case; the full-size trail is too large for a
-    multi-pass capture, so its traffic is that ratio times its own
-    algorithmic bytes (the halo overhead per cell is the same tile geometry).
-    """
-    if form == "fp32" and kernel == "k_fp32_step":
-        return alg * (4.3015e9 / 3.9909e9)
+
+def traffic_per_launch(form: str, workload: str, kernel: str, alg: float):
+    """DRAM traffic (read + write bytes) of one launch, or None when no ncu
+    capture of this workload's kernel is recorded."""
+    if form == "fp32" and kernel == "k_fp32_step" and workload in TRAFFIC_RATIO:
+        return alg * TRAFFIC_RATIO[workload]
     return None
 
 
@@ -201,12 +230,16 @@ def _unlimited_stack():
 
 def cpu_baseline(name: str, steps: int, budget_s: float = 20.0):
     """Time the reference CPU path on a slab of the workload (full Nx x Ny,
-    reduced Nz) for a few steps; returns a cpu_baseline dict."""
-    p, wp2, nu2, B0, desc, wp = workload(name, 4)
+    reduced Nz) for a few steps; returns a cpu_baseline dict.  Workloads the
+    reference's input format cannot express (extended inputs) run in the C
+    restatement, which implements them; the rest run in the reference binary
+    where it was built from source on this host."""
+    p, wp2, nu2, B0, desc, wp, ext, trail = workload(name, 4)
     threads = os.cpu_count() or 1
     nz = min(p.Nz, max(24, int(4e7 // (p.Nx * p.Ny))))
     ref_exe = os.path.join(ROOT, "oracle", "_ref", "meteor_fork")
-    use_ref = os.path.exists(ref_exe) and os.access(ref_exe, os.X_OK)
+    use_ref = (os.path.exists(ref_exe) and os.access(ref_exe, os.X_OK) and ext is None
+               and trail is None)
     oracle_so = os.path.join(ROOT, "oracle", "_build", "liboracle.so")
     if not use_ref and not os.path.exists(oracle_so):
         from meteorscattering_gb300 import build as B
@@ -219,6 +252,9 @@ def cpu_baseline(name: str, steps: int, budget_s: float = 20.0):
                                     probez=[nz // 2])
             shutil.rmtree(d, ignore_errors=True)
             rd.write_rundir(d, q, wp, np.full((p.Nx, p.Ny), nu2.flat[0]), B0)
+            if ext is not None:
+                rd.write_ext(d, ext)
+            rd.write_trail(d, trail)
             env = dict(os.environ, OMP_NUM_THREADS=str(threads))
             if use_ref:
                 t0 = time.perf_counter()
@@ -303,7 +339,9 @@ def main():
     K, W = args.steps, max(args.warmup, 0)
 
     rank, world, local, pg = dist_setup(args.gpus)
-    p, wp2, nu2, B0, desc, _ = workload(args.workload, K + W + 1)
+    p, wp2, nu2, B0, desc, _, ext, trail = workload(args.workload, K + W + 1)
+    L = ext.pmllen if ext is not None else 10
+    per_cell = trail is not None
     cells = p.Nx * p.Ny * p.Nz
 
     if args.impl == "reference":
@@ -327,7 +365,7 @@ def main():
 
     form = E.FORM_FP32_FUSED if args.form == "fp32" else E.FORM_FP64_PLAIN
     device = local
-    pb = E.Problem.from_params(p, wp2, nu2, B0)
+    pb = make_problem(E, p, wp2, nu2, B0, ext, trail)
     sim = E.Simulation(pb, form=form, device=device, profile=True)
     if W:
         sim.advance(W)
@@ -352,7 +390,7 @@ def main():
     peak, peak_kind = load_peaks()
     roof = None
     if dom:
-        alg = algorithmic_bytes(args.form, dom[0], p)
+        alg = algorithmic_bytes(args.form, dom[0], p, L, per_cell)
         ach = alg / (dom[1] * 1e-3) / 1e9
         roof = {"kernel": dom[0], "bound": "hbm", "achieved": ach, "peak": peak,
                 "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
@@ -365,7 +403,7 @@ def main():
     if not args.no_e2e:
         barrier(pg)
         t0 = time.perf_counter()
-        pb2 = E.Problem.from_params(p, wp2, nu2, B0)
+        pb2 = make_problem(E, p, wp2, nu2, B0, ext, trail)
         s2 = E.Simulation(pb2, form=form, device=device)
         s2.advance(K)
         ntf = s2.read_ntf()
@@ -395,7 +433,7 @@ def main():
                            "form": "fp32_fused" if args.form == "fp32" else "fp64_plain",
                            "parallelism": f"replicas x{world}",
                            "l2": "state larger than L2 (no flush needed)"},
-                "hbm_gbs": (algorithmic_bytes(args.form, dom[0], p) / (dom[1] * 1e-3) / 1e9)
+                "hbm_gbs": (algorithmic_bytes(args.form, dom[0], p, L, per_cell) / (dom[1] * 1e-3) / 1e9)
                 if dom else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "host_wall_s": wall}

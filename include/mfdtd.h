@@ -118,6 +118,26 @@ typedef struct {
                              k and z), psi = pi/2 is TE                         */
 } mfdtd_ext;
 
+/* Parametric meteor trail (extended input; the reference builds trails only
+ * as a 2-D map times a Gaussian in z, setup/meteorrun.m:83-104 and
+ * source/meteor-2.1.cpp:319-334).  Electron density
+ *     n = n0(s) exp(-d^2 / r0^2),
+ * s the position along the axis through `centre` with direction `axis`, d the
+ * distance from that axis; log10 n0 rises linearly from log10n_lo at
+ * s = -s_half to log10n_hi at s = +s_half and is held beyond.  Positions are
+ * the grid's cell coordinates -(N-1)/2*d + i*d along every axis (metres,
+ * grid centre at the origin); omega_p = sqrt(n QE^2 / (E0 ME)) with the
+ * solver's constants.  The engine evaluates the map on the device (FP64), so
+ * no per-cell array crosses the host boundary. */
+typedef struct {
+    double centre[3];   /* m                                  */
+    double axis[3];     /* direction; normalised by the engine */
+    double r0;          /* m, > 0                              */
+    double log10n_lo;   /* log10 of n0 in m^-3 at s = -s_half  */
+    double log10n_hi;   /* log10 of n0 in m^-3 at s = +s_half  */
+    double s_half;      /* m, > 0                              */
+} mfdtd_trail;
+
 typedef struct mfdtd_problem mfdtd_problem; /* parsed inputs + derived tables */
 typedef struct mfdtd_sim mfdtd_sim;         /* device-resident state          */
 
@@ -150,6 +170,9 @@ void mfdtd_ext_defaults(mfdtd_ext *ext);
  * the reference, which cannot express these inputs. */
 int mfdtd_problem_set_ext(mfdtd_problem *pb, const mfdtd_ext *ext, const double *wp3,
                           const double *nu3);
+/* Use a parametric trail for the plasma frequency (replaces wp2 * G(z) and any
+ * wp3 map); NULL removes it.  Run directories carry it as trail.dat. */
+int mfdtd_problem_set_trail(mfdtd_problem *pb, const mfdtd_trail *trail);
 /* Grid and run sizes: out[0..5] = Nx, Ny, Nz, tsteps, nntf, nprobes. */
 int mfdtd_problem_dims(const mfdtd_problem *pb, int64_t out[6]);
 /* Device bytes a simulation of this problem in `form` will hold. */

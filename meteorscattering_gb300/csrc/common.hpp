@@ -69,6 +69,8 @@ struct Problem {
     mfdtd_ext ext{};
     int ext_present = 0;
     std::vector<double> wp3, nu3;      // [Nx][Ny][Nz] omega_p and nu, when given
+    int has_trail = 0;                 // parametric trail (replaces wp2 * G and wp3)
+    mfdtd_trail trail{};               // axis normalised
 
     // derived, extended
     int kappa_on = 0;
@@ -127,5 +129,9 @@ int plain_launch_step(const PlainArgs &a, int t, int record, void *stream, void 
 int plain_launch_flush(const PlainArgs &a, int t_last, void *stream);
 int plain_launch_emax(const PlainArgs &a, void *stream);
 int plain_launch_guard(const PlainArgs &a, void *stream);
+
+// omega_p of a parametric trail at every cell, [Nx][Ny][Nz] doubles
+// (plain_fp64.cu).  The same formula in FP64 feeds the FP32 form.
+void trail_map_fp64(const Problem &P, double *out, void *stream);
 
 }  // namespace mfdtd

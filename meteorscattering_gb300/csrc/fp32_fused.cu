@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "fp32.hpp"
+#include "trail.cuh"
 
 namespace mfdtd {
 namespace {
@@ -212,35 +213,49 @@ __device__ __forceinline__ float obl_h_new_at(const Args &a, float s) {
     const float h1 = a.c1h * h[n + 1] - a.chl * (e[n + 2] - e[n + 1]);
     return h0 + (s - fl) * (h1 - h0);
 }
-// Correction to add to component C of E (IS_E) or H at cell (i,j,k), already
-// scaled by c2/d.  Zero when no curl-term neighbour crosses the surface.
+// Crossing term along axis AX for component C of E (IS_E) or H at cell
+// (i,j,k), already scaled by c2/d_AX.  Along one axis a node type crosses the
+// box surface at two indices only (H: b1-1 and b2-1; E: b1 and b2-1), and only
+// where its coordinates along the other two axes lie inside the box; the
+// neighbour across the surface is the third component.  Same terms as the
+// generic construction (sign = curl sign x side x (T - Tn)).
+template <int PAR, bool IS_E, int C, int AX>
+__device__ __forceinline__ float obl_axis(const Args &a, int i, int j, int k) {
+    constexpr int Q = 3 - C - AX;                                     // neighbour component
+    constexpr int SG = (AX == (C + 1) % 3) ? (IS_E ? 1 : -1) : (IS_E ? -1 : 1);
+    const int idx[3] = {i, j, k};
+    const int b1[3] = {a.bx1, a.by1, a.bz1}, b2[3] = {a.bx2, a.by2, a.bz2};
+    const int n = idx[AX];
+    int nb;      // neighbour index along AX
+    float sgn;
+    if (IS_E) {
+        if (n == b1[AX]) { nb = n - 1; sgn = (float)-SG; }
+        else if (n == b2[AX] - 1) { nb = n; sgn = (float)SG; }
+        else return 0.f;
+    } else {
+        if (n == b1[AX] - 1) { nb = n + 1; sgn = (float)-SG; }
+        else if (n == b2[AX] - 1) { nb = n; sgn = (float)SG; }
+        else return 0.f;
+    }
+    // doubled coordinates of the neighbour: E comp Q is staggered along Q only,
+    // H comp Q along the two axes other than Q
+    int P[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const int st = IS_E ? (d != Q) : (d == Q);  // neighbour staggering
+        const int tst = IS_E ? (d == C) : (d != C); // target staggering
+        P[d] = d == AX ? 2 * nb + st : 2 * idx[d] + tst;
+        if (d != AX && (P[d] < 2 * b1[d] || P[d] > 2 * (b2[d] - 1))) return 0.f;
+    }
+    const float sp = a.kr[0] * (0.5f * P[0]) + a.kr[1] * (0.5f * P[1]) + a.kr[2] * (0.5f * P[2]) + a.s0;
+    const float inc = IS_E ? a.kh[Q] * obl_h_new_at<PAR>(a, sp - 0.5f) : a.ke[Q] * obl_e_at<PAR>(a, sp);
+    const float cd = IS_E ? (AX == 0 ? a.cex : AX == 1 ? a.cey : a.cez)
+                          : (AX == 0 ? a.chx : AX == 1 ? a.chy : a.chz);
+    return sgn * inc * cd;
+}
 template <int PAR, bool IS_E, int C>
-__device__ __noinline__ float obl_corr(const Args &a, int i, int j, int k) {
-    int P[3] = {2 * i, 2 * j, 2 * k};
-#pragma unroll
-    for (int q = 0; q < 3; q++)
-        if (IS_E ? q == C : q != C) P[q] += 1;
-    const int T = obl_in(a, P[0], P[1], P[2]);
-    constexpr int ax[2] = {(C + 1) % 3, (C + 2) % 3};
-    constexpr int comp[2] = {(C + 2) % 3, (C + 1) % 3};
-    constexpr int sg[2] = {IS_E ? 1 : -1, IS_E ? -1 : 1};
-    const float cd[3] = {IS_E ? a.cex : a.chx, IS_E ? a.cey : a.chy, IS_E ? a.cez : a.chz};
-    float acc = 0.f;
-#pragma unroll
-    for (int term = 0; term < 2; term++)
-#pragma unroll
-        for (int side = 1; side >= -1; side -= 2) {
-            int Q[3] = {P[0], P[1], P[2]};
-            Q[ax[term]] += side;
-            const int Tn = obl_in(a, Q[0], Q[1], Q[2]);
-            if (Tn == T) continue;
-            const float sp = a.kr[0] * (0.5f * Q[0]) + a.kr[1] * (0.5f * Q[1]) + a.kr[2] * (0.5f * Q[2]) + a.s0;
-            const float inc = IS_E ? a.kh[comp[term]] * obl_h_new_at<PAR>(a, sp - 0.5f)
-                                   : a.ke[comp[term]] * obl_e_at<PAR>(a, sp);
-            const float v = inc * cd[ax[term]];
-            acc += sg[term] * side * (T - Tn) > 0 ? v : -v;
-        }
-    return acc;
+__device__ __forceinline__ float obl_corr(const Args &a, int i, int j, int k) {
+    return obl_axis<PAR, IS_E, C, (C + 1) % 3>(a, i, j, k) + obl_axis<PAR, IS_E, C, (C + 2) % 3>(a, i, j, k);
 }
 
 // Per-tile facts that are uniform across the CTA.
@@ -1102,6 +1117,23 @@ __global__ void __launch_bounds__(256) k_fp32_scan(const float *__restrict__ ex,
     }
 }
 
+// E0 * omega_p^2 of a parametric trail, FP64 evaluation stored as FP32 in the
+// padded [Nx][Ny][Nzp] layout.
+__global__ void k_trail_wq(TrailDev t, int Nzp, float *out) {
+    const size_t n = (size_t)t.Nx * t.Ny * Nzp;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % Nzp);
+        const size_t ij = q / Nzp;
+        float v = 0.f;
+        if (k < t.Nz) {
+            const double wp = trail_wp(t, (int)(ij / t.Ny), (int)(ij % t.Ny), k);
+            v = (float)(kE0 * wp * wp);
+        }
+        out[q] = v;
+    }
+}
+
 // Copy one slice/field buffer of floats to doubles.
 __global__ void k_f2d(const float *__restrict__ in, double *__restrict__ out, size_t n) {
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
@@ -1195,7 +1227,7 @@ int64_t Fp32Sim::footprint(const Problem &P) {
     const int64_t psi = P.dopml ? (L2 * P.Ny * P.Nz + (int64_t)P.Nx * L2 * P.Nz + (int64_t)P.Nx * P.Ny * L2) * 2 : 0;
     const int64_t nf2 = 2 * P.nntf();
     const int64_t ntf = 8 * nf2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz + (int64_t)P.Nx * P.Ny);
-    const int64_t maps = cells * 4 * ((P.wp3.empty() ? 0 : 1) + (P.nu3.empty() ? 0 : 1));
+    const int64_t maps = cells * 4 * ((P.wp3.empty() && !P.has_trail ? 0 : 1) + (P.nu3.empty() ? 0 : 1));
     return cells * 4 * 15 + maps + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2);
 }
 
@@ -1276,7 +1308,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         for (size_t q = 0; q < wq2.size(); q++) wq2[q] = (float)(kE0 * P.wp2e[q] * P.wp2e[q]);
         for (size_t q = 0; q < nu2.size(); q++) nu2[q] = (float)P.nu2e[q];
         // A per-cell map replaces the 2-D map times the z profile: its G factor is 1.
-        const bool w3 = !P.wp3.empty() && !P.doplate, n3 = !P.nu3.empty() && !P.doplate;
+        const bool w3 = (!P.wp3.empty() || P.has_trail) && !P.doplate;
+        const bool n3 = !P.nu3.empty() && !P.doplate;
         for (int k = 0; k < P.Nz; k++) {
             G[k] = n3 ? 1.f : (float)P.G[k];
             G2[k] = w3 ? 1.f : (float)(P.G[k] * P.G[k]);
@@ -1290,7 +1323,14 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                 }
             return out;
         };
-        a.wq3 = w3 ? m.upload(per_cell(P.wp3, true), s) : nullptr;
+        if (w3 && P.has_trail) {  // generated on the device: no per-cell host array
+            float *wq = m.alloc<float>((size_t)P.Nx * P.Ny * m.Nzp, s);
+            k_trail_wq<<<152 * 8, 256, 0, s>>>(trail_dev(P), m.Nzp, wq);
+            ck(cudaGetLastError(), "trail map");
+            a.wq3 = wq;
+        } else {
+            a.wq3 = w3 ? m.upload(per_cell(P.wp3, true), s) : nullptr;
+        }
         a.nu3 = n3 ? m.upload(per_cell(P.nu3, false), s) : nullptr;
         a.wq2 = m.upload(wq2, s); a.nu2 = m.upload(nu2, s); a.G = m.upload(G, s); a.G2 = m.upload(G2, s);
         std::vector<float> lk(P.lk.begin(), P.lk.end());

@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "common.hpp"
+#include "trail.cuh"
 
 namespace mfdtd {
 namespace {
@@ -650,7 +651,20 @@ __global__ void __launch_bounds__(256) k_nonfinite(const double *__restrict__ ex
     if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flag, 1u);
 }
 
+__global__ void k_trail_map(TrailDev t, double *out) {
+    const size_t n = (size_t)t.Nx * t.Ny * t.Nz;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+         q += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(q % t.Nz), j = (int)((q / t.Nz) % t.Ny), i = (int)(q / ((size_t)t.Ny * t.Nz));
+        out[q] = trail_wp(t, i, j, k);
+    }
+}
+
 }  // namespace
+
+void trail_map_fp64(const Problem &P, double *out, void *stream) {
+    k_trail_map<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(trail_dev(P), out);
+}
 
 int plain_launch_guard(const PlainArgs &a, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;

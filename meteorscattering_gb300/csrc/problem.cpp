@@ -61,6 +61,26 @@ bool file_exists(const std::string &path) {
 // rundir.py write_ext) and the per-cell maps it announces.  The reference
 // never writes these files, so its run directories are unaffected.
 void read_ext_sidecars(const std::string &dir, Problem &P) {
+    // trail.dat: 8-byte magic then 12 doubles (centre[3], axis[3], r0,
+    // log10n_lo, log10n_hi, s_half, 0, 0).
+    const std::string tpath = dir + "/trail.dat";
+    if (file_exists(tpath)) {
+        Reader r;
+        r.name = tpath;
+        r.buf = slurp(tpath);
+        if (r.buf.size() < 8 || std::memcmp(r.buf.data(), "MFDTDT01", 8) != 0)
+            throw Error(MFDTD_EIO, tpath + ": not a trail file (bad magic)");
+        r.off = 8;
+        mfdtd_trail t;
+        for (double &v : t.centre) v = r.get<double>();
+        for (double &v : t.axis) v = r.get<double>();
+        t.r0 = r.get<double>();
+        t.log10n_lo = r.get<double>();
+        t.log10n_hi = r.get<double>();
+        t.s_half = r.get<double>();
+        P.trail = t;
+        P.has_trail = 1;
+    }
     const std::string path = dir + "/ext.dat";
     if (!file_exists(path)) return;
     Reader r;
@@ -86,6 +106,7 @@ void read_ext_sidecars(const std::string &dir, Problem &P) {
     e.inc_psi = r.get<double>();
     P.ext = e;
     P.ext_present = 1;
+    if (!has_wp3 && !has_nu3) return;
     const size_t n3 = P.cells();
     for (int q = 0; q < 2; q++) {
         if (!(q == 0 ? has_wp3 : has_nu3)) continue;
@@ -271,6 +292,15 @@ Problem problem_from_params(const mfdtd_params &p, const double *wp2, const doub
 
 void Problem::derive() {
     if (!ext_present) ext_defaults(ext);
+    if (has_trail) {
+        const double an = sqrt(trail.axis[0] * trail.axis[0] + trail.axis[1] * trail.axis[1] +
+                               trail.axis[2] * trail.axis[2]);
+        if (!(an > 0) || !(trail.r0 > 0) || !(trail.s_half > 0) || !std::isfinite(trail.log10n_lo) ||
+            !std::isfinite(trail.log10n_hi) || trail.log10n_lo > 30 || trail.log10n_hi > 30)
+            throw Error(MFDTD_EINVAL, "trail: need a nonzero axis, r0 > 0, s_half > 0 and "
+                                      "log10 densities <= 30");
+        for (double &v : trail.axis) v = v / an;
+    }
     L = ext.pmllen;  // source/meteor-2.1.cpp:343 (10)
     if (ext_present) {
         if (L < 1 || L > kMaxPml) throw Error(MFDTD_EINVAL, "pmllen must be in [1, 32]");

@@ -183,7 +183,14 @@ struct mfdtd_sim {
         a.PeyxI = dalloc<double>(L2); a.PezxI = dalloc<double>(L2);
         a.PhyxI = dalloc<double>(L2); a.PhzxI = dalloc<double>(L2);
         a.wp2 = upload(P.wp2e); a.nu2 = upload(P.nu2e); a.G = upload(P.G);
-        a.wp3 = P.wp3.empty() ? nullptr : upload(P.wp3);
+        if (P.has_trail) {  // omega_p of the parametric trail, evaluated on the device
+            double *w = dalloc<double>(NC);
+            mfdtd::trail_map_fp64(P, w, stream);
+            mfdtd::ck(cudaGetLastError(), "trail map");
+            a.wp3 = w;
+        } else {
+            a.wp3 = P.wp3.empty() ? nullptr : upload(P.wp3);
+        }
         a.nu3 = P.nu3.empty() ? nullptr : upload(P.nu3);
         a.xc = upload(P.x); a.yc = upload(P.y); a.zc = upload(P.z);
         a.lk = upload(P.lk); a.src = upload(P.src); a.phase = upload(P.phase);
@@ -536,6 +543,17 @@ void mfdtd_ext_defaults(mfdtd_ext *ext) {
     if (ext) mfdtd::ext_defaults(*ext);
 }
 
+int mfdtd_problem_set_trail(mfdtd_problem *pb, const mfdtd_trail *trail) {
+    return guarded([&] {
+        if (!pb) throw Error(MFDTD_EINVAL, "NULL problem");
+        Problem P = pb->P;
+        P.has_trail = trail ? 1 : 0;
+        if (trail) P.trail = *trail;
+        P.derive();
+        pb->P = std::move(P);
+    });
+}
+
 int mfdtd_problem_set_ext(mfdtd_problem *pb, const mfdtd_ext *ext, const double *wp3,
                           const double *nu3) {
     return guarded([&] {
@@ -573,7 +591,8 @@ int mfdtd_problem_footprint(const mfdtd_problem *pb, int32_t form, int64_t *byte
         const int64_t ntf = 8 * nf2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz + (int64_t)P.Nx * P.Ny);
         const int64_t misc = 8 * ((int64_t)P.tsteps * (2 + nf2 + 6 * P.nprobes()) + (int64_t)P.lk.size() +
                                   4 * ((int64_t)P.Nx * P.Ny + P.Nx + P.Ny + P.Nz));
-        if (form == MFDTD_FORM_FP64_PLAIN) *bytes = 8 * (9 * NC + psi) + 8 * ntf + misc;
+        const int64_t maps = 8 * NC * ((P.wp3.empty() && !P.has_trail ? 0 : 1) + (P.nu3.empty() ? 0 : 1));
+        if (form == MFDTD_FORM_FP64_PLAIN) *bytes = 8 * (9 * NC + psi) + 8 * ntf + misc + maps;
         else *bytes = mfdtd::Fp32Sim::footprint(P);
     });
 }

@@ -34,7 +34,7 @@ EXPORTS = (
     "mfdtd_sim_read_probes", "mfdtd_sim_read_field", "mfdtd_sim_write_outputs",
     "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_sim_far_field",
     "mfdtd_far_field_static", "mfdtd_last_error", "mfdtd_version", "mfdtd_ext_defaults",
-    "mfdtd_problem_set_ext",
+    "mfdtd_problem_set_ext", "mfdtd_problem_set_trail",
 )
 
 
@@ -72,6 +72,12 @@ class Ext(C.Structure):
         ("pml_m", C.c_double), ("kappa_max", C.c_double), ("alpha_max", C.c_double),
         ("inc_theta", C.c_double), ("inc_phi", C.c_double), ("inc_psi", C.c_double),
     ]
+
+
+class Trail(C.Structure):
+    """``mfdtd_trail`` -- parametric trail."""
+    _fields_ = [("centre", C.c_double * 3), ("axis", C.c_double * 3), ("r0", C.c_double),
+                ("log10n_lo", C.c_double), ("log10n_hi", C.c_double), ("s_half", C.c_double)]
 
 
 _lib: Optional[C.CDLL] = None
@@ -113,6 +119,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
                                              dp, vp]),
         "mfdtd_ext_defaults": (None, [C.POINTER(Ext)]),
         "mfdtd_problem_set_ext": (C.c_int, [vp, C.POINTER(Ext), dp, dp]),
+        "mfdtd_problem_set_trail": (C.c_int, [vp, C.POINTER(Trail)]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -213,6 +220,18 @@ class Problem:
             return _dp(a)
 
         _check(lib.mfdtd_problem_set_ext(self._h, C.byref(e), arr(wp3), arr(nu3)))
+        return self
+
+    def set_trail(self, trail=None) -> "Problem":
+        """Parametric trail (a :class:`rundir.TrailParams`) for the plasma
+        frequency, evaluated on the device; None removes it."""
+        lib = load_library()
+        if trail is None:
+            _check(lib.mfdtd_problem_set_trail(self._h, None))
+            return self
+        t = Trail((C.c_double * 3)(*trail.centre), (C.c_double * 3)(*trail.axis), trail.r0,
+                  trail.log10n_lo, trail.log10n_hi, trail.s_half)
+        _check(lib.mfdtd_problem_set_trail(self._h, C.byref(t)))
         return self
 
     def dims(self):

@@ -199,7 +199,7 @@ def write_rundir(path: str, p: RunParams, wp: np.ndarray, nu: np.ndarray,
     with open(os.path.join(path, "nu.dat"), "wb") as f:
         f.write(nu.tobytes(order="F"))
     for name in ("output_E.dat", "output_H.dat", "output_J.dat", "Probe.dat",
-                 "output_NTF.dat", "log.txt", "ext.dat", "wp3.dat", "nu3.dat"):
+                 "output_NTF.dat", "log.txt", "ext.dat", "wp3.dat", "nu3.dat", "trail.dat"):
         fp = os.path.join(path, name)
         if os.path.exists(fp):
             os.remove(fp)
@@ -272,28 +272,69 @@ def write_ext(path: str, e: ExtParams, wp3: Optional[np.ndarray] = None,
             os.remove(fp)
 
 
-def tilted_trail_wp3(Nx: int, Ny: int, Nz: int, dx: float, tilt_deg: float, r0: float,
-                     log10n_lo: float, log10n_hi: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
-    """Per-cell plasma frequency of a straight trail whose axis is tilted by
-    ``tilt_deg`` from +z toward +x (staircased on the grid).  Density
-    n = n0(s) exp(-r^2 / r0^2), r the distance to the axis, s the position
-    along it; log10 n0 varies linearly from ``log10n_lo`` at the bottom of the
-    grid to ``log10n_hi`` at the top.  Cell-centred exact coordinates."""
-    x = grid_coords(Nx, dx)[:, None, None] - centre[0]
-    y = grid_coords(Ny, dx)[None, :, None] - centre[1]
-    z = grid_coords(Nz, dx)[None, None, :] - centre[2]
-    t = math.radians(tilt_deg)
-    ax = (math.sin(t), 0.0, math.cos(t))
+@dataclasses.dataclass
+class TrailParams:
+    """``mfdtd_trail`` of ``include/mfdtd.h``: n = n0(s) exp(-d^2/r0^2) about
+    an axis through ``centre`` along ``axis``; log10 n0 linear in s from
+    ``log10n_lo`` at s = -s_half to ``log10n_hi`` at s = +s_half, held beyond."""
+
+    centre: Sequence[float] = (0.0, 0.0, 0.0)
+    axis: Sequence[float] = (0.0, 0.0, 1.0)
+    r0: float = 1.0
+    log10n_lo: float = 14.0
+    log10n_hi: float = 14.0
+    s_half: float = 1.0
+
+    @classmethod
+    def tilted(cls, tilt_deg: float, r0: float, log10n_lo: float, log10n_hi: float,
+               s_half: float, centre=(0.0, 0.0, 0.0)) -> "TrailParams":
+        """Axis tilted ``tilt_deg`` from +z toward +x."""
+        t = math.radians(tilt_deg)
+        return cls(tuple(centre), (math.sin(t), 0.0, math.cos(t)), r0, log10n_lo, log10n_hi, s_half)
+
+
+TRAIL_MAGIC = b"MFDTDT01"
+
+
+def write_trail(path: str, t: Optional[TrailParams]) -> None:
+    """``trail.dat``: 8-byte magic and 12 float64 (centre, axis, r0, log10n_lo,
+    log10n_hi, s_half, 0, 0); ``None`` removes the file."""
+    fp = os.path.join(path, "trail.dat")
+    if t is None:
+        if os.path.exists(fp):
+            os.remove(fp)
+        return
+    with open(fp, "wb") as f:
+        f.write(TRAIL_MAGIC + struct.pack("<12d", *t.centre, *t.axis, t.r0, t.log10n_lo,
+                                          t.log10n_hi, t.s_half, 0.0, 0.0))
+
+
+def trail_wp3(Nx: int, Ny: int, Nz: int, dx: float, t: TrailParams) -> np.ndarray:
+    """The per-cell plasma frequency the engine evaluates for trail ``t``
+    (exact cell coordinates), as an ``[Nx][Ny][Nz]`` array."""
+    a = np.asarray(t.axis, dtype=np.float64)
+    a = a / math.sqrt(float(a @ a))
+    x = grid_coords(Nx, dx)[:, None, None] - t.centre[0]
+    y = grid_coords(Ny, dx)[None, :, None] - t.centre[1]
+    z = grid_coords(Nz, dx)[None, None, :] - t.centre[2]
     out = np.empty((Nx, Ny, Nz))
-    half = 0.5 * (Nz - 1) * dx
     for i in range(Nx):  # plane by plane keeps the temporaries small
         xi = x[i]
-        s_ax = xi * ax[0] + z * ax[2]                       # [1, Nz]
-        r2 = xi * xi + y * y + z * z - s_ax * s_ax          # [Ny, Nz]
-        frac = np.clip((s_ax + half) / (2 * half), 0.0, 1.0)
-        n0 = 10.0 ** (log10n_lo + (log10n_hi - log10n_lo) * frac)
-        out[i] = plasma_frequency(n0 * np.exp(-np.maximum(r2, 0.0) / (r0 * r0)))[0]
+        s = xi * a[0] + y * a[1] + z * a[2]
+        d2 = np.maximum(xi * xi + y * y + z * z - s * s, 0.0)
+        frac = np.clip((s + t.s_half) / (2 * t.s_half), 0.0, 1.0)
+        n0 = 10.0 ** (t.log10n_lo + (t.log10n_hi - t.log10n_lo) * frac)
+        out[i] = plasma_frequency(n0 * np.exp(-d2 / (t.r0 * t.r0)))
     return out
+
+
+def tilted_trail_wp3(Nx: int, Ny: int, Nz: int, dx: float, tilt_deg: float, r0: float,
+                     log10n_lo: float, log10n_hi: float, centre=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Per-cell plasma frequency of a straight trail tilted ``tilt_deg`` from +z
+    toward +x whose log10 density runs from ``log10n_lo`` at the bottom of the
+    grid to ``log10n_hi`` at the top."""
+    t = TrailParams.tilted(tilt_deg, r0, log10n_lo, log10n_hi, 0.5 * (Nz - 1) * dx, centre)
+    return trail_wp3(Nx, Ny, Nz, dx, t)
 
 
 def plasma_sphere_wp3(Nx: int, Ny: int, Nz: int, dx: float, radius: float,

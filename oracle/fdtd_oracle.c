@@ -72,6 +72,8 @@ typedef struct {
     double *wp2, *nu2; /* [Nx][Ny], C order as read */
     or_ext ext;
     double *wp3, *nu3; /* [Nx][Ny][Nz] per-cell maps (extended inputs) or NULL */
+    int has_trail;     /* trail.dat: parametric trail (extended input) */
+    double trail[10];  /* centre[3], axis[3] (normalised), r0, log10n_lo, log10n_hi, s_half */
 } or_in;
 
 static double now_s(void) {
@@ -192,6 +194,22 @@ static int read_inputs(const char *dir, or_in *p) {
     if (!f) return -1;
     e |= rd(p->nu2, 8, n2, f);
     fclose(f);
+    /* trail.dat: magic then 12 doubles */
+    f = open_in(dir, "trail.dat", "rb");
+    if (f) {
+        char magic[8];
+        double tv[12];
+        if (rd(magic, 1, 8, f) || memcmp(magic, "MFDTDT01", 8) || rd(tv, 8, 12, f)) {
+            fclose(f);
+            return -2;
+        }
+        fclose(f);
+        double an = sqrt(tv[3] * tv[3] + tv[4] * tv[4] + tv[5] * tv[5]);
+        if (!(an > 0) || !(tv[6] > 0) || !(tv[9] > 0)) return -3;
+        for (int q = 0; q < 10; q++) p->trail[q] = tv[q];
+        for (int q = 3; q < 6; q++) p->trail[q] = tv[q] / an;
+        p->has_trail = 1;
+    }
     /* per-cell maps announced by ext.dat */
     size_t n3 = n2 * (size_t)p->Nz;
     if (p->ext.has_wp3) {
@@ -486,6 +504,19 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                         wpe[c] = in.wp2[(size_t)i * Ny + j] * exp(-pow((z[k] - in.metloc[2]), 2) / (msig0 * msig0));
                         nue[c] = in.nu2[(size_t)i * Ny + j] * exp(-pow((z[k] - in.metloc[2]), 2) / (msig0 * msig0));
                         if (in.wp3) wpe[c] = in.wp3[c]; /* per-cell maps (extended inputs) */
+                        if (in.has_trail) { /* parametric trail, exact cell coordinates */
+                            const double *T = in.trail;
+                            const double px = -(Nx - 1) / 2.0 * dx + dx * i - T[0];
+                            const double py = -(Ny - 1) / 2.0 * dy + dy * j - T[1];
+                            const double pz = -(Nz - 1) / 2.0 * dz + dz * k - T[2];
+                            const double sa = px * T[3] + py * T[4] + pz * T[5];
+                            double d2 = px * px + py * py + pz * pz - sa * sa;
+                            if (d2 < 0) d2 = 0;
+                            double fr = (sa + T[9]) / (2 * T[9]);
+                            fr = fr < 0 ? 0 : (fr > 1 ? 1 : fr);
+                            const double n = pow(10.0, T[7] + (T[8] - T[7]) * fr) * exp(-d2 / (T[6] * T[6]));
+                            wpe[c] = sqrt(n * OR_QE * OR_QE / (OR_E0 * OR_ME));
+                        }
                         if (in.nu3) nue[c] = in.nu3[c];
                     }
         }
@@ -586,6 +617,10 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
                         (k) >= bz1 - 1 && (k) <= bz2 &&                                \
                         !((i) > bx1 && (i) < bx2 - 2 && (j) > by1 && (j) < by2 - 2 &&    \
                           (k) > bz1 && (k) < bz2 - 2))
+    /* next k of the shell scan: inside an interior (i,j) column the run
+     * bz1+1 .. bz2-3 holds no crossing and is skipped */
+#define SHELL_NEXT(i, j, k) (((i) > bx1 && (i) < bx2 - 2 && (j) > by1 && (j) < by2 - 2 && \
+                              (k) == bz1) ? bz2 - 2 : (k) + 1)
 
     /* NTF running sums, R21:558-610. */
     double *Ezdft = dalloc(2 * (size_t)nntf), *Eydft = dalloc(2 * (size_t)nntf);
@@ -701,7 +736,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
         } else {
             for (int i = bx1 - 1; i <= bx2; i++)
                 for (int j = by1 - 1; j <= by2; j++)
-                    for (int k = bz1 - 1; k <= bz2; k++) {
+                    for (int k = bz1 - 1; k <= bz2; k = SHELL_NEXT(i, j, k)) {
                         double corr;
                         if (SHELL(i, j, k) && obl_corr(&O, 0, 0, i, j, k, Ezinc, &corr))
                             Hx[I3(i, j, k)] = Hx[I3(i, j, k)] + c2h * corr;
@@ -742,7 +777,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
         } else {
             for (int i = bx1 - 1; i <= bx2; i++)
                 for (int j = by1 - 1; j <= by2; j++)
-                    for (int k = bz1 - 1; k <= bz2; k++) {
+                    for (int k = bz1 - 1; k <= bz2; k = SHELL_NEXT(i, j, k)) {
                         double corr;
                         if (SHELL(i, j, k) && obl_corr(&O, 0, 1, i, j, k, Ezinc, &corr))
                             Hy[I3(i, j, k)] = Hy[I3(i, j, k)] + c2h * corr;
@@ -785,7 +820,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
         } else {
             for (int i = bx1 - 1; i <= bx2; i++)
                 for (int j = by1 - 1; j <= by2; j++)
-                    for (int k = bz1 - 1; k <= bz2; k++) {
+                    for (int k = bz1 - 1; k <= bz2; k = SHELL_NEXT(i, j, k)) {
                         double corr;
                         if (SHELL(i, j, k) && obl_corr(&O, 0, 2, i, j, k, Ezinc, &corr))
                             Hz[I3(i, j, k)] = Hz[I3(i, j, k)] + c2h * corr;
@@ -972,7 +1007,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
         } else {
             for (int i = bx1 - 1; i <= bx2; i++)
                 for (int j = by1 - 1; j <= by2; j++)
-                    for (int k = bz1 - 1; k <= bz2; k++) {
+                    for (int k = bz1 - 1; k <= bz2; k = SHELL_NEXT(i, j, k)) {
                         double corr;
                         if (SHELL(i, j, k) && obl_corr(&O, 1, 0, i, j, k, Hyinc, &corr))
                             Ex[I3(i, j, k)] = Ex[I3(i, j, k)] + c2e0 * corr;
@@ -1015,7 +1050,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
         } else {
             for (int i = bx1 - 1; i <= bx2; i++)
                 for (int j = by1 - 1; j <= by2; j++)
-                    for (int k = bz1 - 1; k <= bz2; k++) {
+                    for (int k = bz1 - 1; k <= bz2; k = SHELL_NEXT(i, j, k)) {
                         double corr;
                         if (SHELL(i, j, k) && obl_corr(&O, 1, 1, i, j, k, Hyinc, &corr))
                             Ey[I3(i, j, k)] = Ey[I3(i, j, k)] + c2e0 * corr;
@@ -1060,7 +1095,7 @@ int oracle_run_dir(const char *dir, int max_steps, int nthreads, int mirror_dead
         } else {
             for (int i = bx1 - 1; i <= bx2; i++)
                 for (int j = by1 - 1; j <= by2; j++)
-                    for (int k = bz1 - 1; k <= bz2; k++) {
+                    for (int k = bz1 - 1; k <= bz2; k = SHELL_NEXT(i, j, k)) {
                         double corr;
                         if (SHELL(i, j, k) && obl_corr(&O, 1, 2, i, j, k, Hyinc, &corr))
                             Ez[I3(i, j, k)] = Ez[I3(i, j, k)] + c2e0 * corr;

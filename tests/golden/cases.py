@@ -119,3 +119,23 @@ def write_ext_case(d, case):
     p, wp, nu, B0, ext, wp3, nu3 = case
     rd.write_rundir(d, p, wp, nu, B0)
     rd.write_ext(d, ext, wp3, nu3)
+
+
+def trail_case(N=(48, 48, 48), steps=160):
+    """Parametric trail (trail.dat): tilted 30 degrees, log10 n0 from 13 to 15,
+    magnetized with the co-located Lee-Kalluri update, oblique incidence, the
+    benchmark's CPML grading.  Returns (RunParams, wp, nu, B0, ExtParams,
+    TrailParams)."""
+    p, wp, nu, B0 = _ext_mk(N=N, doB0=1, nu=3e4, metsize=(1e200, 1e200), tsteps=steps)
+    ext = rd.ExtParams(pmllen=8, tfsf_gap=6, ntf_gap=3, pml_m=3.0, kappa_max=5.0, alpha_max=0.05,
+                       oblique=1, exact_coords=1, lk_colocated=1, inc_theta=math.radians(70),
+                       inc_phi=math.radians(20))
+    tr = rd.TrailParams.tilted(30.0, 0.8, 13.0, 15.0, 0.5 * (N[2] - 1) * p.dx)
+    return p, wp * 0, nu, B0, ext, tr
+
+
+def write_trail_case(d, case):
+    p, wp, nu, B0, ext, tr = case
+    rd.write_rundir(d, p, wp, nu, B0)
+    rd.write_ext(d, ext)
+    rd.write_trail(d, tr)

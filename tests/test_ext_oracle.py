@@ -116,6 +116,23 @@ def test_ext_cases_run_finite_in_the_oracle(built, tmp_path, name):
     assert np.isfinite(v).all() and np.abs(v).max() > 0
 
 
+def test_oracle_trail_matches_the_map_generator(built, tmp_path):
+    """The oracle's parametric-trail evaluation (trail.dat) and the numpy map
+    generator (rundir.trail_wp3 written as wp3.dat) describe the same plasma:
+    the runs agree to rounding of the transcendental functions."""
+    case = golden_cases.trail_case()
+    p, wp, nu, B0, ext, tr = case
+    da = os.path.join(str(tmp_path), "trail")
+    golden_cases.write_trail_case(da, case)
+    H.run_oracle(da)
+    db = _run(tmp_path, "map", p, wp, nu, B0, ext, rd.trail_wp3(p.Nx, p.Ny, p.Nz, p.dx, tr))
+    A = rd.read_ntf(os.path.join(da, "output_NTF.dat"), p)
+    B = rd.read_ntf(os.path.join(db, "output_NTF.dat"), p)
+    a = np.concatenate([A[k].ravel() for k, _ in rd.NTF_FACE_ORDER])
+    b = np.concatenate([B[k].ravel() for k, _ in rd.NTF_FACE_ORDER])
+    assert np.abs(a).max() > 1.0 and H.rel_l2(a, b) < 1e-10
+
+
 # ---- host logic of the extended inputs (library, no GPU) ----------------------
 
 def test_ext_file_roundtrip(tmp_path):
@@ -160,3 +177,14 @@ def test_set_ext_checks_map_shape(built):
     pb = E.Problem.from_params(p, np.asarray(wp), np.asarray(nu), B0)
     with pytest.raises(ValueError):
         pb.set_ext(rd.ExtParams(), wp3=np.zeros((p.Nx, p.Ny, p.Nz + 1)))
+
+
+def test_trail_rejects_bad_parameters(built):
+    p, wp, nu, B0 = golden_cases.cases()["lk_trail"]
+    pb = E.Problem.from_params(p, np.asarray(wp), np.asarray(nu), B0)
+    for bad in (dict(r0=0.0), dict(axis=(0.0, 0.0, 0.0)), dict(s_half=-1.0), dict(log10n_hi=40.0)):
+        with pytest.raises(E.MfdtdError) as ei:
+            pb.set_trail(rd.TrailParams(**bad))
+        assert E.STATUS[ei.value.code] == "EINVAL"
+    pb.set_trail(rd.TrailParams())
+    pb.set_trail(None)

@@ -109,3 +109,38 @@ def test_plasma_sphere_against_mie(built, tmp_path):
         err = np.abs(10 * np.log10(got[form] / want))
         assert err.max() < 0.7, (form, err)  # measured <= 0.55 dB with the FP64 oracle
     assert np.abs(10 * np.log10(got[E.FORM_FP32_FUSED] / got[E.FORM_FP64_PLAIN])).max() < 0.1
+
+
+def _groups(d, p):
+    ntf = rd.read_ntf(os.path.join(d, "output_NTF.dat"), p)
+    pr = rd.read_probes(os.path.join(d, "Probe.dat"), p.tsteps)
+    es = rd.read_slices(os.path.join(d, "output_E.dat"), p, True)
+    return (np.concatenate([ntf[k].ravel() for k, _ in rd.NTF_FACE_ORDER]),
+            np.concatenate([pr[k].ravel() for k in ("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")]),
+            np.concatenate([r[k].ravel() for r in es for k in ("z", "y", "x")]))
+
+
+def test_plain_trail_matches_oracle(built, tmp_path):
+    """Parametric trail evaluated on the device (CUDA exp/pow) against the
+    oracle's host evaluation: FP64 fields and sums within 1e-12 relative L2;
+    every integer (file sizes, record count, probe indices) identical."""
+    case = golden_cases.trail_case()
+    p = case[0]
+    da, db = os.path.join(str(tmp_path), "gpu"), os.path.join(str(tmp_path), "orc")
+    golden_cases.write_trail_case(da, case)
+    golden_cases.write_trail_case(db, case)
+    E.run_rundir(da)
+    H.run_oracle(db)
+    for name in H.OUTPUTS:
+        assert os.path.getsize(os.path.join(da, name)) == os.path.getsize(os.path.join(db, name))
+    for ga, gb in zip(_groups(da, p), _groups(db, p)):
+        assert np.abs(gb).max() > 0 and H.rel_l2(ga, gb) < 1e-12
+
+
+def test_fp32_trail_close_to_plain(built, tmp_path):
+    case = golden_cases.trail_case()
+    p = case[0]
+    d = os.path.join(str(tmp_path), "r")
+    golden_cases.write_trail_case(d, case)
+    a, b = _sim(d, E.FORM_FP64_PLAIN).read_ntf(), _sim(d, E.FORM_FP32_FUSED).read_ntf()
+    assert H.rel_l2(_faces(b, p), _faces(a, p)) < 1e-3
