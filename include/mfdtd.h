@@ -180,7 +180,7 @@ int mfdtd_problem_footprint(const mfdtd_problem *pb, int32_t form, int64_t *byte
 
 /* ---- simulation (device) -------------------------------------------------- */
 int mfdtd_sim_create(const mfdtd_problem *pb, const mfdtd_run_opts *opts, mfdtd_sim **out);
-void mfdtd_sim_destroy(mfdtd_sim *s);
+void mfdtd_sim_destroy(mfdtd_sim *s);  /* leaves its batch first, if any */
 /* Advance `nsteps` time steps (source/meteor-2.1.cpp:652-1574 per step).
  * Record-step side effects (max|Ex| log line, slice records) are kept in the
  * handle when `collect_records` is nonzero. Asynchronous unless a record step
@@ -245,6 +245,34 @@ int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t Nx, int32_t 
  * MFDTD_EINVAL when `which` is past the last class. */
 int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t name_len,
                            double *avg_ms, int64_t *launches);
+
+/* ---- batches (chosen form: many trails in one persistent kernel) ----------
+ * No counterpart in the reference, which runs one trail per process and fans
+ * trails out as separate PBS jobs (setup/meteorbatch.m, setup/writepbsfile.m).
+ * A batch advances up to mfdtd_batch_capacity() FP32 simulations together:
+ * each time step is one launch of a persistent kernel whose CTAs pull
+ * (simulation, tile, x-slab) work items from a device queue, boundary tiles
+ * first; two steps are replayed as one CUDA graph.  Members keep their fields
+ * on the device; a member past its step count idles until removed.  Members
+ * join at step 0, must share the batch's device and current update (Young DI,
+ * uniform Lee-Kalluri or tabulated Lee-Kalluri), and cannot be advanced on
+ * their own while in a batch.  Read a member's results only after
+ * mfdtd_batch_sync. */
+typedef struct mfdtd_batch mfdtd_batch;
+int mfdtd_batch_capacity(void);
+int mfdtd_batch_create(int32_t device, mfdtd_batch **out);
+void mfdtd_batch_destroy(mfdtd_batch *b);  /* members stay valid */
+int mfdtd_batch_add(mfdtd_batch *b, mfdtd_sim *s);
+int mfdtd_batch_remove(mfdtd_batch *b, mfdtd_sim *s);
+/* Enqueue nsteps time steps of every member (asynchronous). */
+int mfdtd_batch_run(mfdtd_batch *b, int32_t nsteps);
+/* Wait for the batch; updates every member's step index. */
+int mfdtd_batch_sync(mfdtd_batch *b);
+/* Autotuner: time every (slab depth, CTAs per SM) pair on the live members
+ * (they advance while being timed) and keep the fastest; best_* may be NULL. */
+int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depths,
+                     const int32_t *ctas_per_sm, int32_t n_ctas, int32_t *best_depth,
+                     int32_t *best_ctas);
 
 /* ---- errors ---------------------------------------------------------------- */
 /* Copy the last error message of the calling thread into buf (NUL-terminated). */

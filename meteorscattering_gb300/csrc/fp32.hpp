@@ -5,6 +5,8 @@
 
 namespace mfdtd {
 
+class Fp32Batch;
+
 class Fp32Sim {
 public:
     static int64_t footprint(const Problem &P);
@@ -28,11 +30,44 @@ public:
     double *const *ntf_arrays() const;
     ~Fp32Sim();
 
-private:
     struct Impl;
+    Impl *impl() const { return impl_; }
+
+private:
+    friend class Fp32Batch;
     Impl *impl_ = nullptr;
     int64_t bytes_ = 0;
     int m_cur_ = 0;  // which ping-pong set holds the current E/H state
+};
+
+// Many FP32 simulations advanced together, one persistent-kernel launch per
+// time step, two steps replayed as one CUDA graph (fp32_fused.cu).
+class Fp32Batch {
+public:
+    explicit Fp32Batch(int device);
+    ~Fp32Batch();
+    static int capacity();
+    // Join at step 0; returns the slot.  Throws when full or when the current
+    // update differs from the batch's.
+    int add(Fp32Sim *sim, int t0);
+    void remove(Fp32Sim *sim);
+    // Advance every member `nticks` steps (members at their step count idle);
+    // returns kernel launches enqueued.  Asynchronous on stream().
+    int run(int nticks);
+    void sync();
+    int steps_done(const Fp32Sim *sim) const;
+    // Try every (slab depth, CTAs per SM) pair on the live batch and keep the
+    // fastest; returns the steps spent.
+    int tune(const int *chunks, int nchunks, const int *ctas, int nctas);
+    int tuned_chunk() const;
+    int tuned_ctas() const;
+    long long tick() const;
+    void *stream() const;
+    int impl_device() const;
+    struct Impl;
+
+private:
+    Impl *impl_;
 };
 
 }  // namespace mfdtd

@@ -54,6 +54,19 @@ struct Maps {
     CUtensorMap E[2][3], H[2][3], J[3];
 };
 
+// CPML and auxiliary-line coefficient tables of one simulation, in global
+// memory (read on the boundary path only), so that Args stays small enough
+// for a batch of simulations to keep their Args in the constant bank.
+struct Tables {
+    float Bh[2 * kMaxPml], Ahx[2 * kMaxPml], Ahy[2 * kMaxPml], Ahz[2 * kMaxPml];
+    float Be[2 * kMaxPml], Aex[2 * kMaxPml], Aey[2 * kMaxPml], Aez[2 * kMaxPml];
+    // kappa != 1 derivative terms (1/kappa - 1)/d per slab index
+    float Khx[2 * kMaxPml], Khy[2 * kMaxPml], Khz[2 * kMaxPml];
+    float Kex[2 * kMaxPml], Key[2 * kMaxPml], Kez[2 * kMaxPml];
+    // auxiliary-line CPML (oblique incidence), A pre-divided by the line cell
+    float Bh1[2 * kMaxPml], Ah1[2 * kMaxPml], Be1[2 * kMaxPml], Ae1[2 * kMaxPml];
+};
+
 struct Args {
     int Nx, Ny, Nz, Nzp, L, xshift, yshift, zshift;
     int bx1, bx2, by1, by2, bz1, bz2, ntfb, nntf, ssx, ssy, ssz;
@@ -65,17 +78,12 @@ struct Args {
     float c1s, c2s, csx, csy, csz;           // sphere (doplate == 2)
     float dtf, c0di;                         // dt, 2*E0*dt
     double platesize;
-    float Bh[2 * kMaxPml], Ahx[2 * kMaxPml], Ahy[2 * kMaxPml], Ahz[2 * kMaxPml];
-    float Be[2 * kMaxPml], Aex[2 * kMaxPml], Aey[2 * kMaxPml], Aez[2 * kMaxPml];
+    const Tables *tb;    // CPML / line tables (global memory)
     float lku[18];       // Lee-Kalluri matrices when nu is uniform over the grid
-    // extended inputs: kappa != 1 derivative terms (1/kappa - 1)/d per slab index
-    int kappa_on;
-    float Khx[2 * kMaxPml], Khy[2 * kMaxPml], Khz[2 * kMaxPml];
-    float Kex[2 * kMaxPml], Key[2 * kMaxPml], Kez[2 * kMaxPml];
+    int kappa_on;        // kappa != 1: the CPML corrections carry the 1/kappa term
     // oblique incidence: auxiliary line (E in inc[][1], H in inc[][2])
     int oblique, M, ashift, lk_colocated;
     float kr[3], s0, ke[3], kh[3], chl, cel;   // chl = c2h/dl, cel = c2e0/dl
-    float Bh1[2 * kMaxPml], Ah1[2 * kMaxPml], Be1[2 * kMaxPml], Ae1[2 * kMaxPml];  // A/dl
     // state
     float *E[2][3], *H[2][3], *J[3];
     float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
@@ -327,18 +335,18 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                 const int sy = hslab(j, Ny, L, a.yshift);
                 if (sy >= 0) {
                     const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                    const float p = a.Bh[sy] * a.Ph[PAR][0][o2] + a.Ahy[sy] * dEz;
+                    const float p = a.tb->Bh[sy] * a.Ph[PAR][0][o2] + a.tb->Ahy[sy] * dEz;
                     if (store_psi) a.Ph[PAR ^ 1][0][o2] = p;
                     h -= a.c2h * p;
-                    if (a.kappa_on) h -= a.c2h * (a.Khy[sy] * dEz);
+                    if (a.kappa_on) h -= a.c2h * (a.tb->Khy[sy] * dEz);
                 }
                 const int sz = hslab(k, Nz, L, a.zshift);
                 if (sz >= 0) {
                     const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                    const float p = a.Bh[sz] * a.Ph[PAR][1][o2] + a.Ahz[sz] * dEy;
+                    const float p = a.tb->Bh[sz] * a.Ph[PAR][1][o2] + a.tb->Ahz[sz] * dEy;
                     if (store_psi) a.Ph[PAR ^ 1][1][o2] = p;
                     h += a.c2h * p;
-                    if (a.kappa_on) h += a.c2h * (a.Khz[sz] * dEy);
+                    if (a.kappa_on) h += a.c2h * (a.tb->Khz[sz] * dEy);
                 }
             }
         }
@@ -358,19 +366,19 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-            const float p = a.Bh[sx] * (use_pf ? pf_yx : a.Ph[PAR][2][o2]) + a.Ahx[sx] * dEz;
+            const float p = a.tb->Bh[sx] * (use_pf ? pf_yx : a.Ph[PAR][2][o2]) + a.tb->Ahx[sx] * dEz;
             if (store_psi) a.Ph[PAR ^ 1][2][o2] = p;
             h += a.c2h * p;
-            if (a.kappa_on) h += a.c2h * (a.Khx[sx] * dEz);
+            if (a.kappa_on) h += a.c2h * (a.tb->Khx[sx] * dEz);
         }
         if (!CLEAN && a.dopml) {
             const int sz = hslab(k, Nz, L, a.zshift);
             if (sz >= 0) {
                 const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                const float p = a.Bh[sz] * a.Ph[PAR][3][o2] + a.Ahz[sz] * dEx;
+                const float p = a.tb->Bh[sz] * a.Ph[PAR][3][o2] + a.tb->Ahz[sz] * dEx;
                 if (store_psi) a.Ph[PAR ^ 1][3][o2] = p;
                 h -= a.c2h * p;
-                if (a.kappa_on) h -= a.c2h * (a.Khz[sz] * dEx);
+                if (a.kappa_on) h -= a.c2h * (a.tb->Khz[sz] * dEx);
             }
         }
         o.y = h;
@@ -389,19 +397,19 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-            const float p = a.Bh[sx] * (use_pf ? pf_zx : a.Ph[PAR][4][o2]) + a.Ahx[sx] * dEy;
+            const float p = a.tb->Bh[sx] * (use_pf ? pf_zx : a.Ph[PAR][4][o2]) + a.tb->Ahx[sx] * dEy;
             if (store_psi) a.Ph[PAR ^ 1][4][o2] = p;
             h -= a.c2h * p;
-            if (a.kappa_on) h -= a.c2h * (a.Khx[sx] * dEy);
+            if (a.kappa_on) h -= a.c2h * (a.tb->Khx[sx] * dEy);
         }
         if (!CLEAN && a.dopml) {
             const int sy = hslab(j, Ny, L, a.yshift);
             if (sy >= 0) {
                 const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                const float p = a.Bh[sy] * a.Ph[PAR][5][o2] + a.Ahy[sy] * dEx;
+                const float p = a.tb->Bh[sy] * a.Ph[PAR][5][o2] + a.tb->Ahy[sy] * dEx;
                 if (store_psi) a.Ph[PAR ^ 1][5][o2] = p;
                 h += a.c2h * p;
-                if (a.kappa_on) h += a.c2h * (a.Khy[sy] * dEx);
+                if (a.kappa_on) h += a.c2h * (a.tb->Khy[sy] * dEx);
             }
         }
         o.z = h;
@@ -437,7 +445,7 @@ __device__ void line_update(const Args &a, int t) {
                 v = a.c1h * h[n] - a.chl * (e[n + 1] - e[n]);
                 if (n >= M - L - 1) {
                     const int s = n - a.ashift;
-                    const float p = a.Bh1[s] * a.incP[PAR][2][s] + a.Ah1[s] * (e[n + 1] - e[n]);
+                    const float p = a.tb->Bh1[s] * a.incP[PAR][2][s] + a.tb->Ah1[s] * (e[n + 1] - e[n]);
                     a.incP[PAR ^ 1][2][s] = p;
                     v -= a.c2h * p;
                 }
@@ -451,7 +459,7 @@ __device__ void line_update(const Args &a, int t) {
                 v = a.c1e0 * e[n] - a.cel * (h2[n] - h2[n - 1]);
                 if (n >= M - L - 1) {
                     const int s = n - a.ashift;
-                    const float p = a.Be1[s] * a.incP[PAR][1][s] + a.Ae1[s] * (h2[n] - h2[n - 1]);
+                    const float p = a.tb->Be1[s] * a.incP[PAR][1][s] + a.tb->Ae1[s] * (h2[n] - h2[n - 1]);
                     a.incP[PAR ^ 1][1][s] = p;
                     v -= a.c2e0 * p;
                 }
@@ -472,8 +480,8 @@ __device__ void line_update(const Args &a, int t) {
             vz = a.c1h * hz[i] - a.chx * (ey[i + 1] - ey[i]);
             if (a.dopml && i >= Nx - L - 1) {
                 const int s = i - a.xshift;
-                const float py = a.Bh[s] * a.incP[PAR][2][s] + a.Ahx[s] * (ez[i + 1] - ez[i]);
-                const float pz = a.Bh[s] * a.incP[PAR][3][s] + a.Ahx[s] * (ey[i + 1] - ey[i]);
+                const float py = a.tb->Bh[s] * a.incP[PAR][2][s] + a.tb->Ahx[s] * (ez[i + 1] - ez[i]);
+                const float pz = a.tb->Bh[s] * a.incP[PAR][3][s] + a.tb->Ahx[s] * (ey[i + 1] - ey[i]);
                 a.incP[PAR ^ 1][2][s] = py;
                 a.incP[PAR ^ 1][3][s] = pz;
                 vy += a.c2h * py;
@@ -491,8 +499,8 @@ __device__ void line_update(const Args &a, int t) {
             vz = a.c1e0 * ez[i] + a.cex * (hy2[i] - hy2[i - 1]);
             if (a.dopml && i >= Nx - L - 1) {
                 const int s = i - a.xshift;
-                const float py = a.Be[s] * a.incP[PAR][0][s] + a.Aex[s] * (hz2[i] - hz2[i - 1]);
-                const float pz = a.Be[s] * a.incP[PAR][1][s] + a.Aex[s] * (hy2[i] - hy2[i - 1]);
+                const float py = a.tb->Be[s] * a.incP[PAR][0][s] + a.tb->Aex[s] * (hz2[i] - hz2[i - 1]);
+                const float pz = a.tb->Be[s] * a.incP[PAR][1][s] + a.tb->Aex[s] * (hy2[i] - hy2[i - 1]);
                 a.incP[PAR ^ 1][0][s] = py;
                 a.incP[PAR ^ 1][1][s] = pz;
                 vy -= a.c2e0 * py;
@@ -811,18 +819,18 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         const int sy = eslab(j, Ny, L, a.yshift);
                         if (sy >= 0) {
                             const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                            const float p = a.Be[sy] * a.Pe[0][o2] + a.Aey[sy] * dHz;
+                            const float p = a.tb->Be[sy] * a.Pe[0][o2] + a.tb->Aey[sy] * dHz;
                             a.Pe[0][o2] = p;
                             e += a.c2e0 * p;
-                            if (a.kappa_on) e += a.c2e0 * (a.Key[sy] * dHz);
+                            if (a.kappa_on) e += a.c2e0 * (a.tb->Key[sy] * dHz);
                         }
                         const int sz = eslab(k, Nz, L, a.zshift);
                         if (sz >= 0) {
                             const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                            const float p = a.Be[sz] * a.Pe[1][o2] + a.Aez[sz] * dHy;
+                            const float p = a.tb->Be[sz] * a.Pe[1][o2] + a.tb->Aez[sz] * dHy;
                             a.Pe[1][o2] = p;
                             e -= a.c2e0 * p;
-                            if (a.kappa_on) e -= a.c2e0 * (a.Kez[sz] * dHy);
+                            if (a.kappa_on) e -= a.c2e0 * (a.tb->Kez[sz] * dHy);
                         }
                     }
                 }
@@ -845,11 +853,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                     float p = 0.f;
                     if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
                         const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
-                        p = a.Be[sxe] * ceyx + a.Aex[sxe] * dHz;
+                        p = a.tb->Be[sxe] * ceyx + a.tb->Aex[sxe] * dHz;
                         a.Pe[2][o2] = p;
                     }
                     e -= a.c2e0 * p;
-                    if (a.kappa_on) e -= a.c2e0 * (a.Kex[sxe] * dHz);
+                    if (a.kappa_on) e -= a.c2e0 * (a.tb->Kex[sxe] * dHz);
                 }
                 if (!CLEAN && a.dopml) {
                     const int sz = eslab(k, Nz, L, a.zshift);
@@ -857,11 +865,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         float p = 0.f;
                         if (j < Ny - 1) {
                             const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                            p = a.Be[sz] * a.Pe[3][o2] + a.Aez[sz] * dHx;
+                            p = a.tb->Be[sz] * a.Pe[3][o2] + a.tb->Aez[sz] * dHx;
                             a.Pe[3][o2] = p;
                         }
                         e += a.c2e0 * p;
-                        if (a.kappa_on) e += a.c2e0 * (a.Kez[sz] * dHx);
+                        if (a.kappa_on) e += a.c2e0 * (a.tb->Kez[sz] * dHx);
                     }
                 }
                 ey = e;
@@ -890,20 +898,20 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                     float p = 0.f;
                     if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
                         const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
-                        p = a.Be[sxe] * cezx + a.Aex[sxe] * dHy;
+                        p = a.tb->Be[sxe] * cezx + a.tb->Aex[sxe] * dHy;
                         a.Pe[4][o2] = p;
                     }
                     e += a.c2e0 * p;
-                    if (a.kappa_on) e += a.c2e0 * (a.Kex[sxe] * dHy);
+                    if (a.kappa_on) e += a.c2e0 * (a.tb->Kex[sxe] * dHy);
                 }
                 if (!CLEAN && a.dopml) {
                     const int sy = eslab(j, Ny, L, a.yshift);
                     if (sy >= 0 && k < Nz - 1) {
                         const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                        const float p = a.Be[sy] * a.Pe[5][o2] + a.Aey[sy] * dHx;
+                        const float p = a.tb->Be[sy] * a.Pe[5][o2] + a.tb->Aey[sy] * dHx;
                         a.Pe[5][o2] = p;
                         e -= a.c2e0 * p;
-                        if (a.kappa_on) e -= a.c2e0 * (a.Key[sy] * dHx);
+                        if (a.kappa_on) e -= a.c2e0 * (a.tb->Key[sy] * dHx);
                     }
                 }
                 ez = e;
@@ -987,10 +995,16 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 }
 
 // ---------------------------------------------------------------------------
+// One work item: tile `tile_id` of simulation `a` over x-chunk `chunk` (planes
+// chunk*a.chunk .. +a.chunk).  The item with `first` set also advances the
+// incident line and records the probes of the previous step.  `inited` says
+// whether the CTA's stage mbarriers hold an earlier item's objects (they are
+// invalidated and re-initialised).  Returns false when a bounded wait ran out
+// (the simulation's error flag is then set).
 template <int PAR, int JM>
-__global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
-    k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
+__device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int tile_id, int chunk,
+                                         bool first, int t, int record, unsigned char *smem_raw,
+                                         bool inited) {
     MarchCtx c;
     // TMA destinations must be 128-byte aligned; the launch reserves 128 spare bytes.
     c.smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
@@ -1001,24 +1015,19 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
     c.warp = c.tid >> 5;
     c.lane = c.tid & 31;
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
-    // Boundary tiles (general path, about 3x the work of an interior tile) are
-    // launched first so that they overlap the bulk of the grid instead of
-    // forming a tail.
-    const int tile_id = a.tile_order[blockIdx.x];
     c.k0 = (tile_id % a.ntk) * TK;
     c.j0 = (tile_id / a.ntk) * TJ;
-    c.i_begin = blockIdx.z * a.chunk;
+    c.i_begin = chunk * a.chunk;
     c.i_end = min(Nx, c.i_begin + a.chunk);
-    if (c.i_begin >= Nx) return;
+    if (c.i_begin >= Nx) return true;
     c.p0 = max(c.i_begin - 1, 0);
     c.q_last = min(c.i_end, Nx - 1);  // last plane loaded
     const size_t plane = (size_t)Ny * a.Nzp;
 
-    const bool first_cta = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
-    if (first_cta) line_update<PAR>(a, t);
+    if (first) line_update<PAR>(a, t);
 
     // Probes of the previous step from the read set (source/meteor-2.1.cpp:1443-1455).
-    if (first_cta && t > 0 && c.warp == 9 && c.lane >= 8 && c.lane - 8 < a.nprobes) {
+    if (first && t > 0 && c.warp == 9 && c.lane >= 8 && c.lane - 8 < a.nprobes) {
         const int pidx = c.lane - 8;
         const int ix = a.probe_ijk[3 * pidx], iy = a.probe_ijk[3 * pidx + 1], iz = a.probe_ijk[3 * pidx + 2];
         const size_t sI = plane, sJ = a.Nzp;
@@ -1035,6 +1044,11 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
     }
 
     if (c.tid == PROD) {
+        // An earlier item's barriers have no pending operation (every stage it
+        // issued was waited for), so they can be invalidated and reused.
+        if (inited)
+            for (int s = 0; s < NS; s++)
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&c.bar[s])) : "memory");
         for (int s = 0; s < NS; s++) mbar_init(&c.bar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -1072,13 +1086,72 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
             }
         }
     }
+    return fail_q < 0;
+}
+
+// One time step of one simulation: one CTA per (tile, x-chunk).  Boundary
+// tiles (general path, several times the work of an interior tile) are
+// launched first so that they overlap the bulk of the grid instead of forming
+// a tail.
+template <int PAR, int JM>
+__global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
+    k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const bool first = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
+    run_item<PAR, JM>(maps, a, a.tile_order[blockIdx.x], blockIdx.z, first, t, record, smem_raw, false);
+}
+
+// ---------------------------------------------------------------------------
+// Batched form: many simulations advance one time step per launch.  Their Args
+// sit in constant-bank slots, their TMA descriptors in global memory.  A
+// persistent grid (a few CTAs per SM) pulls work items -- (simulation, tile,
+// x-chunk) -- from a device queue until it is empty; items of boundary tiles
+// come first.  A simulation past its step count keeps its slot but gets no
+// work.  k_batch_advance then moves every simulation to its next step and
+// resets the queue, so K steps replay as one CUDA graph.
+constexpr int kMaxBatch = 56;  // 56 x 1080-byte Args in the 64 KB constant bank
+__constant__ Args c_jobs[kMaxBatch];
+
+struct BatchItem {
+    int job, tile, chunk, first;
+};
+
+template <int PAR, int JM>
+__global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
+    k_fp32_batch(const BatchItem *__restrict__ items, const int *__restrict__ n_items, int *next,
+                 const Maps *__restrict__ maps, const int *__restrict__ job_t,
+                 const int *__restrict__ job_end) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    __shared__ int s_item;
+    bool inited = false;
+    const int n = *n_items;
+    for (;;) {
+        __syncthreads();  // everyone has read s_item of the previous round
+        if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= n) break;
+        const BatchItem w = items[it];
+        const int t = job_t[w.job];
+        if (t >= job_end[w.job]) continue;
+        if (!run_item<PAR, JM>(maps[w.job], c_jobs[w.job], w.tile, w.chunk, w.first != 0, t, 0, smem_raw,
+                               inited))
+            break;
+        inited = true;
+    }
+}
+
+__global__ void k_batch_advance(int *job_t, const int *job_end, int njobs, int *next) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < njobs && job_t[j] < job_end[j]) job_t[j] += 1;
+    if (j == 0) *next = 0;
 }
 
 // E probes of the final step (the per-step ones ride in the next pass).
-__global__ void k_fp32_flush(const Args a, int t_last) {
+__global__ void k_fp32_flush(const Args a, int t_last, int par) {
     const int p = threadIdx.x;
     if (p >= a.nprobes) return;
-    const int par = (t_last + 1) & 1;  // set written by the last pass
+    // `par`: the set written by the last pass
     const size_t sI = (size_t)a.Ny * a.Nzp, sJ = a.Nzp;
     const int ix = a.probe_ijk[3 * p], iy = a.probe_ijk[3 * p + 1], iz = a.probe_ijk[3 * p + 2];
     const size_t c = ix * sI + iy * sJ + iz;
@@ -1200,6 +1273,8 @@ struct Fp32Sim::Impl {
     size_t dtmp_len = 0;
     unsigned int *scan = nullptr;  // [0] max|Ex| bits, [1] bad flag
     int jm = 0;  // J method of the kernel variant
+    std::vector<int> tile_order;   // host copy: boundary tiles first
+    int n_boundary = 0;            // how many of them are boundary tiles
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
         void *p = nullptr;
@@ -1261,6 +1336,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     a.kappa_on = P.kappa_on;
     a.oblique = P.oblique;
     a.lk_colocated = P.ext.lk_colocated;
+    Tables T;
+    std::memset(&T, 0, sizeof T);
     if (P.oblique) {
         a.M = P.M; a.ashift = P.ashift; a.s0 = (float)P.s0;
         for (int q = 0; q < 3; q++) {
@@ -1268,17 +1345,22 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         }
         a.chl = (float)(P.c2h / P.dl); a.cel = (float)(P.c2e0 / P.dl);
         for (int q = 0; q < 2 * P.L; q++) {
-            a.Bh1[q] = (float)P.Bh1[q]; a.Ah1[q] = (float)(P.Ah1[q] / P.dl);
-            a.Be1[q] = (float)P.Be1[q]; a.Ae1[q] = (float)(P.Ae1[q] / P.dl);
+            T.Bh1[q] = (float)P.Bh1[q]; T.Ah1[q] = (float)(P.Ah1[q] / P.dl);
+            T.Be1[q] = (float)P.Be1[q]; T.Ae1[q] = (float)(P.Ae1[q] / P.dl);
         }
     }
     for (int q = 0; q < 2 * P.L; q++) {
-        a.Khx[q] = (float)(P.Kh[q] / P.dx); a.Khy[q] = (float)(P.Kh[q] / P.dy); a.Khz[q] = (float)(P.Kh[q] / P.dz);
-        a.Kex[q] = (float)(P.Ke[q] / P.dx); a.Key[q] = (float)(P.Ke[q] / P.dy); a.Kez[q] = (float)(P.Ke[q] / P.dz);
-        a.Bh[q] = (float)P.Bh[q];
-        a.Ahx[q] = (float)(P.Ah[q] / P.dx); a.Ahy[q] = (float)(P.Ah[q] / P.dy); a.Ahz[q] = (float)(P.Ah[q] / P.dz);
-        a.Be[q] = (float)P.Be[q];
-        a.Aex[q] = (float)(P.Ae[q] / P.dx); a.Aey[q] = (float)(P.Ae[q] / P.dy); a.Aez[q] = (float)(P.Ae[q] / P.dz);
+        T.Khx[q] = (float)(P.Kh[q] / P.dx); T.Khy[q] = (float)(P.Kh[q] / P.dy); T.Khz[q] = (float)(P.Kh[q] / P.dz);
+        T.Kex[q] = (float)(P.Ke[q] / P.dx); T.Key[q] = (float)(P.Ke[q] / P.dy); T.Kez[q] = (float)(P.Ke[q] / P.dz);
+        T.Bh[q] = (float)P.Bh[q];
+        T.Ahx[q] = (float)(P.Ah[q] / P.dx); T.Ahy[q] = (float)(P.Ah[q] / P.dy); T.Ahz[q] = (float)(P.Ah[q] / P.dz);
+        T.Be[q] = (float)P.Be[q];
+        T.Aex[q] = (float)(P.Ae[q] / P.dx); T.Aey[q] = (float)(P.Ae[q] / P.dy); T.Aez[q] = (float)(P.Ae[q] / P.dz);
+    }
+    {
+        Tables *d = m.alloc<Tables>(1, s);
+        ck(cudaMemcpyAsync(d, &T, sizeof T, cudaMemcpyHostToDevice, s), "H2D");
+        a.tb = d;
     }
     const size_t NC = (size_t)P.Nx * P.Ny * m.Nzp;
     for (int b = 0; b < 2; b++)
@@ -1402,7 +1484,9 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                 for (int q = 0; q < 6; q++) cl = cl && !hits(jlo, jhi, sy[q]) && !hits(klo, khi, sz[q]);
                 (cl ? later : order).push_back(ty * ntk + tk);
             }
+        m.n_boundary = (int)order.size();
         order.insert(order.end(), later.begin(), later.end());
+        m.tile_order = order;
         a.tile_order = m.upload(order, s);
         a.ntk = ntk;
     }
@@ -1418,7 +1502,8 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     if (ev) cudaEventRecord((cudaEvent_t)ev[0], s);
     const int rec = record ? 1 : 0;
     auto go = [&](auto kern) { kern<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t, rec); };
-    if ((t & 1) == 0) {
+    // The pass reads the set holding the current state and writes the other.
+    if (m_cur_ == 0) {
         if (m.jm == 0) go(k_fp32_step<0, 0>);
         else if (m.jm == 1) go(k_fp32_step<0, 1>);
         else go(k_fp32_step<0, 2>);
@@ -1428,7 +1513,7 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
         else go(k_fp32_step<1, 2>);
     }
     if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
-    m_cur_ = (t + 1) & 1;
+    m_cur_ ^= 1;
     return 1;
 }
 
@@ -1487,7 +1572,7 @@ double Fp32Sim::guard(void *stream) {
 void Fp32Sim::flush(int t_last, void *stream) {
     Impl &m = *impl_;
     if (m.nprobes <= 0) return;
-    k_fp32_flush<<<1, 32, 0, (cudaStream_t)stream>>>(m.a, t_last);
+    k_fp32_flush<<<1, 32, 0, (cudaStream_t)stream>>>(m.a, t_last, m_cur_);
 }
 
 void Fp32Sim::read_ntf(int q, double *out, void *stream) {
@@ -1517,6 +1602,273 @@ void Fp32Sim::read_field(int comp, double *out, void *stream) {
 }
 
 double *const *Fp32Sim::ntf_arrays() const { return impl_->a.ntf; }
+
+// ---------------------------------------------------------------------------
+// Batch of FP32 simulations advanced by the persistent kernel.
+
+struct Fp32Batch::Impl {
+    int device = 0, sms = 148, jm = -1;
+    cudaStream_t stream = nullptr;
+    Fp32Sim *slot[kMaxBatch] = {};
+    int tsteps[kMaxBatch] = {};
+    int host_t[kMaxBatch] = {};     // steps done, mirrored on the host
+    BatchItem *items = nullptr;
+    int item_cap = 0, n_items = 0;
+    int *d_n = nullptr, *d_next = nullptr, *d_t = nullptr, *d_end = nullptr;
+    Maps *d_maps = nullptr;
+    long long tick = 0;             // global step counter: parity of every slot's pass
+    bool dirty = true;
+    int chunk = 0;                  // planes per item (0: per-simulation default)
+    int ctas_per_sm = 3;
+    cudaGraphExec_t graph = nullptr;
+    int graph_ctas = 0;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<std::pair<int, double>> tune_log;  // (chunk * 16 + ctas, ms per tick)
+
+    ~Impl() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph) cudaGraphExecDestroy(graph);
+        cudaFree(items); cudaFree(d_n); cudaFree(d_next); cudaFree(d_t); cudaFree(d_end); cudaFree(d_maps);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+int Fp32Batch::capacity() { return kMaxBatch; }
+
+Fp32Batch::Fp32Batch(int device) : impl_(new Impl()) {
+    Impl &b = *impl_;
+    b.device = device;
+    ck(cudaSetDevice(device), "cudaSetDevice");
+    cudaDeviceGetAttribute(&b.sms, cudaDevAttrMultiProcessorCount, device);
+    ck(cudaStreamCreateWithFlags(&b.stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    ck(cudaMalloc(&b.d_n, 4), "cudaMalloc");
+    ck(cudaMalloc(&b.d_next, 4), "cudaMalloc");
+    ck(cudaMalloc(&b.d_t, 4 * kMaxBatch), "cudaMalloc");
+    ck(cudaMalloc(&b.d_end, 4 * kMaxBatch), "cudaMalloc");
+    ck(cudaMalloc(&b.d_maps, sizeof(Maps) * kMaxBatch), "cudaMalloc");
+    ck(cudaMemsetAsync(b.d_n, 0, 4, b.stream), "memset");
+    ck(cudaMemsetAsync(b.d_next, 0, 4, b.stream), "memset");
+    ck(cudaMemsetAsync(b.d_t, 0, 4 * kMaxBatch, b.stream), "memset");
+    ck(cudaMemsetAsync(b.d_end, 0, 4 * kMaxBatch, b.stream), "memset");
+    ck(cudaEventCreate(&b.e0), "event");
+    ck(cudaEventCreate(&b.e1), "event");
+    for (int jm = 0; jm < 3; jm++) {
+        auto attr = [](const void *f) {
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+        };
+        if (jm == 0) { attr((const void *)k_fp32_batch<0, 0>); attr((const void *)k_fp32_batch<1, 0>); }
+        if (jm == 1) { attr((const void *)k_fp32_batch<0, 1>); attr((const void *)k_fp32_batch<1, 1>); }
+        if (jm == 2) { attr((const void *)k_fp32_batch<0, 2>); attr((const void *)k_fp32_batch<1, 2>); }
+    }
+    ck(cudaStreamSynchronize(b.stream), "batch set-up");
+}
+
+Fp32Batch::~Fp32Batch() { delete impl_; }
+
+void *Fp32Batch::stream() const { return impl_->stream; }
+
+int Fp32Batch::add(Fp32Sim *sim, int t0) {
+    Impl &b = *impl_;
+    Fp32Sim::Impl &m = *sim->impl_;
+    if (t0 != 0) throw Error(MFDTD_ESTATE, "batch: a simulation joins at step 0");
+    if (b.jm >= 0 && m.jm != b.jm)
+        throw Error(MFDTD_EINVAL, "batch: every simulation of a batch uses the same current update "
+                                  "(Young DI, uniform Lee-Kalluri, or tabulated Lee-Kalluri)");
+    int s = -1;
+    for (int q = 0; q < kMaxBatch; q++)
+        if (!b.slot[q]) { s = q; break; }
+    if (s < 0) throw Error(MFDTD_ENOMEM, "batch: all " + std::to_string(kMaxBatch) + " slots in use");
+    ck(cudaStreamSynchronize(b.stream), "batch");
+    // The state is all zeros in both sets, so the simulation can take the
+    // parity of the current tick.
+    sim->m_cur_ = (int)(b.tick & 1);
+    ck(cudaMemcpyToSymbolAsync(c_jobs, &m.a, sizeof(Args), sizeof(Args) * s, cudaMemcpyHostToDevice, b.stream),
+       "cudaMemcpyToSymbol");
+    ck(cudaMemcpyAsync(b.d_maps + s, &m.maps, sizeof(Maps), cudaMemcpyHostToDevice, b.stream), "H2D");
+    int zero = 0, end = m.tsteps;
+    ck(cudaMemcpyAsync(b.d_t + s, &zero, 4, cudaMemcpyHostToDevice, b.stream), "H2D");
+    ck(cudaMemcpyAsync(b.d_end + s, &end, 4, cudaMemcpyHostToDevice, b.stream), "H2D");
+    ck(cudaStreamSynchronize(b.stream), "batch add");
+    b.slot[s] = sim;
+    b.tsteps[s] = m.tsteps;
+    b.host_t[s] = 0;
+    b.jm = m.jm;
+    b.dirty = true;
+    return s;
+}
+
+void Fp32Batch::remove(Fp32Sim *sim) {
+    Impl &b = *impl_;
+    for (int q = 0; q < kMaxBatch; q++)
+        if (b.slot[q] == sim) {
+            ck(cudaStreamSynchronize(b.stream), "batch");
+            int zero = 0;
+            ck(cudaMemcpy(b.d_end + q, &zero, 4, cudaMemcpyHostToDevice), "H2D");
+            b.slot[q] = nullptr;
+            b.dirty = true;
+        }
+    bool any = false;
+    for (int q = 0; q < kMaxBatch; q++) any |= b.slot[q] != nullptr;
+    if (!any) b.jm = -1;
+}
+
+int Fp32Batch::steps_done(const Fp32Sim *sim) const {
+    for (int q = 0; q < kMaxBatch; q++)
+        if (impl_->slot[q] == sim) return impl_->host_t[q];
+    return -1;
+}
+
+// Work items of every simulation still short of its step count: boundary
+// tiles of all simulations first (their general path is the slow one), then
+// interior tiles, each split into x-chunks (the slab depth).
+static void build_items(Fp32Batch::Impl &b) {
+    std::vector<BatchItem> first, rest;
+    for (int q = 0; q < kMaxBatch; q++) {
+        Fp32Sim *sim = b.slot[q];
+        if (!sim || b.host_t[q] >= b.tsteps[q]) continue;
+        Fp32Sim::Impl &m = *sim->impl();
+        const int chunk = b.chunk > 0 ? b.chunk : m.a.chunk;
+        const int nch = (m.Nx + chunk - 1) / chunk;
+        for (size_t ti = 0; ti < m.tile_order.size(); ti++)
+            for (int c = 0; c < nch; c++) {
+                BatchItem w{q, m.tile_order[ti], c, ti == 0 && c == 0};
+                ((int)ti < m.n_boundary ? first : rest).push_back(w);
+            }
+    }
+    first.insert(first.end(), rest.begin(), rest.end());
+    if ((int)first.size() > b.item_cap) {
+        cudaFree(b.items);
+        b.item_cap = (int)first.size() * 2 + 1024;
+        ck(cudaMalloc(&b.items, sizeof(BatchItem) * b.item_cap), "cudaMalloc");
+        if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
+    }
+    b.n_items = (int)first.size();
+    if (b.n_items)
+        ck(cudaMemcpyAsync(b.items, first.data(), sizeof(BatchItem) * b.n_items, cudaMemcpyHostToDevice,
+                           b.stream), "H2D");
+    ck(cudaMemcpyAsync(b.d_n, &b.n_items, 4, cudaMemcpyHostToDevice, b.stream), "H2D");
+    b.dirty = false;
+}
+
+// The simulations' chunk length is written into their constant slots (Args).
+static void apply_chunk(Fp32Batch::Impl &b) {
+    for (int q = 0; q < kMaxBatch; q++) {
+        Fp32Sim *sim = b.slot[q];
+        if (!sim) continue;
+        Args a = sim->impl()->a;
+        if (b.chunk > 0) a.chunk = b.chunk;
+        ck(cudaMemcpyToSymbolAsync(c_jobs, &a, sizeof(Args), sizeof(Args) * q, cudaMemcpyHostToDevice,
+                                   b.stream), "cudaMemcpyToSymbol");
+    }
+}
+
+static void launch_tick(Fp32Batch::Impl &b, int par) {
+    const dim3 grid(b.sms * b.ctas_per_sm);
+    auto go = [&](auto kern) {
+        kern<<<grid, NTHREADS, SMEM_B, b.stream>>>(b.items, b.d_n, b.d_next, b.d_maps, b.d_t, b.d_end);
+    };
+    if (par == 0) {
+        if (b.jm == 0) go(k_fp32_batch<0, 0>);
+        else if (b.jm == 1) go(k_fp32_batch<0, 1>);
+        else go(k_fp32_batch<0, 2>);
+    } else {
+        if (b.jm == 0) go(k_fp32_batch<1, 0>);
+        else if (b.jm == 1) go(k_fp32_batch<1, 1>);
+        else go(k_fp32_batch<1, 2>);
+    }
+    k_batch_advance<<<1, kMaxBatch, 0, b.stream>>>(b.d_t, b.d_end, kMaxBatch, b.d_next);
+}
+
+// Two ticks (one of each parity) captured once and replayed.
+static void ensure_graph(Fp32Batch::Impl &b) {
+    if (b.graph && b.graph_ctas == b.ctas_per_sm) return;
+    if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
+    cudaGraph_t g;
+    ck(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal), "capture");
+    launch_tick(b, 0);
+    launch_tick(b, 1);
+    ck(cudaStreamEndCapture(b.stream, &g), "capture");
+    ck(cudaGraphInstantiate(&b.graph, g, 0), "cudaGraphInstantiate");
+    cudaGraphDestroy(g);
+    b.graph_ctas = b.ctas_per_sm;
+}
+
+int Fp32Batch::run(int nticks) {
+    Impl &b = *impl_;
+    if (b.jm < 0 || nticks <= 0) return 0;
+    if (b.dirty) build_items(b);
+    int launches = 0;
+    int done = 0;
+    // A tick of odd parity first, so that the graph (even, odd) starts even.
+    if (b.tick & 1) { launch_tick(b, 1); b.tick++; done++; launches += 2; }
+    if (nticks - done >= 2) ensure_graph(b);
+    while (nticks - done >= 2) {
+        ck(cudaGraphLaunch(b.graph, b.stream), "cudaGraphLaunch");
+        b.tick += 2; done += 2; launches += 4;
+    }
+    if (done < nticks) { launch_tick(b, (int)(b.tick & 1)); b.tick++; done++; launches += 2; }
+    ck(cudaGetLastError(), "batch launch");
+    for (int q = 0; q < kMaxBatch; q++)
+        if (b.slot[q]) {
+            const int before = b.host_t[q];
+            b.host_t[q] = std::min(b.tsteps[q], before + nticks);
+            // every pass flips the simulation's current set
+            if ((b.host_t[q] - before) & 1) b.slot[q]->m_cur_ ^= 1;
+            if (b.host_t[q] >= b.tsteps[q] && before < b.tsteps[q]) b.dirty = true;
+        }
+    return launches;
+}
+
+void Fp32Batch::sync() {
+    ck(cudaStreamSynchronize(impl_->stream), "batch sync");
+    for (int q = 0; q < kMaxBatch; q++)
+        if (impl_->slot[q]) impl_->slot[q]->check(impl_->stream);
+}
+
+// Online autotuning: each candidate (slab depth, CTAs per SM) advances the
+// live batch by two ticks, timed with events; the fastest candidate is kept.
+// The work is not wasted -- the simulations advance -- so the tuner costs
+// only the ticks spent on slower settings.
+int Fp32Batch::tune(const int *chunks, int nchunks, const int *ctas, int nctas) {
+    Impl &b = *impl_;
+    if (b.jm < 0) return 0;
+    double best = 1e300;
+    int best_chunk = b.chunk, best_ctas = b.ctas_per_sm, ticks = 0;
+    b.tune_log.clear();
+    for (int ci = 0; ci < nchunks; ci++)
+        for (int ki = 0; ki < nctas; ki++) {
+            int left = 1 << 30;
+            for (int q = 0; q < kMaxBatch; q++)
+                if (b.slot[q]) left = std::min(left, b.tsteps[q] - b.host_t[q]);
+            if (left < 4) break;
+            b.chunk = chunks[ci];
+            b.ctas_per_sm = std::max(1, std::min(ctas[ki], b.jm == 2 ? 2 : 3));
+            apply_chunk(b);
+            b.dirty = true;
+            run(2);  // settle (graph capture, item rebuild)
+            ck(cudaEventRecord(b.e0, b.stream), "event");
+            run(2);
+            ck(cudaEventRecord(b.e1, b.stream), "event");
+            ck(cudaEventSynchronize(b.e1), "event");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, b.e0, b.e1);
+            b.tune_log.push_back({chunks[ci] * 16 + b.ctas_per_sm, ms / 2});
+            ticks += 4;
+            if (ms < best) { best = ms; best_chunk = b.chunk; best_ctas = b.ctas_per_sm; }
+        }
+    b.chunk = best_chunk;
+    b.ctas_per_sm = best_ctas;
+    apply_chunk(b);
+    b.dirty = true;
+    return ticks;
+}
+
+int Fp32Batch::tuned_chunk() const { return impl_->chunk; }
+int Fp32Batch::impl_device() const { return impl_->device; }
+int Fp32Batch::tuned_ctas() const { return impl_->ctas_per_sm; }
+long long Fp32Batch::tick() const { return impl_->tick; }
 
 Fp32Sim::~Fp32Sim() { delete impl_; }
 

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 #include <sys/resource.h>
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -78,8 +79,11 @@ void set_last_error(const std::string &msg) { g_last_error = msg; }
 
 }  // namespace mfdtd
 
+struct mfdtd_batch;
+
 struct mfdtd_sim {
     Problem P;
+    mfdtd_batch *batch = nullptr;  // set while the simulation is a batch member
     mfdtd_run_opts opts{};
     int form = MFDTD_FORM_FP64_PLAIN;
     cudaStream_t stream = nullptr;
@@ -285,6 +289,7 @@ struct mfdtd_sim {
     }
 
     void advance(int nsteps, bool collect) {
+        if (batch) throw Error(MFDTD_ESTATE, "the simulation is a batch member (mfdtd_batch_remove first)");
         if (nsteps < 0 || t + nsteps > P.tsteps)
             throw Error(MFDTD_EINVAL, "advance past tsteps");
         int64_t launches = 0;
@@ -463,6 +468,11 @@ struct mfdtd_sim {
     }
 };
 
+struct mfdtd_batch {
+    std::unique_ptr<mfdtd::Fp32Batch> fb;
+    std::vector<mfdtd_sim *> members;
+};
+
 namespace {
 
 int fail(const Error &e) {
@@ -606,7 +616,10 @@ int mfdtd_sim_create(const mfdtd_problem *pb, const mfdtd_run_opts *opts, mfdtd_
     });
 }
 
-void mfdtd_sim_destroy(mfdtd_sim *s) { delete s; }
+void mfdtd_sim_destroy(mfdtd_sim *s) {
+    if (s && s->batch) mfdtd_batch_remove(s->batch, s);  // never leave a dangling member
+    delete s;
+}
 
 int mfdtd_sim_advance(mfdtd_sim *s, int32_t nsteps, int32_t collect_records) {
     return guarded([&] {
@@ -705,6 +718,87 @@ int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t
         if (name && name_len) std::snprintf(name, name_len, "%s", s->kname[which].c_str());
         if (avg_ms) *avg_ms = s->kcount[which] ? s->ktotal_ms[which] / s->kcount[which] : 0.0;
         if (launches) *launches = s->kcount[which];
+    });
+}
+
+int mfdtd_batch_capacity(void) { return mfdtd::Fp32Batch::capacity(); }
+
+int mfdtd_batch_create(int32_t device, mfdtd_batch **out) {
+    return guarded([&] {
+        if (!out) throw Error(MFDTD_EINVAL, "NULL argument");
+        std::unique_ptr<mfdtd_batch> b(new mfdtd_batch());
+        b->fb.reset(new mfdtd::Fp32Batch(device));
+        *out = b.release();
+    });
+}
+
+void mfdtd_batch_destroy(mfdtd_batch *b) {
+    if (!b) return;
+    try {
+        b->fb->sync();
+    } catch (...) {
+    }
+    for (mfdtd_sim *s : b->members) s->batch = nullptr;
+    delete b;
+}
+
+int mfdtd_batch_add(mfdtd_batch *b, mfdtd_sim *s) {
+    return guarded([&] {
+        if (!b || !s) throw Error(MFDTD_EINVAL, "NULL argument");
+        if (s->batch) throw Error(MFDTD_ESTATE, "the simulation is already a batch member");
+        if (s->form != MFDTD_FORM_FP32_FUSED) throw Error(MFDTD_EINVAL, "batches hold FP32 simulations");
+        if (s->opts.device != b->fb->impl_device())
+            throw Error(MFDTD_EINVAL, "the simulation lives on another device");
+        mfdtd::ck(cudaStreamSynchronize(s->stream), "sim");
+        b->fb->add(s->f32.get(), s->t);
+        s->batch = b;
+        b->members.push_back(s);
+    });
+}
+
+int mfdtd_batch_remove(mfdtd_batch *b, mfdtd_sim *s) {
+    return guarded([&] {
+        if (!b || !s) throw Error(MFDTD_EINVAL, "NULL argument");
+        if (s->batch != b) throw Error(MFDTD_EINVAL, "not a member of this batch");
+        b->fb->sync();
+        const int done = b->fb->steps_done(s->f32.get());
+        if (done >= 0) s->t = done;
+        b->fb->remove(s->f32.get());
+        s->batch = nullptr;
+        b->members.erase(std::find(b->members.begin(), b->members.end(), s));
+    });
+}
+
+int mfdtd_batch_run(mfdtd_batch *b, int32_t nsteps) {
+    return guarded([&] {
+        if (!b || nsteps < 0) throw Error(MFDTD_EINVAL, "bad arguments");
+        b->fb->run(nsteps);
+    });
+}
+
+int mfdtd_batch_sync(mfdtd_batch *b) {
+    return guarded([&] {
+        if (!b) throw Error(MFDTD_EINVAL, "NULL batch");
+        b->fb->sync();
+        for (mfdtd_sim *s : b->members) {
+            const int done = b->fb->steps_done(s->f32.get());
+            if (done >= 0) s->t = done;
+        }
+    });
+}
+
+int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depths,
+                     const int32_t *ctas_per_sm, int32_t n_ctas, int32_t *best_depth,
+                     int32_t *best_ctas) {
+    return guarded([&] {
+        if (!b || !slab_depths || !ctas_per_sm || n_depths <= 0 || n_ctas <= 0)
+            throw Error(MFDTD_EINVAL, "bad arguments");
+        for (int q = 0; q < n_depths; q++)
+            if (slab_depths[q] < 2) throw Error(MFDTD_EINVAL, "slab depth must be >= 2");
+        std::vector<int> d(slab_depths, slab_depths + n_depths), c(ctas_per_sm, ctas_per_sm + n_ctas);
+        b->fb->tune(d.data(), n_depths, c.data(), n_ctas);
+        if (best_depth) *best_depth = b->fb->tuned_chunk();
+        if (best_ctas) *best_ctas = b->fb->tuned_ctas();
     });
 }
 

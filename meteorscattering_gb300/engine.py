@@ -34,7 +34,9 @@ EXPORTS = (
     "mfdtd_sim_read_probes", "mfdtd_sim_read_field", "mfdtd_sim_write_outputs",
     "mfdtd_sim_last_timing", "mfdtd_sim_kernel_stats", "mfdtd_sim_far_field",
     "mfdtd_far_field_static", "mfdtd_last_error", "mfdtd_version", "mfdtd_ext_defaults",
-    "mfdtd_problem_set_ext", "mfdtd_problem_set_trail",
+    "mfdtd_problem_set_ext", "mfdtd_problem_set_trail", "mfdtd_batch_capacity",
+    "mfdtd_batch_create", "mfdtd_batch_destroy", "mfdtd_batch_add", "mfdtd_batch_remove",
+    "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune",
 )
 
 
@@ -120,6 +122,15 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_ext_defaults": (None, [C.POINTER(Ext)]),
         "mfdtd_problem_set_ext": (C.c_int, [vp, C.POINTER(Ext), dp, dp]),
         "mfdtd_problem_set_trail": (C.c_int, [vp, C.POINTER(Trail)]),
+        "mfdtd_batch_capacity": (C.c_int, []),
+        "mfdtd_batch_create": (C.c_int, [i32, C.POINTER(vp)]),
+        "mfdtd_batch_destroy": (None, [vp]),
+        "mfdtd_batch_add": (C.c_int, [vp, vp]),
+        "mfdtd_batch_remove": (C.c_int, [vp, vp]),
+        "mfdtd_batch_run": (C.c_int, [vp, i32]),
+        "mfdtd_batch_sync": (C.c_int, [vp]),
+        "mfdtd_batch_tune": (C.c_int, [vp, C.POINTER(i32), i32, C.POINTER(i32), i32,
+                                       C.POINTER(i32), C.POINTER(i32)]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -335,6 +346,56 @@ class Simulation:
         if self._h:
             load_library().mfdtd_sim_destroy(self._h)
             self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """FP32 simulations advanced together by the persistent kernel (see
+    ``mfdtd_batch_*`` in include/mfdtd.h)."""
+
+    def __init__(self, device: int = 0):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.mfdtd_batch_create(device, C.byref(h)))
+        self._h = h
+        self._members = []
+
+    @staticmethod
+    def capacity() -> int:
+        return load_library().mfdtd_batch_capacity()
+
+    def add(self, sim: "Simulation") -> None:
+        _check(load_library().mfdtd_batch_add(self._h, sim._h))
+        self._members.append(sim)
+
+    def remove(self, sim: "Simulation") -> None:
+        _check(load_library().mfdtd_batch_remove(self._h, sim._h))
+        self._members.remove(sim)
+
+    def run(self, nsteps: int) -> None:
+        _check(load_library().mfdtd_batch_run(self._h, nsteps))
+
+    def sync(self) -> None:
+        _check(load_library().mfdtd_batch_sync(self._h))
+
+    def tune(self, slab_depths=(16, 32, 64, 128), ctas_per_sm=(2, 3)):
+        d = (C.c_int32 * len(slab_depths))(*slab_depths)
+        c = (C.c_int32 * len(ctas_per_sm))(*ctas_per_sm)
+        bd, bc = C.c_int32(), C.c_int32()
+        _check(load_library().mfdtd_batch_tune(self._h, d, len(slab_depths), c, len(ctas_per_sm),
+                                               C.byref(bd), C.byref(bc)))
+        return bd.value, bc.value
+
+    def close(self):
+        if self._h:
+            load_library().mfdtd_batch_destroy(self._h)
+            self._h = None
+            self._members = []
 
     def __del__(self):
         try:
