@@ -274,6 +274,36 @@ int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depth
                      const int32_t *ctas_per_sm, int32_t n_ctas, int32_t *best_depth,
                      int32_t *best_ctas);
 
+/* ---- serving loop (chosen form) ---------------------------------------------
+ * No counterpart in the reference (its sweep driver is MATLAB + PBS,
+ * setup/meteorbatch.m).  A server owns a worker thread on one device.  Jobs
+ * (a problem plus the radar directions wanted) are queued by
+ * mfdtd_server_submit and admitted in arrival order while their FP32 device
+ * footprint fits under hbm_cap_bytes and their batch has a free slot; every
+ * round the worker advances all admitted jobs steps_per_round steps in
+ * batches (one per current-update kind, overlapping on the device), retires
+ * the jobs that reached their step count -- far field computed on the device,
+ * device memory freed -- and admits waiting jobs into the freed space.
+ * Fields stay on the device from admission to retirement. */
+typedef struct mfdtd_server mfdtd_server;
+int mfdtd_server_create(int32_t device, int64_t hbm_cap_bytes, int32_t steps_per_round,
+                        mfdtd_server **out);
+/* Stops the worker; jobs not yet retired are dropped. */
+void mfdtd_server_destroy(mfdtd_server *s);
+/* Queue a job: the problem is copied; theta/phi[ndir] in radians (as for
+ * mfdtd_sim_far_field).  Fails with MFDTD_ENOMEM when the job alone exceeds
+ * the cap. */
+int mfdtd_server_submit(mfdtd_server *s, const mfdtd_problem *pb, int32_t ndir,
+                        const double *theta, const double *phi, int64_t *job_id);
+/* Wait up to wait_ms for the job.  *done = 1: out[nntf*ndir*3] holds the cross
+ * sections (mfdtd_sim_far_field layout), times[0..2] = seconds from submission
+ * to admission, to retirement, and device seconds are not separable (0); the
+ * job record is released.  *done = 0: still queued or running. */
+int mfdtd_server_poll(mfdtd_server *s, int64_t job_id, int32_t wait_ms, double *out, int64_t n_out,
+                      double times[3], int32_t *done);
+/* out[0..4] = submitted, queued, running, retired, device bytes in use. */
+int mfdtd_server_stats(mfdtd_server *s, int64_t out[5]);
+
 /* ---- errors ---------------------------------------------------------------- */
 /* Copy the last error message of the calling thread into buf (NUL-terminated). */
 int mfdtd_last_error(char *buf, size_t n);

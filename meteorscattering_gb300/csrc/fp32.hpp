@@ -16,6 +16,9 @@ public:
     // (may be null) receives kernel_classes()+1 boundary events.
     int step(int t, bool record, void *stream, void *const *ev);
     static int kernel_classes();
+    // Current-update kind of this simulation's kernel (0 Young DI, 1 uniform
+    // Lee-Kalluri, 2 tabulated Lee-Kalluri); batches group by it.
+    int current_update() const;
     static const char *kernel_name(int which);
     // Record-step outputs in the reference file layout (doubles).
     void record(double *E, double *H, double *emax, void *stream);

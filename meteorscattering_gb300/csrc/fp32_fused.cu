@@ -1494,6 +1494,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
 }
 
 int Fp32Sim::kernel_classes() { return 1; }
+int Fp32Sim::current_update() const { return impl_->jm; }
 const char *Fp32Sim::kernel_name(int) { return "k_fp32_step"; }
 
 int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {

@@ -4,6 +4,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <map>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -828,6 +832,277 @@ int mfdtd_run_rundir(const char *dir, const mfdtd_run_opts *opts) {
         }
         fs.log("All done!\n");
         fs.log("Total run time = " + mfdtd::fmt_g((mfdtd::wall_s() - tStart) / 60.0) + "minutes.\n");
+    });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Serving loop
+
+namespace {
+
+struct ServerJob {
+    int64_t id = 0;
+    Problem P;
+    std::vector<double> theta, phi;
+    std::unique_ptr<mfdtd_sim> sim;
+    int64_t bytes = 0;
+    int kind = -1;                 // current-update kind (batch key)
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int state = 0;                 // 0 queued, 1 running, 2 retired, 3 failed
+    int code = 0;
+    std::string err;
+    std::vector<double> result;
+};
+
+}  // namespace
+
+struct mfdtd_server {
+    int device = 0;
+    int64_t cap = 0;
+    int steps = 100;
+    std::thread worker;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    bool stop = false;
+    int64_t next_id = 1, n_submitted = 0, n_retired = 0, used = 0;
+    std::deque<ServerJob *> queued;
+    std::map<int64_t, std::unique_ptr<ServerJob>> jobs;
+    std::vector<ServerJob *> running;
+    std::map<int, std::unique_ptr<mfdtd_batch>> batches;
+
+    void loop() {
+        cudaSetDevice(device);
+        for (;;) {
+            // admit in arrival order while memory and slots allow
+            std::vector<ServerJob *> admit;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                if (running.empty() && queued.empty() && !stop)
+                    cv_work.wait_for(lk, std::chrono::milliseconds(20));
+                if (stop) break;
+                int64_t free_bytes = cap - used;
+                std::map<int, int> members;
+                for (auto &kv : batches) members[kv.first] = (int)kv.second->members.size();
+                while (!queued.empty()) {
+                    ServerJob *j = queued.front();
+                    if (j->bytes > free_bytes) break;  // arrival order: no overtaking
+                    if (members[j->kind] >= mfdtd::Fp32Batch::capacity()) break;
+                    queued.pop_front();
+                    free_bytes -= j->bytes;
+                    members[j->kind]++;
+                    used += j->bytes;
+                    admit.push_back(j);
+                }
+            }
+            for (ServerJob *j : admit) {
+                try {
+                    mfdtd_run_opts o{};
+                    o.form = MFDTD_FORM_FP32_FUSED;
+                    o.device = device;
+                    o.quiet = 1;
+                    j->sim.reset(new mfdtd_sim());
+                    j->sim->init(j->P, &o);
+                    auto &b = batches[j->kind];
+                    if (!b) {
+                        b.reset(new mfdtd_batch());
+                        b->fb.reset(new mfdtd::Fp32Batch(device));
+                    }
+                    b->fb->add(j->sim->f32.get(), 0);
+                    j->sim->batch = b.get();
+                    b->members.push_back(j->sim.get());
+                    std::lock_guard<std::mutex> lk(mu);
+                    j->state = 1;
+                    j->t_admit = mfdtd::wall_s();
+                    running.push_back(j);
+                } catch (const Error &e) {
+                    finish_failed(j, e.code, e.what());
+                } catch (const std::exception &e) {
+                    finish_failed(j, MFDTD_ECUDA, e.what());
+                }
+            }
+            if (running.empty()) continue;
+            // one round: every batch advances; the batches overlap on the device
+            for (auto &kv : batches)
+                if (!kv.second->members.empty()) kv.second->fb->run(steps);
+            for (auto &kv : batches) {
+                if (kv.second->members.empty()) continue;
+                try {
+                    kv.second->fb->sync();
+                } catch (const Error &e) {
+                    for (mfdtd_sim *m : kv.second->members)
+                        for (ServerJob *j : running)
+                            if (j->sim.get() == m) j->code = e.code, j->err = e.what();
+                }
+                for (mfdtd_sim *m : kv.second->members) {
+                    const int d = kv.second->fb->steps_done(m->f32.get());
+                    if (d >= 0) m->t = d;
+                }
+            }
+            // retire
+            std::vector<ServerJob *> still;
+            for (ServerJob *j : running) {
+                mfdtd_sim *m = j->sim.get();
+                if (j->code == 0 && m->t < m->P.tsteps) {
+                    still.push_back(j);
+                    continue;
+                }
+                try {
+                    if (j->code) throw Error(j->code, j->err);
+                    mfdtd_batch *b = m->batch;
+                    b->fb->remove(m->f32.get());
+                    b->members.erase(std::find(b->members.begin(), b->members.end(), m));
+                    m->batch = nullptr;
+                    const int nd = (int)j->theta.size();
+                    j->result.assign((size_t)m->P.nntf() * nd * 3, 0.0);
+                    m->flush();
+                    std::vector<double> sd = m->source_dft();
+                    mfdtd::far_field_fp64(m->P, m->f32->ntf_arrays(), sd.data(), nd, j->theta.data(),
+                                          j->phi.data(), j->result.data(), m->stream);
+                    j->sim.reset();
+                    std::lock_guard<std::mutex> lk(mu);
+                    used -= j->bytes;
+                    j->state = 2;
+                    j->t_done = mfdtd::wall_s();
+                    n_retired++;
+                } catch (const Error &e) {
+                    if (m && m->batch) {
+                        mfdtd_batch *b = m->batch;
+                        b->fb->remove(m->f32.get());
+                        b->members.erase(std::find(b->members.begin(), b->members.end(), m));
+                        m->batch = nullptr;
+                    }
+                    j->sim.reset();
+                    finish_failed(j, e.code, e.what());
+                }
+                cv_done.notify_all();
+            }
+            std::lock_guard<std::mutex> lk(mu);
+            running.swap(still);
+        }
+    }
+
+    void finish_failed(ServerJob *j, int code, const std::string &msg) {
+        std::lock_guard<std::mutex> lk(mu);
+        if (j->state == 1 || j->state == 0) used -= j->bytes;
+        j->state = 3;
+        j->code = code;
+        j->err = msg;
+        j->t_done = mfdtd::wall_s();
+        cv_done.notify_all();
+    }
+
+    ~mfdtd_server() {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+        }
+        cv_work.notify_all();
+        if (worker.joinable()) worker.join();
+        for (auto &kv : jobs)
+            if (kv.second->sim && kv.second->sim->batch) {
+                mfdtd_batch *b = kv.second->sim->batch;
+                try {
+                    b->fb->remove(kv.second->sim->f32.get());
+                } catch (...) {
+                }
+                kv.second->sim->batch = nullptr;
+            }
+        jobs.clear();
+        batches.clear();
+    }
+};
+
+extern "C" {
+
+int mfdtd_server_create(int32_t device, int64_t hbm_cap_bytes, int32_t steps_per_round,
+                        mfdtd_server **out) {
+    return guarded([&] {
+        if (!out || hbm_cap_bytes <= 0 || steps_per_round <= 0) throw Error(MFDTD_EINVAL, "bad arguments");
+        std::unique_ptr<mfdtd_server> s(new mfdtd_server());
+        s->device = device;
+        s->cap = hbm_cap_bytes;
+        s->steps = steps_per_round;
+        mfdtd::ck(cudaSetDevice(device), "cudaSetDevice");
+        mfdtd_server *raw = s.get();
+        s->worker = std::thread([raw] { raw->loop(); });
+        *out = s.release();
+    });
+}
+
+void mfdtd_server_destroy(mfdtd_server *s) { delete s; }
+
+int mfdtd_server_submit(mfdtd_server *s, const mfdtd_problem *pb, int32_t ndir, const double *theta,
+                        const double *phi, int64_t *job_id) {
+    return guarded([&] {
+        if (!s || !pb || !theta || !phi || ndir <= 0 || !job_id) throw Error(MFDTD_EINVAL, "bad arguments");
+        std::unique_ptr<ServerJob> j(new ServerJob());
+        j->P = pb->P;
+        j->theta.assign(theta, theta + ndir);
+        j->phi.assign(phi, phi + ndir);
+        j->bytes = mfdtd::Fp32Sim::footprint(j->P);
+        if (j->bytes > s->cap) throw Error(MFDTD_ENOMEM, "job footprint exceeds the server's device cap");
+        // The batch key: the current update the FP32 kernel will use.
+        const Problem &P = j->P;
+        int kind = 0;
+        if (P.doB0) {
+            bool uniform = !P.lk.empty();
+            for (size_t q = 18; q < P.lk.size() && uniform; q++) uniform = P.lk[q] == P.lk[q % 18];
+            kind = uniform ? 1 : 2;
+        }
+        j->kind = kind;
+        j->t_submit = mfdtd::wall_s();
+        std::lock_guard<std::mutex> lk(s->mu);
+        j->id = s->next_id++;
+        *job_id = j->id;
+        s->queued.push_back(j.get());
+        s->jobs[j->id] = std::move(j);
+        s->n_submitted++;
+        s->cv_work.notify_all();
+    });
+}
+
+int mfdtd_server_poll(mfdtd_server *s, int64_t job_id, int32_t wait_ms, double *out, int64_t n_out,
+                      double times[3], int32_t *done) {
+    return guarded([&] {
+        if (!s || !done) throw Error(MFDTD_EINVAL, "bad arguments");
+        std::unique_lock<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(job_id);
+        if (it == s->jobs.end()) throw Error(MFDTD_EINVAL, "unknown job id");
+        ServerJob *j = it->second.get();
+        if (j->state < 2 && wait_ms > 0)
+            s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return j->state >= 2; });
+        *done = j->state >= 2 ? 1 : 0;
+        if (j->state < 2) return;
+        if (j->state == 3) {
+            const int code = j->code ? j->code : MFDTD_ECUDA;
+            const std::string msg = j->err;
+            s->jobs.erase(it);
+            throw Error(code, "job failed: " + msg);
+        }
+        if (out) {
+            if (n_out < (int64_t)j->result.size()) throw Error(MFDTD_EINVAL, "output buffer too small");
+            std::memcpy(out, j->result.data(), j->result.size() * 8);
+        }
+        if (times) {
+            times[0] = j->t_admit - j->t_submit;
+            times[1] = j->t_done - j->t_submit;
+            times[2] = 0;
+        }
+        s->jobs.erase(it);
+    });
+}
+
+int mfdtd_server_stats(mfdtd_server *s, int64_t out[5]) {
+    return guarded([&] {
+        if (!s || !out) throw Error(MFDTD_EINVAL, "bad arguments");
+        std::lock_guard<std::mutex> lk(s->mu);
+        out[0] = s->n_submitted;
+        out[1] = (int64_t)s->queued.size();
+        out[2] = (int64_t)s->running.size();
+        out[3] = s->n_retired;
+        out[4] = s->used;
     });
 }
 

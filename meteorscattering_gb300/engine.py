@@ -36,7 +36,8 @@ EXPORTS = (
     "mfdtd_far_field_static", "mfdtd_last_error", "mfdtd_version", "mfdtd_ext_defaults",
     "mfdtd_problem_set_ext", "mfdtd_problem_set_trail", "mfdtd_batch_capacity",
     "mfdtd_batch_create", "mfdtd_batch_destroy", "mfdtd_batch_add", "mfdtd_batch_remove",
-    "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune",
+    "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune", "mfdtd_server_create",
+    "mfdtd_server_destroy", "mfdtd_server_submit", "mfdtd_server_poll", "mfdtd_server_stats",
 )
 
 
@@ -131,6 +132,11 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_batch_sync": (C.c_int, [vp]),
         "mfdtd_batch_tune": (C.c_int, [vp, C.POINTER(i32), i32, C.POINTER(i32), i32,
                                        C.POINTER(i32), C.POINTER(i32)]),
+        "mfdtd_server_create": (C.c_int, [i32, i64, i32, C.POINTER(vp)]),
+        "mfdtd_server_destroy": (None, [vp]),
+        "mfdtd_server_submit": (C.c_int, [vp, vp, i32, dp, dp, C.POINTER(i64)]),
+        "mfdtd_server_poll": (C.c_int, [vp, i64, i32, dp, i64, dp, C.POINTER(i32)]),
+        "mfdtd_server_stats": (C.c_int, [vp, C.POINTER(i64)]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -396,6 +402,57 @@ class Batch:
             load_library().mfdtd_batch_destroy(self._h)
             self._h = None
             self._members = []
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """The native serving loop (``mfdtd_server_*``): submit problems with the
+    radar directions wanted, poll for their cross sections."""
+
+    def __init__(self, device: int = 0, hbm_cap_bytes: int = 150 * 10 ** 9,
+                 steps_per_round: int = 100):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.mfdtd_server_create(device, int(hbm_cap_bytes), steps_per_round, C.byref(h)))
+        self._h = h
+        self._nf = {}
+
+    def submit(self, problem: Problem, theta, phi) -> int:
+        th = np.ascontiguousarray(theta, dtype=np.float64)
+        ph = np.ascontiguousarray(phi, dtype=np.float64)
+        jid = C.c_int64()
+        _check(load_library().mfdtd_server_submit(self._h, problem._h, th.size, _dp(th), _dp(ph),
+                                                  C.byref(jid)))
+        self._nf[jid.value] = (problem.dims()[4], th.size)
+        return jid.value
+
+    def poll(self, job_id: int, wait_ms: int = 0):
+        """(done, sigma[nntf, ndir, 3] or None, (to_admission_s, to_done_s))."""
+        nf, nd = self._nf[job_id]
+        out = np.empty((nf, nd, 3), dtype=np.float64)
+        times = np.zeros(3)
+        done = C.c_int32()
+        _check(load_library().mfdtd_server_poll(self._h, job_id, wait_ms, _dp(out), out.size,
+                                                _dp(times), C.byref(done)))
+        if not done.value:
+            return False, None, None
+        del self._nf[job_id]
+        return True, out, (times[0], times[1])
+
+    def stats(self):
+        out = (C.c_int64 * 5)()
+        _check(load_library().mfdtd_server_stats(self._h, out))
+        return dict(zip(("submitted", "queued", "running", "retired", "device_bytes"), out))
+
+    def close(self):
+        if self._h:
+            load_library().mfdtd_server_destroy(self._h)
+            self._h = None
 
     def __del__(self):
         try:
