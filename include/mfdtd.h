@@ -213,7 +213,10 @@ int mfdtd_sim_last_timing(const mfdtd_sim *s, double *ms_per_step, int64_t *laun
  * analysis/loadconstants.m and the incident power of the source DFT, as the
  * MATLAB does.  out[(m * ndir + d) * 3 + {0, 1, 2}] = sigma, and its two
  * polarisation parts |L_phi + eta0 N_theta|^2 and |L_theta - eta0 N_phi|^2
- * terms, in m^2, for frequency m.  method 0: FP64 on the CUDA cores. */
+ * terms, in m^2, for frequency m.  method 0: FP64 on the CUDA cores.
+ * method 1: the dense contraction (sums x phases) on the tensor cores in TF32
+ * with a three-term split (about 21 bits per product) and FP32 accumulation;
+ * the angular reduction in FP64. */
 int mfdtd_sim_far_field(mfdtd_sim *s, int32_t ndir, const double *theta, const double *phi,
                         int32_t method, double *out);
 
@@ -282,8 +285,9 @@ int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depth
  * footprint fits under hbm_cap_bytes and their batch has a free slot; every
  * round the worker advances all admitted jobs steps_per_round steps in
  * batches (one per current-update kind, overlapping on the device), retires
- * the jobs that reached their step count -- far field computed on the device,
- * device memory freed -- and admits waiting jobs into the freed space.
+ * the jobs that reached their step count -- far field computed on the device
+ * (method 1: the contraction on the tensor cores), device memory freed -- and
+ * admits waiting jobs into the freed space.
  * Fields stay on the device from admission to retirement. */
 typedef struct mfdtd_server mfdtd_server;
 int mfdtd_server_create(int32_t device, int64_t hbm_cap_bytes, int32_t steps_per_round,

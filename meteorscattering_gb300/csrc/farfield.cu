@@ -14,7 +14,15 @@
 //            P[u][b] = w_b exp(-jk s_u pos_b), s_u the distinct values of r_b
 //            over the direction set (a theta/phi grid has few of them);
 //   stage 2 (reduction):    L[d] += exp(-jk r_n n0) dA sum_a w_a exp(-jk r_a pos_a) T[u(d)][a].
-// Both stages run in FP64 on the CUDA cores.
+// Method 0 runs both stages in FP64 on the CUDA cores.  Method 1 runs stage 1
+// -- the dense contraction; on the faces whose b axis is y there is one u per
+// direction, so it is a full GEMM -- on the tensor cores (tcgen05, TF32 with
+// FP32 accumulation).  Each operand is split into a TF32 head and a TF32
+// tail, x = hi + lo, and the three significant products hi*hi + hi*lo + lo*hi
+// are accumulated in one GEMM by concatenating the splits along K, which
+// keeps about 21 bits per product.  The complex product is one real GEMM:
+// rows [Pr | Pi] of the phase against rows [Xr | -Xi] (real part) and
+// [Xi | Xr] (imaginary part) of the sums.  Stage 2 stays FP64.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -26,6 +34,7 @@
 
 #include "common.hpp"
 #include "farfield.hpp"
+#include "tc_gemm.cuh"
 
 namespace mfdtd {
 namespace {
@@ -120,6 +129,137 @@ __global__ void __launch_bounds__(256) k_ff_reduce(double2 *out, const double2 *
     }
 }
 
+// ---- tensor-core stage 1 -----------------------------------------------------
+__device__ __forceinline__ float tf32_round(float x) {
+    return __uint_as_float((__float_as_uint(x) + 0x1000u) & ~0x1FFFu);
+}
+// TF32 head and tail of an FP64 value: hi + lo carries about 21 bits.
+__device__ __forceinline__ void tf32_split(double v, float &hi, float &lo) {
+    hi = tf32_round((float)v);
+    lo = tf32_round((float)(v - (double)hi));
+}
+
+// sin and cos of an FP64 phase: the argument is reduced to [-pi, pi] in FP64
+// and evaluated in FP32 (about 23 bits, more than the 21 the TF32 split keeps;
+// FP64 transcendentals are slow on this part).
+__device__ __forceinline__ void sincos_reduced(double x, float *sn, float *cs) {
+    const double two_pi = 6.283185307179586;
+    const double r = x - two_pi * rint(x * (1.0 / two_pi));
+    sincosf((float)r, sn, cs);
+}
+
+// Phase operand: row u, K = [Phi_r Phi_i | Phi_r Phi_i | Plo_r Plo_i] (B each),
+// zero-padded to Kpad and to Upad rows.  One thread per (u, b).
+__global__ void k_tc_pack_phase(float *A, const double *s, int U, int B, int Kpad, double k,
+                                double b_off, double hb, int halve_ends) {
+    const int u = blockIdx.y;
+    float *row = A + (size_t)u * Kpad;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+        float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+        if (u < U) {
+            const double pos = (b + b_off) * hb;
+            float sn, cs;
+            sincos_reduced(-k * s[u] * pos, &sn, &cs);
+            const double w = (halve_ends && (b == 0 || b == B - 1)) ? 0.5 : 1.0;
+            tf32_split(w * (double)cs, rh, rl);
+            tf32_split(w * (double)sn, ih, il);
+        }
+        row[b] = rh; row[B + b] = ih;              // meets the sums head
+        row[2 * B + b] = rh; row[3 * B + b] = ih;  // meets the sums tail
+        row[4 * B + b] = rl; row[5 * B + b] = il;  // phase tail, meets the sums head
+    }
+    for (int q = 6 * B + blockIdx.x * blockDim.x + threadIdx.x; q < Kpad; q += gridDim.x * blockDim.x)
+        row[q] = 0.f;
+}
+
+// Sums operand: row r = c * 2A + 2a + {0 re, 1 im} for the components c of one
+// face kind, K = [X_hi | X_lo | X_hi] with the real row [Xr, -Xi] and the
+// imaginary row [Xi, Xr]; X(a,b) = cos-sum + i sin-sum of the DFT arrays.
+struct PackSrc {
+    const double *src[2];
+};
+__global__ void k_tc_pack_sums(float *Bm, PackSrc ps, int ncomp, int A, int B, int a0, int b0, int Bs,
+                               int n2, int m, int Kpad) {
+    const int r = blockIdx.y;
+    const int c = r / (2 * A), a = (r % (2 * A)) / 2, im = r & 1;
+    float *row = Bm + (size_t)r * Kpad;
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < B; b += gridDim.x * blockDim.x) {
+        float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+        if (c < ncomp) {
+            const size_t o = ((size_t)(a0 + a) * Bs + (b0 + b)) * n2 + 2 * m;
+            const double xr = ps.src[c][o + 1], xi = ps.src[c][o];
+            tf32_split(im ? xi : xr, h0, l0);    // first half of each segment
+            tf32_split(im ? xr : -xi, h1, l1);   // second half
+        }
+        row[b] = h0; row[B + b] = h1;              // meets the phase head
+        row[2 * B + b] = l0; row[3 * B + b] = l1;  // sums tail, meets the phase head
+        row[4 * B + b] = h0; row[5 * B + b] = h1;  // meets the phase tail
+    }
+    for (int q = 6 * B + blockIdx.x * blockDim.x + threadIdx.x; q < Kpad; q += gridDim.x * blockDim.x)
+        row[q] = 0.f;
+}
+
+// Stage 2 reading stage 1 from the FP32 GEMM tile: T[u][a] = (C[u][col0 + 2a],
+// C[u][col0 + 2a + 1]).  One warp per direction (faces are a few hundred cells
+// wide), FP64 accumulation, FP32-evaluated phases.
+__global__ void __launch_bounds__(256) k_ff_reduce_tc(double2 *out, const float *C, int ldc, int col0,
+                                                      const int *umap, const double *ra, const double *rn,
+                                                      int D, int A, double k, double a_off, double ha,
+                                                      int halve_ends, double n0, double area) {
+    const int d = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (d >= D) return;
+    const float2 *row = (const float2 *)(C + (size_t)umap[d] * ldc + col0);
+    const double kr = -k * ra[d];
+    double re = 0, im = 0;
+    for (int a = lane; a < A; a += 32) {
+        float sn, cs;
+        sincos_reduced(kr * ((a + a_off) * ha), &sn, &cs);
+        const double w = (halve_ends && (a == 0 || a == A - 1)) ? 0.5 : 1.0;
+        const float2 t = row[a];
+        re += w * ((double)cs * t.x - (double)sn * t.y);
+        im += w * ((double)cs * t.y + (double)sn * t.x);
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        re += __shfl_down_sync(0xffffffffu, re, off);
+        im += __shfl_down_sync(0xffffffffu, im, off);
+    }
+    if (lane == 0) {
+        float sn, cs;
+        sincos_reduced(-k * rn[d] * n0, &sn, &cs);
+        out[d].x += area * ((double)cs * re - (double)sn * im);
+        out[d].y += area * ((double)cs * im + (double)sn * re);
+    }
+}
+
+using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                              const cuuint64_t *, const cuuint32_t *, const cuuint32_t *,
+                              CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                              CUtensorMapFloatOOBfill);
+EncodeFn tensor_map_encoder() {
+    static EncodeFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !p)
+            throw Error(MFDTD_ECUDA, "cuTensorMapEncodeTiled is not available");
+        fn = (EncodeFn)p;
+    }
+    return fn;
+}
+
+// K-major operand [rows][Kpad] fp32, 128 x 32 boxes with 128-byte swizzling.
+void tc_operand_map(CUtensorMap *m, float *base, int rows, int Kpad) {
+    cuuint64_t dims[2] = {(cuuint64_t)Kpad, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)Kpad * 4};
+    cuuint32_t box[2] = {(cuuint32_t)tc::BK, 128}, es[2] = {1, 1};
+    CUresult r = tensor_map_encoder()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, base, dims, strides, box, es,
+                                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw Error(MFDTD_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+}
+
 struct FaceDesc {
     int n_ax, a_ax, b_ax;  // 0 = x, 1 = y, 2 = z
     bool high;             // back / top / right
@@ -141,8 +281,16 @@ const CompDesc kComps[3][4] = {
 
 // Far-field of the 24 device arrays `ntf` (file layout) for the given directions.
 void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdft, int ndir,
-                    const double *theta, const double *phi, double *out, void *stream) {
+                    const double *theta, const double *phi, double *out, void *stream, int method) {
     cudaStream_t st = (cudaStream_t)stream;
+    if (method == 1) {
+        static bool attr_done = false;
+        if (!attr_done) {
+            ck(cudaFuncSetAttribute(tc::k_tc_gemm_tf32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    tc::SMEM_BYTES), "attr");
+            attr_done = true;
+        }
+    }
     const int nf = P.nntf(), ntfb = P.ntfb, n2 = 2 * nf;
     const int dims[3] = {P.Nx, P.Ny, P.Nz};
     const double h[3] = {P.dx, P.dy, P.dz};
@@ -200,6 +348,44 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
             if (A <= 0 || B <= 0) continue;
             const double a_off = kind == 0 ? ntfb : ntfb + 0.5;
             const double b_off = kind == 0 ? ntfb + 0.5 : ntfb;
+            if (method == 1) {
+                // stage 1 on the tensor cores, both components of this kind at once
+                const CompDesc *cs[2];
+                int ncomp = 0;
+                for (int c = 0; c < 4; c++)
+                    if (kComps[F.n_ax][c].kind == kind) cs[ncomp++] = &kComps[F.n_ax][c];
+                const int Upad = (U + 127) / 128 * 128, Nrows = ncomp * 2 * A;
+                const int Npad = (Nrows + 127) / 128 * 128, Kpad = (6 * B + 31) / 32 * 32;
+                float *Am = (float *)dmalloc((size_t)Upad * Kpad * 4);
+                float *Bm = (float *)dmalloc((size_t)Npad * Kpad * 4);
+                float *Cm = (float *)dmalloc((size_t)Upad * Npad * 4);
+                unsigned int *err = (unsigned int *)dmalloc(4);
+                ck(cudaMemsetAsync(err, 0, 4, st), "memset");
+                CUtensorMap ma, mb;
+                tc_operand_map(&ma, Am, Upad, Kpad);
+                tc_operand_map(&mb, Bm, Npad, Kpad);
+                PackSrc ps{{ntf[f * 4 + cs[0]->q], ntf[f * 4 + cs[ncomp > 1 ? 1 : 0]->q]}};
+                for (int m = 0; m < nf; m++) {
+                    const double k = 2 * kPI * P.fntf[m] / vp;
+                    k_tc_pack_phase<<<dim3((B + 127) / 128, Upad), 128, 0, st>>>(
+                        Am, d_s, U, B, Kpad, k, b_off, h[F.b_ax], kind == 1);
+                    k_tc_pack_sums<<<dim3((B + 127) / 128, Npad), 128, 0, st>>>(
+                        Bm, ps, ncomp, A, B, ntfb, ntfb, Nb, n2, m, Kpad);
+                    tc::k_tc_gemm_tf32<<<dim3(Npad / 128, Upad / 128), tc::THREADS, tc::SMEM_BYTES, st>>>(
+                        ma, mb, Cm, Npad, Kpad / tc::BK, err);
+                    for (int ci = 0; ci < ncomp; ci++) {
+                        double2 *o = acc + ((size_t)m * 6 + cs[ci]->vec * 3 + cs[ci]->axis) * ndir;
+                        k_ff_reduce_tc<<<(ndir + 7) / 8, 256, 0, st>>>(o, Cm, Npad, ci * 2 * A, d_umap, d_r[F.a_ax],
+                                                             d_r[F.n_ax], ndir, A, k, a_off, h[F.a_ax],
+                                                             kind == 0, n0, area);
+                    }
+                }
+                unsigned int herr = 0;
+                ck(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st), "D2H");
+                ck(cudaStreamSynchronize(st), "far field");
+                if (herr) throw Error(MFDTD_ETIMEOUT, "far field: a tensor-core GEMM wait ran out");
+                continue;
+            }
             double2 *Pm = (double2 *)dmalloc((size_t)U * B * sizeof(double2));
             double2 *T = (double2 *)dmalloc((size_t)U * A * sizeof(double2));
             for (int m = 0; m < nf; m++) {

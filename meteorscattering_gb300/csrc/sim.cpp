@@ -705,11 +705,11 @@ int mfdtd_sim_far_field(mfdtd_sim *s, int32_t ndir, const double *theta, const d
                         int32_t method, double *out) {
     return guarded([&] {
         if (!s || !theta || !phi || !out || ndir <= 0) throw Error(MFDTD_EINVAL, "bad arguments");
-        if (method != 0) throw Error(MFDTD_EINVAL, "unknown far-field method");
+        if (method != 0 && method != 1) throw Error(MFDTD_EINVAL, "unknown far-field method");
         s->flush();
         std::vector<double> sd = s->source_dft();
         double *const *ntf = s->form == MFDTD_FORM_FP64_PLAIN ? s->pa.ntf : s->f32->ntf_arrays();
-        mfdtd::far_field_fp64(s->P, ntf, sd.data(), ndir, theta, phi, out, s->stream);
+        mfdtd::far_field_fp64(s->P, ntf, sd.data(), ndir, theta, phi, out, s->stream, method);
     });
 }
 
@@ -959,7 +959,7 @@ struct mfdtd_server {
                     m->flush();
                     std::vector<double> sd = m->source_dft();
                     mfdtd::far_field_fp64(m->P, m->f32->ntf_arrays(), sd.data(), nd, j->theta.data(),
-                                          j->phi.data(), j->result.data(), m->stream);
+                                          j->phi.data(), j->result.data(), m->stream, 1);
                     j->sim.reset();
                     std::lock_guard<std::mutex> lk(mu);
                     used -= j->bytes;
