@@ -424,6 +424,36 @@ def population_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def farfield_bench(args):
+    """Far-field projection (bistatic RCS on the 2-degree theta/phi grid,
+    16380 directions) of a 384^3 FP32 simulation advanced 20 steps: method 1
+    (dense stage on the tensor cores) against method 0 (FP64 CUDA cores)."""
+    from meteorscattering_gb300 import build as B
+    B.build()
+    from meteorscattering_gb300 import engine as E
+    from meteorscattering_gb300 import sweep
+    N, dx, f0 = 384, 0.15, 50e6
+    p = rd.RunParams(Nx=N, Ny=N, Nz=N, tsteps=20, dt=rd.stable_dt(dx), f0=f0, fsig=20.0,
+                     gridfactor=(rd.C0 / f0) / dx, numfiles=1, savefields=0, fntf=[f0],
+                     metsize=(1e200, 1e200), doB0=0, probex=[], probey=[], probez=[])
+    pb = E.Problem.from_params(p, np.zeros((N, N)), np.full((N, N), 1e5), (0.0, 0.0, 0.0))
+    sim = E.Simulation(pb, form=E.FORM_FP32_FUSED)
+    sim.advance(20)
+    th, ph = sweep.direction_grid(2.0)
+    times = {}
+    for m in ([1] if args.steps <= 1 else [1, 0, 1]):
+        t0 = time.perf_counter()
+        sim.far_field(th, ph, method=m)
+        times.setdefault(m, []).append(time.perf_counter() - t0)
+    line = {"metric": "far-field projections/s", "value": 1.0 / min(times[1]), "unit": "1/s",
+            "n_gpus": 1, "higher_is_better": True, "dtype": "tf32x3/f64",
+            "config": {"workload": f"{N}^3 FP32 simulation, bistatic RCS at {th.size} directions, "
+                                   "1 frequency"},
+            "ms": {"tensor_cores": 1e3 * min(times[1]),
+                   "fp64_cuda_cores": 1e3 * times[0][0] if 0 in times else None}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,6 +468,9 @@ def main():
     args = ap.parse_args()
     if args.workload in ("sweep", "serve") and args.impl == "gb300":
         population_bench(args)
+        return
+    if args.workload == "farfield" and args.impl == "gb300":
+        farfield_bench(args)
         return
     K, W = args.steps, max(args.warmup, 0)
 

@@ -38,7 +38,7 @@ namespace {
 constexpr int TJ = 8, TK = 32;             // tile rows (j) x columns (k)
 constexpr int EJ = TJ + 2, EK = TK + 8;    // E box: rows j0-1..j0+TJ, cols k0-4..k0+TK+3
 constexpr int HJ = TJ + 1, HK = TK + 4;    // H box: rows j0-1..j0+TJ-1, cols k0-4..k0+TK-1
-constexpr int NS = 4;                      // pipeline stages
+constexpr int NS = 5;                      // pipeline stages
 constexpr int NTHREADS = 320;              // 8 tile warps + halo-row warp + halo-column warp
 constexpr int PROD = NTHREADS - 1;         // producer thread (idle lane of the halo-column warp)
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
@@ -47,7 +47,8 @@ constexpr int STAGE_B = 3 * E_B + 3 * H_B + 3 * J_B;
 constexpr int STAGE_TX = 3 * EJ * EK * 4 + 3 * HJ * HK * 4 + 3 * TJ * TK * 4;  // bytes per stage
 constexpr int HN_COLS = TK + 1;            // new-H plane: cols k0-1..k0+TK-1
 constexpr int HN_B = 3 * HJ * HN_COLS * 4;
-constexpr int SMEM_B = NS * STAGE_B + align128(HN_B) + NS * 8 + 16 + 128;
+// two new-H planes (alternating per x plane), NS stage barriers, two poll flags
+constexpr int SMEM_B = NS * STAGE_B + 2 * align128(HN_B) + NS * 8 + 16 + 128;  // flags: 3 ints
 constexpr double kE0 = 8.85419e-12;
 
 struct Maps {
@@ -558,7 +559,6 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     const int dj = c.dj, dk = c.dk, j = c.j, k = c.k, warp = c.warp;
     const bool tile = warp < TJ;
     const bool valid = c.valid, in_grid = c.in_grid;
-    float *hn = c.hn;
 
     // J method: JM 0 = Young DI, 1 = Lee-Kalluri with one matrix pair for the
     // whole grid (read from the constant bank), 2 = Lee-Kalluri table.
@@ -601,23 +601,30 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     // One thread polls the stage mbarriers; the rest of the CTA sleeps in the
     // CTA barrier instead of spinning.  The poller's mbarrier acquire plus
     // bar.sync make the TMA data visible to every thread.
+    // One CTA barrier per x plane, between the H and the E updates:
+    //   * before it the poller waits for the stage plane q+1's H will read
+    //     (plane q+2's E box);
+    //   * after it every thread has finished plane q-1 (its E update came
+    //     before plane q's H), so the producer refills plane q-1's slot with
+    //     plane q-1+NS, and the new-H plane alternates between two buffers so
+    //     plane q+1's H never overwrites values plane q's E still reads;
+    //   * the poll flag alternates as well, so a fast thread never overwrites
+    //     the flag a slow thread has not read yet.
     volatile int *okflag = (volatile int *)(c.bar + NS);
     auto stage_ready = [&](int qq) {
         return qq > c.q_last || mbar_wait(&c.bar[(qq - c.p0) % NS], ((qq - c.p0) / NS) & 1);
     };
-    if (c.tid == PROD) *okflag = (stage_ready(c.p0) && stage_ready(c.p0 + 1)) ? 1 : 0;
+    if (c.tid == PROD) okflag[2] = (stage_ready(c.p0) && stage_ready(c.p0 + 1)) ? 1 : 0;
     __syncthreads();
-    if (!*okflag) return c.p0;
-    // End of a plane: wait for the stage the next plane needs, release the
-    // CTA, then refill the slot this plane used.
-    auto end_plane = [&](int q) -> bool {
-        if (c.tid == PROD) *okflag = stage_ready(q + 2) ? 1 : 0;
+    if (!okflag[2]) return c.p0;
+    auto mid_plane = [&](int q) -> bool {
+        if (c.tid == PROD) okflag[q & 1] = stage_ready(q + 2) ? 1 : 0;
         __syncthreads();
-        if (!*okflag) return false;
-        if (c.tid == PROD && q + NS <= c.q_last) {
+        if (!okflag[q & 1]) return false;
+        if (c.tid == PROD && q > c.p0 && q - 1 + NS <= c.q_last) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_stage<PAR>(maps, c, q + NS);
-            c.issued = q + NS;
+            issue_stage<PAR>(maps, c, q - 1 + NS);
+            c.issued = q - 1 + NS;
         }
         return true;
     };
@@ -628,8 +635,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         const float cwq = nwq, cnu = nnu, chyx = nhyx, chzx = nhzx, ceyx = neyx, cezx = nezx;
         pf_load(q + 1, nwq, nnu, nhyx, nhzx, neyx, nezx);
         const int slot = (q - c.p0) % NS;
-        // Stages q and q+1 are resident: the end-of-plane barrier of the
-        // previous iteration (or the one before the loop) guarantees it.
+        float *hn = c.hn + (q & 1) * (align128(HN_B) / 4);  // this plane's new-H buffer
+        // Stages q and q+1 are resident: the barrier of the previous plane
+        // (or the one before the loop) guarantees it.
         const Stage s = stage_at(c.smem + slot * STAGE_B);
         const Stage s1 = stage_at(c.smem + ((q + 1 - c.p0) % NS) * STAGE_B);
         const bool real = q >= c.i_begin;
@@ -703,7 +711,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 a.H[PAR ^ 1][1][cg] = hv.y;
                 a.H[PAR ^ 1][2][cg] = hv.z;
             }
-            __syncthreads();
+            if (!mid_plane(q)) return q + 2;
             if (tile) {
                 const float c1 = a.c1e0, c2 = a.c2e0;
                 const float ex = c1 * exo + (a.cey * (hv.z - HN(2, dj - 1, dk)) - a.cez * (hv.y - HN(1, dj, dk - 1))) - c2 * jx;
@@ -719,7 +727,6 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             }
             hy_prev = hv.y;
             hz_prev = hv.z;
-            if (!end_plane(q)) return q + 2;
             continue;
         }
 
@@ -779,7 +786,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             a.H[PAR ^ 1][1][cg] = hv.y;
             a.H[PAR ^ 1][2][cg] = hv.z;
         }
-        __syncthreads();
+        if (!mid_plane(q)) return q + 2;
 
         // ---- E of this plane (tile), source/meteor-2.1.cpp:1020-1374
         if (valid && real) {
@@ -989,7 +996,6 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         }
         hy_prev = hv.y;
         hz_prev = hv.z;
-        if (!end_plane(q)) return q + 2;
     }
     return -1;
 }
@@ -1009,7 +1015,7 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     // TMA destinations must be 128-byte aligned; the launch reserves 128 spare bytes.
     c.smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
     c.hn = (float *)(c.smem + NS * STAGE_B);
-    c.bar = (uint64_t *)(c.smem + NS * STAGE_B + align128(HN_B));
+    c.bar = (uint64_t *)(c.smem + NS * STAGE_B + 2 * align128(HN_B));
 
     c.tid = threadIdx.x;
     c.warp = c.tid >> 5;
@@ -1092,7 +1098,9 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
 // One time step of one simulation: one CTA per (tile, x-chunk).  Boundary
 // tiles (general path, several times the work of an interior tile) are
 // launched first so that they overlap the bulk of the grid instead of forming
-// a tail.
+// a tail.  (Running them as a separate launch with a larger register budget on
+// a second stream was measured slower: the block scheduler dispatches that
+// launch's CTAs ahead of the interior ones, so the two do not overlap.)
 template <int PAR, int JM>
 __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
     k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
@@ -1276,6 +1284,7 @@ struct Fp32Sim::Impl {
     std::vector<int> tile_order;   // host copy: boundary tiles first
     int n_boundary = 0;            // how many of them are boundary tiles
 
+
     template <class T> T *alloc(size_t n, cudaStream_t s) {
         void *p = nullptr;
         size_t b = std::max<size_t>(n, 1) * sizeof(T);
@@ -1444,12 +1453,14 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         }
     for (int c = 0; c < 3; c++) make_map(&m.maps.J[c], a.J[c], P.Nx, P.Ny, P.Nz, m.Nzp, TK, TJ);
 
-    ck(cudaFuncSetAttribute(k_fp32_step<0, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
-    ck(cudaFuncSetAttribute(k_fp32_step<1, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
-    ck(cudaFuncSetAttribute(k_fp32_step<0, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
-    ck(cudaFuncSetAttribute(k_fp32_step<1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
-    ck(cudaFuncSetAttribute(k_fp32_step<0, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
-    ck(cudaFuncSetAttribute(k_fp32_step<1, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    {
+        auto attr = [](const void *f) {
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+        };
+        attr((const void *)k_fp32_step<0, 0>); attr((const void *)k_fp32_step<1, 0>);
+        attr((const void *)k_fp32_step<0, 1>); attr((const void *)k_fp32_step<1, 1>);
+        attr((const void *)k_fp32_step<0, 2>); attr((const void *)k_fp32_step<1, 2>);
+    }
     m.jm = 0;
     if (P.doB0) {
         bool uniform = !P.lk.empty();
@@ -1513,9 +1524,10 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
         else if (m.jm == 1) go(k_fp32_step<1, 1>);
         else go(k_fp32_step<1, 2>);
     }
+    const int launches = 1;
     if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
     m_cur_ ^= 1;
-    return 1;
+    return launches;
 }
 
 void Fp32Sim::check(void *stream) {
