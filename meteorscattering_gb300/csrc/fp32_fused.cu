@@ -300,8 +300,7 @@ __device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
 template <int PAR, bool CLEAN>
 __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int dj, int dk,
                                        const Stage &s, const Stage &s1, bool store_psi,
-                                       bool want_y, bool want_z, bool tf_in, bool use_pf,
-                                       float pf_yx, float pf_zx) {
+                                       bool want_y, bool want_z, bool tf_in) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
     HVal o;
     o.x = s.h[0][HIDX(dj, dk)];
@@ -367,7 +366,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-            const float p = a.tb->Bh[sx] * (use_pf ? pf_yx : a.Ph[PAR][2][o2]) + a.tb->Ahx[sx] * dEz;
+            const float p = a.tb->Bh[sx] * a.Ph[PAR][2][o2] + a.tb->Ahx[sx] * dEz;
             if (store_psi) a.Ph[PAR ^ 1][2][o2] = p;
             h += a.c2h * p;
             if (a.kappa_on) h += a.c2h * (a.tb->Khx[sx] * dEz);
@@ -398,7 +397,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-            const float p = a.tb->Bh[sx] * (use_pf ? pf_zx : a.Ph[PAR][4][o2]) + a.tb->Ahx[sx] * dEy;
+            const float p = a.tb->Bh[sx] * a.Ph[PAR][4][o2] + a.tb->Ahx[sx] * dEy;
             if (store_psi) a.Ph[PAR ^ 1][4][o2] = p;
             h -= a.c2h * p;
             if (a.kappa_on) h -= a.c2h * (a.tb->Khx[sx] * dEy);
@@ -570,33 +569,22 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     const double *ph = a.phase + (size_t)t * nf * 2;
     const size_t col = (size_t)(valid ? j : 0) * a.Nzp + (valid ? k : 0);
 
-    // Per-plane values that live in global memory are prefetched one plane
-    // ahead into registers, so their latency overlaps the previous plane's
-    // work: the plasma weight (and collision frequency) of the thread's (i,j)
-    // column and, inside the x CPML slabs, the four x-normal psi values.
+    // The plasma weight (and collision frequency) of the thread's cell is
+    // prefetched one plane ahead into registers, so its latency overlaps the
+    // previous plane's work.  (Prefetching the x-normal CPML psi the same way
+    // was measured slower: the registers it holds across the plane loop made
+    // the boundary path spill.)
     const int jj = valid ? j : 0, kk = valid ? k : 0;
-    auto pf_load = [&](int qq, float &wq, float &nu, float &hyx, float &hzx, float &eyx, float &ezx) {
+    auto pf_load = [&](int qq, float &wq, float &nu) {
         if (!valid || qq >= Nx) return;
         const size_t ij = (size_t)qq * Ny + jj;
         const size_t cq = (size_t)qq * plane + (size_t)jj * a.Nzp + kk;
         wq = a.wq3 ? a.wq3[cq] : a.wq2[ij];
         if (JM == 0) nu = a.nu3 ? a.nu3[cq] : a.nu2[ij];
-        if (a.dopml) {
-            const int sh = hslab(qq, Nx, L, a.xshift), se = eslab(qq, Nx, L, a.xshift);
-            if (sh >= 0) {
-                const size_t o2 = ((size_t)sh * Ny + jj) * Nz + kk;
-                hyx = a.Ph[PAR][2][o2];
-                hzx = a.Ph[PAR][4][o2];
-            }
-            if (se >= 0) {
-                const size_t o2 = ((size_t)se * Ny + jj) * Nz + kk;
-                eyx = a.Pe[2][o2];
-                ezx = a.Pe[4][o2];
-            }
-        }
+
     };
-    float nwq = 0.f, nnu = 0.f, nhyx = 0.f, nhzx = 0.f, neyx = 0.f, nezx = 0.f;
-    pf_load(c.p0, nwq, nnu, nhyx, nhzx, neyx, nezx);
+    float nwq = 0.f, nnu = 0.f;
+    pf_load(c.p0, nwq, nnu);
 
     // One thread polls the stage mbarriers; the rest of the CTA sleeps in the
     // CTA barrier instead of spinning.  The poller's mbarrier acquire plus
@@ -632,8 +620,8 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
     for (int q = c.p0; q < c.i_end; q++) {
         const int i = q;
-        const float cwq = nwq, cnu = nnu, chyx = nhyx, chzx = nhzx, ceyx = neyx, cezx = nezx;
-        pf_load(q + 1, nwq, nnu, nhyx, nhzx, neyx, nezx);
+        const float cwq = nwq, cnu = nnu;
+        pf_load(q + 1, nwq, nnu);
         const int slot = (q - c.p0) % NS;
         float *hn = c.hn + (q & 1) * (align128(HN_B) / 4);  // this plane's new-H buffer
         // Stages q and q+1 are resident: the barrier of the previous plane
@@ -775,7 +763,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         HVal hv = {0.f, 0.f, 0.f};
         if (in_grid)
             hv = h_cell<PAR, CLEAN>(a, i, j, k, dj, dk, s, s1, tile && real, warp != TJ,
-                                    warp != TJ + 1, tf_in, tile, chyx, chzx);
+                                    warp != TJ + 1, tf_in);
         if (c.role_ok) {
             HN(0, dj, dk) = hv.x;
             if (warp != TJ) HN(1, dj, dk) = hv.y;
@@ -860,7 +848,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                     float p = 0.f;
                     if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
                         const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
-                        p = a.tb->Be[sxe] * ceyx + a.tb->Aex[sxe] * dHz;
+                        p = a.tb->Be[sxe] * a.Pe[2][o2] + a.tb->Aex[sxe] * dHz;
                         a.Pe[2][o2] = p;
                     }
                     e -= a.c2e0 * p;
@@ -905,7 +893,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                     float p = 0.f;
                     if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
                         const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
-                        p = a.tb->Be[sxe] * cezx + a.tb->Aex[sxe] * dHy;
+                        p = a.tb->Be[sxe] * a.Pe[4][o2] + a.tb->Aex[sxe] * dHy;
                         a.Pe[4][o2] = p;
                     }
                     e += a.c2e0 * p;
@@ -1198,20 +1186,14 @@ __global__ void __launch_bounds__(256) k_fp32_scan(const float *__restrict__ ex,
     }
 }
 
-// E0 * omega_p^2 of a parametric trail, FP64 evaluation stored as FP32 in the
-// padded [Nx][Ny][Nzp] layout.
+// E0 * omega_p^2 of a parametric trail in the padded [Nx][Ny][Nzp] layout.
 __global__ void k_trail_wq(TrailDev t, int Nzp, float *out) {
     const size_t n = (size_t)t.Nx * t.Ny * Nzp;
     for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n;
          q += (size_t)gridDim.x * blockDim.x) {
         const int k = (int)(q % Nzp);
         const size_t ij = q / Nzp;
-        float v = 0.f;
-        if (k < t.Nz) {
-            const double wp = trail_wp(t, (int)(ij / t.Ny), (int)(ij % t.Ny), k);
-            v = (float)(kE0 * wp * wp);
-        }
-        out[q] = v;
+        out[q] = k < t.Nz ? trail_wq_f32(t, (int)(ij / t.Ny), (int)(ij % t.Ny), k) : 0.f;
     }
 }
 

@@ -25,6 +25,23 @@ inline TrailDev trail_dev(const Problem &P) {
     return t;
 }
 
+// E0 * omega_p^2 for the FP32 form: geometry in FP64, the density's exp10/exp
+// in FP32 (the map is stored in FP32; FP64 transcendentals are slow here).
+__device__ __forceinline__ float trail_wq_f32(const TrailDev &t, int i, int j, int k) {
+    const double kQE = 1.602177e-19, kE0 = 8.85419e-12, kME = 9.10939e-31;
+    const double x = -(t.Nx - 1) / 2.0 * t.dx + t.dx * i - t.c[0];
+    const double y = -(t.Ny - 1) / 2.0 * t.dy + t.dy * j - t.c[1];
+    const double z = -(t.Nz - 1) / 2.0 * t.dz + t.dz * k - t.c[2];
+    const double s = x * t.a[0] + y * t.a[1] + z * t.a[2];
+    double d2 = x * x + y * y + z * z - s * s;
+    if (d2 < 0) d2 = 0;
+    double f = (s + t.sh) / (2 * t.sh);
+    f = f < 0 ? 0 : (f > 1 ? 1 : f);
+    const float lg = (float)(t.lo + (t.hi - t.lo) * f);
+    const float n = exp10f(lg) * expf((float)(-d2 / (t.r0 * t.r0)));
+    return (float)(kE0 * (kQE * kQE / (kE0 * kME))) * n;  // E0 wp^2 = n QE^2 / ME
+}
+
 __device__ __forceinline__ double trail_wp(const TrailDev &t, int i, int j, int k) {
     const double kQE = 1.602177e-19, kE0 = 8.85419e-12, kME = 9.10939e-31;
     const double x = -(t.Nx - 1) / 2.0 * t.dx + t.dx * i - t.c[0];
