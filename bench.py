@@ -456,6 +456,72 @@ def farfield_bench(args):
     print(json.dumps(line), flush=True)
 
 
+def mie_bench(args, steps: int = 4000, courant: float = 0.5):
+    """Precision check on the 128^3 plasma sphere: homogeneous unmagnetized
+    collisional plasma sphere (radius 2 m, n = 5e13 m^-3, nu = 1e5 1/s),
+    dx = 0.15 m, 10-cell CPML, 4000 steps, a Gaussian-modulated pulse covering
+    30-70 MHz along +x (E along z), RCS at 11 frequencies on the 2-degree
+    theta/phi grid.  Reports, for the FP32 fused form against the FP64 plain
+    form: field relative L2 after the last step and the RCS dB error per
+    angle; for both forms: the backscatter error against the FP64 Mie
+    series (oracle/mie.py; the test-infrastructure oracle is used here as the
+    checker only)."""
+    from meteorscattering_gb300 import build as B
+    B.build()
+    from meteorscattering_gb300 import engine as E
+    from meteorscattering_gb300 import sweep
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import mie
+    N, dx, f0 = 128, 0.15, 50e6
+    dt = rd.stable_dt(dx, courant)
+    freqs = list(np.linspace(30e6, 70e6, 11))
+    p = rd.RunParams(Nx=N, Ny=N, Nz=N, tsteps=steps, dt=dt, f0=f0,
+                     fsig=1 / (2 * math.pi * 15e6 * dt), gridfactor=(rd.C0 / f0) / dx,
+                     numfiles=1, savefields=0, fntf=freqs, metsize=(1e200, 1e200), doB0=0,
+                     probex=[], probey=[], probez=[], sourcepol=1)
+    n_e, nu, R = 5e13, 1e5, 2.0
+    wp3 = rd.plasma_sphere_wp3(N, N, N, dx, R, n_e)
+    th, ph = sweep.direction_grid(2.0)
+    res, fields, times = {}, {}, {}
+    for form in (E.FORM_FP64_PLAIN, E.FORM_FP32_FUSED):
+        pb = E.Problem.from_params(p, np.zeros((N, N)), np.full((N, N), nu), (0.0, 0.0, 0.0))
+        pb.set_ext(rd.ExtParams(exact_coords=1), wp3=wp3)
+        sim = E.Simulation(pb, form=form)
+        t0 = time.perf_counter()
+        sim.advance(steps)
+        sim.sync()
+        times[form] = time.perf_counter() - t0
+        res[form] = sim.far_field(th, ph, method=0)[..., 0]
+        fields[form] = sim.read_field(2)  # Ez after the last step
+        back = sim.far_field(np.array([math.pi / 2]), np.array([math.pi]), method=0)[:, 0, 0]
+        res[(form, "back")] = back
+        sim.close()
+    s64, s32 = res[E.FORM_FP64_PLAIN], res[E.FORM_FP32_FUSED]
+    mask = s64 > s64.max(axis=1, keepdims=True) * 1e-3
+    db = np.abs(10 * np.log10(s32 / s64))
+    want = mie.sphere_backscatter(freqs, R, mie.plasma_eps(freqs, float(rd.plasma_frequency(n_e)), nu))
+    mie64 = 10 * np.log10(res[(E.FORM_FP64_PLAIN, "back")] / want)
+    mie32 = 10 * np.log10(res[(E.FORM_FP32_FUSED, "back")] / want)
+    e64, e32 = fields[E.FORM_FP64_PLAIN].ravel(), fields[E.FORM_FP32_FUSED].ravel()
+    line = {"metric": "RCS error vs FP64 plain and vs Mie", "value": float(db[mask].max()),
+            "unit": "dB (FP32 vs FP64, max over angles within 30 dB of the peak)",
+            "higher_is_better": False, "n_gpus": 1, "steps": steps, "dtype": "f32 vs f64",
+            "data": "synthetic",
+            "config": {"workload": "128^3 plasma sphere r=2 m n=5e13 nu=1e5, dx=0.15 m, "
+                                   "10-cell CPML, 30-70 MHz pulse along +x, 11 frequencies, "
+                                   "2-degree theta/phi grid",
+                       "dt_s": dt, "courant": courant},
+            "fp32_vs_fp64": {"field_rel_l2_Ez_final": float(np.linalg.norm(e32 - e64) / np.linalg.norm(e64)),
+                             "rcs_db_max": float(db[mask].max()),
+                             "rcs_db_p99": float(np.percentile(db[mask], 99)),
+                             "rcs_db_max_per_freq": [float(db[m][mask[m]].max()) for m in range(len(freqs))]},
+            "vs_mie_backscatter_db": {"freqs_mhz": [f / 1e6 for f in freqs],
+                                      "fp64_plain": [float(v) for v in mie64],
+                                      "fp32_fused": [float(v) for v in mie32]},
+            "seconds": {"fp64_plain": times[E.FORM_FP64_PLAIN], "fp32_fused": times[E.FORM_FP32_FUSED]}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -473,6 +539,9 @@ def main():
         return
     if args.workload == "farfield" and args.impl == "gb300":
         farfield_bench(args)
+        return
+    if args.workload == "mie" and args.impl == "gb300":
+        mie_bench(args)
         return
     K, W = args.steps, max(args.warmup, 0)
 
