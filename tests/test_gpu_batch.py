@@ -8,6 +8,12 @@ the surface and the run) to 1e-6 relative L2, the probe series (point values)
 to 2e-5 (measured 5.8e-6 after 200 steps).  Members of different sizes and
 step counts share the batch; one joins at an odd tick; one finishes early and
 idles while the rest continue.
+
+The non-cubic member is a 52 x 56 x 64 magnetized trail.  (The golden
+"rect" case is 52 x 52 x 40: with the default 10-cell TF/SF gap its box is
+empty along z, so no incident field enters and its FP32 fields are only the
+rounding residue of the two coinciding face corrections, about 1e-9; a
+relative comparison of two such residues says nothing.)
 """
 import dataclasses
 import os
@@ -37,6 +43,11 @@ def _long(name, steps):
     return dataclasses.replace(p, dt=rd.stable_dt(p.dx, 0.9), tsteps=steps, numfiles=1), wp, nu, B0
 
 
+def _noncubic(steps):
+    p, wp, nu, B0 = golden_cases._mk(N=(52, 56, 64), doB0=1)
+    return dataclasses.replace(p, dt=rd.stable_dt(p.dx, 0.9), tsteps=steps, numfiles=1), wp, nu, B0
+
+
 def _alone(pb):
     s = E.Simulation(pb, form=E.FORM_FP32_FUSED)
     s.advance(s.dims[3])
@@ -46,7 +57,7 @@ def _alone(pb):
 
 
 def test_batch_members_match_their_single_runs(built):
-    cases = [_long("lk_trail", 240), _long("rect", 200), _long("lk_numap", 240)]
+    cases = [_long("lk_trail", 240), _noncubic(200), _long("lk_numap", 240)]
     pbs = [_problem(c) for c in cases]
     want = [_alone(pb) for pb in pbs]
     b = E.Batch()
@@ -55,7 +66,7 @@ def test_batch_members_match_their_single_runs(built):
     b.add(sims[1])
     b.run(7)                    # the third member joins at an odd tick
     b.add(sims[2])
-    b.run(240)                  # rect finishes at 200 and idles
+    b.run(240)                  # the non-cubic member finishes at 200 and idles
     b.sync()
     for s, c, (ntf, prb) in zip(sims, cases, want):
         assert s.step_index == c[0].tsteps
