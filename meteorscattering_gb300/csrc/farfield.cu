@@ -29,7 +29,6 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
-#include <map>
 #include <vector>
 
 #include "common.hpp"
@@ -201,7 +200,13 @@ __global__ void k_tc_pack_sums(float *Bm, PackSrc ps, int ncomp, int A, int B, i
 
 // Stage 2 reading stage 1 from the FP32 GEMM tile: T[u][a] = (C[u][col0 + 2a],
 // C[u][col0 + 2a + 1]).  One warp per direction (faces are a few hundred cells
-// wide), FP64 accumulation, FP32-evaluated phases.
+// wide).  Lane l takes a = l, l + 32, ...: its first phase and the phase step
+// of 32 cells are reduced in FP64 once, and the phasor then advances by FP32
+// complex rotation (a dozen steps on a face of a few hundred cells, about 1e-6
+// rad of drift, the order of the stage-1 split's own error).  The terms are
+// FP32 like the stage-1 result they weight; lanes combine in FP64.  (FP64
+// arithmetic per term ran at this part's reduced FP64 rate: 0.24 ms a
+// launch on a 384^3 grid at 16,380 directions.)
 __global__ void __launch_bounds__(256) k_ff_reduce_tc(double2 *out, const float *C, int ldc, int col0,
                                                       const int *umap, const double *ra, const double *rn,
                                                       int D, int A, double k, double a_off, double ha,
@@ -210,15 +215,20 @@ __global__ void __launch_bounds__(256) k_ff_reduce_tc(double2 *out, const float 
     if (d >= D) return;
     const float2 *row = (const float2 *)(C + (size_t)umap[d] * ldc + col0);
     const double kr = -k * ra[d];
-    double re = 0, im = 0;
+    float sn, cs, sd, cd;
+    sincos_reduced(kr * ((lane + a_off) * ha), &sn, &cs);
+    sincos_reduced(kr * (32.0 * ha), &sd, &cd);
+    float fre = 0.f, fim = 0.f;
     for (int a = lane; a < A; a += 32) {
-        float sn, cs;
-        sincos_reduced(kr * ((a + a_off) * ha), &sn, &cs);
-        const double w = (halve_ends && (a == 0 || a == A - 1)) ? 0.5 : 1.0;
+        const float w = (halve_ends && (a == 0 || a == A - 1)) ? 0.5f : 1.0f;
         const float2 t = row[a];
-        re += w * ((double)cs * t.x - (double)sn * t.y);
-        im += w * ((double)cs * t.y + (double)sn * t.x);
+        fre += w * (cs * t.x - sn * t.y);
+        fim += w * (cs * t.y + sn * t.x);
+        const float cn = cs * cd - sn * sd;
+        sn = sn * cd + cs * sd;
+        cs = cn;
     }
+    double re = fre, im = fim;
     for (int off = 16; off > 0; off >>= 1) {
         re += __shfl_down_sync(0xffffffffu, re, off);
         im += __shfl_down_sync(0xffffffffu, im, off);
@@ -317,25 +327,39 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
     // accumulators [freq][vec][axis][dir]
     double2 *acc = (double2 *)dmalloc((size_t)nf * 6 * ndir * sizeof(double2));
     ck(cudaMemsetAsync(acc, 0, (size_t)nf * 6 * ndir * sizeof(double2), st), "memset");
+    // tensor-core GEMM timeout flag (method 1), read once after every launch
+    unsigned int *err = (unsigned int *)dmalloc(4);
+    ck(cudaMemsetAsync(err, 0, 4, st), "memset");
+
+    // Distinct direction cosines along each axis (u), and the map d -> u.
+    // Stage 1 runs over u only: on a regular theta/phi grid far fewer values
+    // than directions.  Faces whose in-plane b axis is the same share them.
+    std::vector<double> svals[3];
+    std::vector<int> umaps[3];
+    double *d_sv[3];
+    int *d_um[3];
+    for (int ax = 0; ax < 3; ax++) {
+        std::vector<int> order(ndir);
+        for (int d = 0; d < ndir; d++) order[d] = d;
+        std::sort(order.begin(), order.end(), [&](int x, int y) { return r[ax][x] < r[ax][y]; });
+        umaps[ax].resize(ndir);
+        for (int q = 0; q < ndir; q++) {
+            const double v = r[ax][order[q]];
+            if (svals[ax].empty() || v != svals[ax].back()) svals[ax].push_back(v);
+            umaps[ax][order[q]] = (int)svals[ax].size() - 1;
+        }
+        d_sv[ax] = (double *)dmalloc(svals[ax].size() * 8);
+        d_um[ax] = (int *)dmalloc(ndir * 4);
+        ck(cudaMemcpyAsync(d_sv[ax], svals[ax].data(), svals[ax].size() * 8, cudaMemcpyHostToDevice, st), "H2D");
+        ck(cudaMemcpyAsync(d_um[ax], umaps[ax].data(), ndir * 4, cudaMemcpyHostToDevice, st), "H2D");
+    }
 
     for (int f = 0; f < 6; f++) {
         const FaceDesc &F = kFaces[f];
         const int Na = dims[F.a_ax], Nb = dims[F.b_ax];
-        // distinct direction cosines along b, and the map d -> u
-        std::map<double, int> uniq;
-        std::vector<int> umap(ndir);
-        for (int d = 0; d < ndir; d++) {
-            auto it = uniq.find(r[F.b_ax][d]);
-            if (it == uniq.end()) it = uniq.emplace(r[F.b_ax][d], (int)uniq.size()).first;
-            umap[d] = it->second;
-        }
-        std::vector<double> svals(uniq.size());
-        for (auto &kv : uniq) svals[kv.second] = kv.first;
-        const int U = (int)svals.size();
-        double *d_s = (double *)dmalloc(U * 8);
-        int *d_umap = (int *)dmalloc(ndir * 4);
-        ck(cudaMemcpyAsync(d_s, svals.data(), U * 8, cudaMemcpyHostToDevice, st), "H2D");
-        ck(cudaMemcpyAsync(d_umap, umap.data(), ndir * 4, cudaMemcpyHostToDevice, st), "H2D");
+        const int U = (int)svals[F.b_ax].size();
+        const double *d_s = d_sv[F.b_ax];
+        const int *d_umap = d_um[F.b_ax];
         const double n0 = (F.high ? dims[F.n_ax] - ntfb : ntfb) * h[F.n_ax];
         const double area = h[F.a_ax] * h[F.b_ax];
         // trims (analysis/meteorNTF.m:66-196): type A keeps a in [ntfb, Na-ntfb]
@@ -359,8 +383,6 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
                 float *Am = (float *)dmalloc((size_t)Upad * Kpad * 4);
                 float *Bm = (float *)dmalloc((size_t)Npad * Kpad * 4);
                 float *Cm = (float *)dmalloc((size_t)Upad * Npad * 4);
-                unsigned int *err = (unsigned int *)dmalloc(4);
-                ck(cudaMemsetAsync(err, 0, 4, st), "memset");
                 CUtensorMap ma, mb;
                 tc_operand_map(&ma, Am, Upad, Kpad);
                 tc_operand_map(&mb, Bm, Npad, Kpad);
@@ -380,10 +402,11 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
                                                              kind == 0, n0, area);
                     }
                 }
-                unsigned int herr = 0;
-                ck(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st), "D2H");
-                ck(cudaStreamSynchronize(st), "far field");
-                if (herr) throw Error(MFDTD_ETIMEOUT, "far field: a tensor-core GEMM wait ran out");
+                // this kind's operands go back to the stream-ordered pool for the next face
+                for (void *q : {(void *)Am, (void *)Bm, (void *)Cm}) {
+                    ck(cudaFreeAsync(q, st), "cudaFreeAsync");
+                    tmp.erase(std::find(tmp.begin(), tmp.end(), q));
+                }
                 continue;
             }
             double2 *Pm = (double2 *)dmalloc((size_t)U * B * sizeof(double2));
@@ -406,9 +429,12 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
         }
     }
     std::vector<double2> h_acc((size_t)nf * 6 * ndir);
+    unsigned int herr = 0;
     ck(cudaMemcpyAsync(h_acc.data(), acc, h_acc.size() * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st), "D2H");
     for (void *p : tmp) ck(cudaFreeAsync(p, st), "cudaFreeAsync");
     ck(cudaStreamSynchronize(st), "far field");
+    if (herr) throw Error(MFDTD_ETIMEOUT, "far field: a tensor-core GEMM wait ran out");
 
     // sigma: analysis/meteorNTF.m:311-332, generalised to (theta, phi)
     const double *Eydft = srcdft, *Ezdft = srcdft + 2 * nf;

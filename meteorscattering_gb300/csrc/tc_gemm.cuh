@@ -11,6 +11,8 @@
 //     mbarrier once the MMAs that read it have completed;
 //   * after the last commit, the four warps read their 32 TMEM lanes (rows)
 //     with tcgen05.ld and store the tile.
+// Two CTAs share an SM (3 stages, 128 of the SM's 512 TMEM columns each), so
+// one CTA's MMAs overlap the other's epilogue and set-up.
 // Every wait is bounded (2 s of %globaltimer); on expiry the CTA sets *err,
 // waits (bounded) for the copies and MMAs it issued, frees its TMEM and returns.
 //
@@ -28,7 +30,7 @@ namespace mfdtd {
 namespace tc {
 
 constexpr int BM = 128, BN = 128, BK = 32;          // tile; BK fp32 = one 128-byte row
-constexpr int NSTAGE = 4;
+constexpr int NSTAGE = 3;                           // 3 x 32 KB: two CTAs fit on one SM
 constexpr int TILE_B = BM * BK * 4;                 // 16 KB per operand tile
 constexpr int STAGE_BYTES = 2 * TILE_B;             // A + B
 constexpr int SMEM_BYTES = NSTAGE * STAGE_BYTES + 1024 /* alignment */ + 256 /* barriers */;
@@ -86,7 +88,7 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
 constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BN >> 3) << 17) |
                             ((uint32_t)(BM >> 4) << 24);
 
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS, 2)
     k_tc_gemm_tf32(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                    float *__restrict__ C, int ldc, int nk, unsigned int *err) {
     extern __shared__ __align__(1024) unsigned char raw[];
@@ -122,7 +124,6 @@ __global__ void __launch_bounds__(THREADS, 1)
     __syncthreads();
 
     int issued = 0;     // TMA stages issued (producer)
-    int committed = 0;  // K chunks whose MMAs were committed (MMA thread)
     if (tid == 0) {
         // producer
         for (int kc = 0; kc < nk; kc++) {
@@ -172,7 +173,6 @@ __global__ void __launch_bounds__(THREADS, 1)
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                              smem_addr(&empty[s]))
                          : "memory");
-            committed = kc + 1;
         }
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_addr(done))
@@ -189,7 +189,6 @@ __global__ void __launch_bounds__(THREADS, 1)
                 while (!bar_test(&full[kc % NSTAGE], (kc / NSTAGE) & 1) && gtimer() - t0 < 200000000ull) {
                 }
             }
-        (void)committed;
     } else {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         // warp w owns TMEM lanes 32w..32w+31 = rows m0 + 32w + lane
