@@ -203,8 +203,9 @@ __global__ void k_tc_pack_sums(float *Bm, PackSrc ps, int ncomp, int A, int B, i
 // wide).  Lane l takes a = l, l + 32, ...: its first phase and the phase step
 // of 32 cells are reduced in FP64 once, and the phasor then advances by FP32
 // complex rotation (a dozen steps on a face of a few hundred cells, about 1e-6
-// rad of drift, the order of the stage-1 split's own error).  The terms are
-// FP32 like the stage-1 result they weight; lanes combine in FP64.  (FP64
+// rad of drift, the order of the stage-1 split's own error).  The terms and
+// the lanes' partial sums are FP32 like the stage-1 result they weight; the
+// face factor is applied in FP64.  (FP64
 // arithmetic per term ran at this part's reduced FP64 rate: 0.24 ms a
 // launch on a 384^3 grid at 16,380 directions.)
 __global__ void __launch_bounds__(256) k_ff_reduce_tc(double2 *out, const float *C, int ldc, int col0,
@@ -228,17 +229,41 @@ __global__ void __launch_bounds__(256) k_ff_reduce_tc(double2 *out, const float 
         sn = sn * cd + cs * sd;
         cs = cn;
     }
-    double re = fre, im = fim;
     for (int off = 16; off > 0; off >>= 1) {
-        re += __shfl_down_sync(0xffffffffu, re, off);
-        im += __shfl_down_sync(0xffffffffu, im, off);
+        fre += __shfl_down_sync(0xffffffffu, fre, off);
+        fim += __shfl_down_sync(0xffffffffu, fim, off);
     }
+    const double re = fre, im = fim;
     if (lane == 0) {
         float sn, cs;
         sincos_reduced(-k * rn[d] * n0, &sn, &cs);
         out[d].x += area * ((double)cs * re - (double)sn * im);
         out[d].y += area * ((double)cs * im + (double)sn * re);
     }
+}
+
+// sigma of every direction from the six accumulated vector potentials (L, N
+// along x, y, z, each `stride` directions apart), analysis/meteorNTF.m:311-332
+// generalised to (theta, phi); c = k^2 / (8 pi eta0) / P_inc.
+__global__ void k_ff_sigma(const double2 *acc, size_t stride, const double *th, const double *ph, int n,
+                           double c, double eta0, double *sig) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= n) return;
+    auto g = [&](int q) { return acc[(size_t)q * stride + d]; };
+    const double2 Lx = g(0), Ly = g(1), Lz = g(2), Nx = g(3), Ny = g(4), Nz = g(5);
+    double stt, ct, sp, cp;
+    sincos(th[d], &stt, &ct);
+    sincos(ph[d], &sp, &cp);
+    const double Lthr = Lx.x * ct * cp + Ly.x * ct * sp - Lz.x * stt, Lthi = Lx.y * ct * cp + Ly.y * ct * sp - Lz.y * stt;
+    const double Lphr = -Lx.x * sp + Ly.x * cp, Lphi = -Lx.y * sp + Ly.y * cp;
+    const double Nthr = Nx.x * ct * cp + Ny.x * ct * sp - Nz.x * stt, Nthi = Nx.y * ct * cp + Ny.y * ct * sp - Nz.y * stt;
+    const double Nphr = -Nx.x * sp + Ny.x * cp, Nphi = -Nx.y * sp + Ny.y * cp;
+    const double ar = Lphr + eta0 * Nthr, ai = Lphi + eta0 * Nthi;
+    const double br = Lthr - eta0 * Nphr, bi = Lthi - eta0 * Nphi;
+    const double sa = c * (ar * ar + ai * ai), sb = c * (br * br + bi * bi);
+    sig[3 * d] = sa + sb;
+    sig[3 * d + 1] = sa;
+    sig[3 * d + 2] = sb;
 }
 
 using EncodeFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
@@ -428,41 +453,27 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
             }
         }
     }
-    std::vector<double2> h_acc((size_t)nf * 6 * ndir);
-    unsigned int herr = 0;
-    ck(cudaMemcpyAsync(h_acc.data(), acc, h_acc.size() * sizeof(double2), cudaMemcpyDeviceToHost, st), "D2H");
-    ck(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st), "D2H");
-    for (void *p : tmp) ck(cudaFreeAsync(p, st), "cudaFreeAsync");
-    ck(cudaStreamSynchronize(st), "far field");
-    if (herr) throw Error(MFDTD_ETIMEOUT, "far field: a tensor-core GEMM wait ran out");
-
-    // sigma: analysis/meteorNTF.m:311-332, generalised to (theta, phi)
+    // sigma on the device: analysis/meteorNTF.m:311-332, generalised to (theta, phi)
+    double *d_th = (double *)dmalloc(ndir * 8), *d_ph = (double *)dmalloc(ndir * 8);
+    double *d_sig = (double *)dmalloc((size_t)nf * ndir * 3 * 8);
+    ck(cudaMemcpyAsync(d_th, theta, ndir * 8, cudaMemcpyHostToDevice, st), "H2D");
+    ck(cudaMemcpyAsync(d_ph, phi, ndir * 8, cudaMemcpyHostToDevice, st), "H2D");
     const double *Eydft = srcdft, *Ezdft = srcdft + 2 * nf;
     for (int m = 0; m < nf; m++) {
         const double k = 2 * kPI * P.fntf[m] / vp;
         const double ezr = Ezdft[2 * m + 1], ezi = Ezdft[2 * m];
         const double eyr = Eydft[2 * m + 1], eyi = Eydft[2 * m];
         const double Pinc = (ezr * ezr + ezi * ezi + eyr * eyr + eyi * eyi) / 2 / eta0;
-        const double c = k * k / (8 * kPI * eta0) / Pinc;
-        for (int d = 0; d < ndir; d++) {
-            auto g = [&](int vec, int ax) { return h_acc[((size_t)m * 6 + vec * 3 + ax) * ndir + d]; };
-            const double ct = std::cos(theta[d]), stt = std::sin(theta[d]);
-            const double cp = std::cos(phi[d]), sp = std::sin(phi[d]);
-            double2 Lx = g(0, 0), Ly = g(0, 1), Lz = g(0, 2), Nx = g(1, 0), Ny = g(1, 1), Nz = g(1, 2);
-            auto th = [&](double2 X, double2 Y, double2 Z) {
-                return make_double2(X.x * ct * cp + Y.x * ct * sp - Z.x * stt, X.y * ct * cp + Y.y * ct * sp - Z.y * stt);
-            };
-            auto phf = [&](double2 X, double2 Y) { return make_double2(-X.x * sp + Y.x * cp, -X.y * sp + Y.y * cp); };
-            const double2 Lth = th(Lx, Ly, Lz), Lph = phf(Lx, Ly), Nth = th(Nx, Ny, Nz), Nph = phf(Nx, Ny);
-            const double ar = Lph.x + eta0 * Nth.x, ai = Lph.y + eta0 * Nth.y;
-            const double br = Lth.x - eta0 * Nph.x, bi = Lth.y - eta0 * Nph.y;
-            const double sa = c * (ar * ar + ai * ai), sb = c * (br * br + bi * bi);
-            double *o = out + ((size_t)m * ndir + d) * 3;
-            o[0] = sa + sb;
-            o[1] = sa;
-            o[2] = sb;
-        }
+        k_ff_sigma<<<(ndir + 127) / 128, 128, 0, st>>>(acc + (size_t)m * 6 * ndir, ndir, d_th, d_ph, ndir,
+                                                       k * k / (8 * kPI * eta0) / Pinc, eta0,
+                                                       d_sig + (size_t)m * ndir * 3);
     }
+    unsigned int herr = 0;
+    ck(cudaMemcpyAsync(out, d_sig, (size_t)nf * ndir * 3 * 8, cudaMemcpyDeviceToHost, st), "D2H");
+    ck(cudaMemcpyAsync(&herr, err, 4, cudaMemcpyDeviceToHost, st), "D2H");
+    for (void *p : tmp) ck(cudaFreeAsync(p, st), "cudaFreeAsync");
+    ck(cudaStreamSynchronize(st), "far field");
+    if (herr) throw Error(MFDTD_ETIMEOUT, "far field: a tensor-core GEMM wait ran out");
 }
 
 }  // namespace mfdtd
@@ -553,26 +564,6 @@ __global__ void k_ff_dirs(const double *th, const double *ph, int n, double *rx,
 }
 
 // sigma and its two polarisation terms from the L, N accumulators of n directions.
-__global__ void k_ff_sigma(const double2 *acc, const double *th, const double *ph, int n, double c,
-                           double eta0, double *sig) {
-    const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= n) return;
-    auto g = [&](int q) { return acc[(size_t)q * kStaticDirs + d]; };
-    const double2 Lx = g(0), Ly = g(1), Lz = g(2), Nx = g(3), Ny = g(4), Nz = g(5);
-    double stt, ct, sp, cp;
-    sincos(th[d], &stt, &ct);
-    sincos(ph[d], &sp, &cp);
-    const double Lthr = Lx.x * ct * cp + Ly.x * ct * sp - Lz.x * stt, Lthi = Lx.y * ct * cp + Ly.y * ct * sp - Lz.y * stt;
-    const double Lphr = -Lx.x * sp + Ly.x * cp, Lphi = -Lx.y * sp + Ly.y * cp;
-    const double Nthr = Nx.x * ct * cp + Ny.x * ct * sp - Nz.x * stt, Nthi = Nx.y * ct * cp + Ny.y * ct * sp - Nz.y * stt;
-    const double Nphr = -Nx.x * sp + Ny.x * cp, Nphi = -Nx.y * sp + Ny.y * cp;
-    const double ar = Lphr + eta0 * Nthr, ai = Lphi + eta0 * Nthi;
-    const double br = Lthr - eta0 * Nphr, bi = Lthi - eta0 * Nphi;
-    const double sa = c * (ar * ar + ai * ai), sb = c * (br * br + bi * bi);
-    sig[3 * d] = sa + sb;
-    sig[3 * d + 1] = sa;
-    sig[3 * d + 2] = sb;
-}
 
 }  // namespace
 }  // namespace mfdtd
@@ -632,7 +623,7 @@ extern "C" int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t N
                 const double ezr = srcdft[2 * nntf + 2 * m + 1], ezi = srcdft[2 * nntf + 2 * m];
                 const double eyr = srcdft[2 * m + 1], eyi = srcdft[2 * m];
                 const double Pinc = (ezr * ezr + ezi * ezi + eyr * eyr + eyi * eyi) / 2 / eta0;
-                k_ff_sigma<<<(nd + 127) / 128, 128, 0, st>>>(sc.acc, sc.th, sc.ph, nd,
+                k_ff_sigma<<<(nd + 127) / 128, 128, 0, st>>>(sc.acc, kStaticDirs, sc.th, sc.ph, nd,
                                                              k * k / (8 * kPI * eta0) / Pinc, eta0, sc.sig);
                 ck(cudaMemcpyAsync(out + ((size_t)m * ndir + d0) * 3, sc.sig, (size_t)nd * 3 * sizeof(double),
                                    cudaMemcpyDeviceToHost, st),
