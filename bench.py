@@ -491,7 +491,14 @@ def mie_bench(args, steps: int = 4000, courant: float = 0.5):
         sim.advance(steps)
         sim.sync()
         times[form] = time.perf_counter() - t0
+        t1 = time.perf_counter()
         res[form] = sim.far_field(th, ph, method=0)[..., 0]
+        times[(form, "ff0")] = time.perf_counter() - t1
+        if form == E.FORM_FP32_FUSED:   # the same projection on the tensor cores
+            sim.far_field(th, ph, method=1)
+            t1 = time.perf_counter()
+            res["tc"] = sim.far_field(th, ph, method=1)[..., 0]
+            times["ff1"] = time.perf_counter() - t1
         fields[form] = sim.read_field(2)  # Ez after the last step
         back = sim.far_field(np.array([math.pi / 2]), np.array([math.pi]), method=0)[:, 0, 0]
         res[(form, "back")] = back
@@ -518,7 +525,11 @@ def mie_bench(args, steps: int = 4000, courant: float = 0.5):
             "vs_mie_backscatter_db": {"freqs_mhz": [f / 1e6 for f in freqs],
                                       "fp64_plain": [float(v) for v in mie64],
                                       "fp32_fused": [float(v) for v in mie32]},
-            "seconds": {"fp64_plain": times[E.FORM_FP64_PLAIN], "fp32_fused": times[E.FORM_FP32_FUSED]}}
+            "seconds": {"fp64_plain": times[E.FORM_FP64_PLAIN], "fp32_fused": times[E.FORM_FP32_FUSED]},
+            "far_field": {"ms_fp64": 1e3 * times[(E.FORM_FP32_FUSED, "ff0")],
+                          "ms_tensor_cores": 1e3 * times["ff1"],
+                          "max_db_tensor_cores_vs_fp64": float(
+                              np.abs(10 * np.log10(res["tc"] / s32))[s32 > s32.max(axis=1, keepdims=True) * 1e-3].max())}}
     print(json.dumps(line), flush=True)
 
 

@@ -35,7 +35,8 @@ typedef enum {
     MFDTD_ENOMEM = -4,   /* device or host allocation failed / over the limit  */
     MFDTD_ETIMEOUT = -5, /* a bounded wait ran out                             */
     MFDTD_ENUMERIC = -6, /* NaN/Inf detected by the field guard                */
-    MFDTD_ESTATE = -7    /* call not valid in the handle's current state        */
+    MFDTD_ESTATE = -7,   /* call not valid in the handle's current state        */
+    MFDTD_ECANCELED = -8 /* the job was canceled (mfdtd_server_cancel)          */
 } mfdtd_status;
 
 /* Arithmetic form of the time stepping. */
@@ -307,6 +308,13 @@ int mfdtd_server_poll(mfdtd_server *s, int64_t job_id, int32_t wait_ms, double *
                       double times[3], int32_t *done);
 /* out[0..4] = submitted, queued, running, retired, device bytes in use. */
 int mfdtd_server_stats(mfdtd_server *s, int64_t out[5]);
+/* Cancel a job.  A queued job leaves the queue at once; a running job leaves
+ * its batch at the end of the worker's current round, without a far field,
+ * and its device memory returns to the cap; a finished job's result is
+ * discarded.  Polling a canceled job then fails with MFDTD_ECANCELED and
+ * releases it (a finished job is released here).  MFDTD_EINVAL for an
+ * unknown id. */
+int mfdtd_server_cancel(mfdtd_server *s, int64_t job_id);
 
 /* ---- errors ---------------------------------------------------------------- */
 /* Copy the last error message of the calling thread into buf (NUL-terminated). */

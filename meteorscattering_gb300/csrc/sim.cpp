@@ -851,6 +851,7 @@ struct ServerJob {
     int kind = -1;                 // current-update kind (batch key)
     double t_submit = 0, t_admit = 0, t_done = 0;
     int state = 0;                 // 0 queued, 1 running, 2 retired, 3 failed
+    bool cancel = false;           // leave at the end of the current round
     int code = 0;
     std::string err;
     std::vector<double> result;
@@ -944,12 +945,18 @@ struct mfdtd_server {
             std::vector<ServerJob *> still;
             for (ServerJob *j : running) {
                 mfdtd_sim *m = j->sim.get();
-                if (j->code == 0 && m->t < m->P.tsteps) {
+                bool cancel;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    cancel = j->cancel;
+                }
+                if (j->code == 0 && !cancel && m->t < m->P.tsteps) {
                     still.push_back(j);
                     continue;
                 }
                 try {
                     if (j->code) throw Error(j->code, j->err);
+                    if (cancel) throw Error(MFDTD_ECANCELED, "canceled");
                     mfdtd_batch *b = m->batch;
                     b->fb->remove(m->f32.get());
                     b->members.erase(std::find(b->members.begin(), b->members.end(), m));
@@ -1091,6 +1098,32 @@ int mfdtd_server_poll(mfdtd_server *s, int64_t job_id, int32_t wait_ms, double *
             times[2] = 0;
         }
         s->jobs.erase(it);
+    });
+}
+
+int mfdtd_server_cancel(mfdtd_server *s, int64_t job_id) {
+    return guarded([&] {
+        if (!s) throw Error(MFDTD_EINVAL, "bad arguments");
+        std::lock_guard<std::mutex> lk(s->mu);
+        auto it = s->jobs.find(job_id);
+        if (it == s->jobs.end()) throw Error(MFDTD_EINVAL, "unknown job id");
+        ServerJob *j = it->second.get();
+        if (j->state >= 2) {  // finished: drop the result
+            s->jobs.erase(it);
+            return;
+        }
+        auto q = std::find(s->queued.begin(), s->queued.end(), j);
+        if (q != s->queued.end()) {  // never admitted: no device memory held
+            s->queued.erase(q);
+            j->state = 3;
+            j->code = MFDTD_ECANCELED;
+            j->err = "canceled";
+            j->t_done = mfdtd::wall_s();
+            s->cv_done.notify_all();
+            return;
+        }
+        j->cancel = true;  // admitted: the worker retires it after this round
+        s->cv_work.notify_all();
     });
 }
 

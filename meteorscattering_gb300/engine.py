@@ -23,7 +23,7 @@ FORM_FP64_PLAIN = 0
 FORM_FP32_FUSED = 1
 
 STATUS = {0: "OK", -1: "EINVAL", -2: "EIO", -3: "ECUDA", -4: "ENOMEM", -5: "ETIMEOUT",
-          -6: "ENUMERIC", -7: "ESTATE"}
+          -6: "ENUMERIC", -7: "ESTATE", -8: "ECANCELED"}
 
 # Every entry point declared in include/mfdtd.h.
 EXPORTS = (
@@ -38,6 +38,7 @@ EXPORTS = (
     "mfdtd_batch_create", "mfdtd_batch_destroy", "mfdtd_batch_add", "mfdtd_batch_remove",
     "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune", "mfdtd_server_create",
     "mfdtd_server_destroy", "mfdtd_server_submit", "mfdtd_server_poll", "mfdtd_server_stats",
+    "mfdtd_server_cancel",
 )
 
 
@@ -137,6 +138,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_server_submit": (C.c_int, [vp, vp, i32, dp, dp, C.POINTER(i64)]),
         "mfdtd_server_poll": (C.c_int, [vp, i64, i32, dp, i64, dp, C.POINTER(i32)]),
         "mfdtd_server_stats": (C.c_int, [vp, C.POINTER(i64)]),
+        "mfdtd_server_cancel": (C.c_int, [vp, i64]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -433,16 +435,26 @@ class Server:
 
     def poll(self, job_id: int, wait_ms: int = 0):
         """(done, sigma[nntf, ndir, 3] or None, (to_admission_s, to_done_s))."""
-        nf, nd = self._nf[job_id]
+        nf, nd = self._nf.get(job_id, (0, 0))   # a canceled job has no result
         out = np.empty((nf, nd, 3), dtype=np.float64)
         times = np.zeros(3)
         done = C.c_int32()
-        _check(load_library().mfdtd_server_poll(self._h, job_id, wait_ms, _dp(out), out.size,
-                                                _dp(times), C.byref(done)))
+        try:
+            _check(load_library().mfdtd_server_poll(self._h, job_id, wait_ms, _dp(out), out.size,
+                                                    _dp(times), C.byref(done)))
+        except MfdtdError:
+            self._nf.pop(job_id, None)   # the native record is released with the error
+            raise
         if not done.value:
             return False, None, None
-        del self._nf[job_id]
+        self._nf.pop(job_id, None)
         return True, out, (times[0], times[1])
+
+    def cancel(self, job_id: int) -> None:
+        """Cancel a queued or running job (or drop a finished one's result).
+        Polling a canceled job raises MfdtdError with code ECANCELED."""
+        _check(load_library().mfdtd_server_cancel(self._h, job_id))
+        self._nf.pop(job_id, None)
 
     def stats(self):
         out = (C.c_int64 * 5)()

@@ -7,6 +7,7 @@
   sigma is within 30 dB of its peak.
 * The device memory of admitted jobs never exceeds the cap.
 * A job larger than the cap is refused at submission.
+* Queued and running jobs can be canceled.
 """
 import time
 
@@ -91,3 +92,39 @@ def test_oversize_job_is_refused(built):
         srv.submit(job.problem(E), th, ph)
     assert E.STATUS[ei.value.code] == "ENOMEM"
     srv.close()
+
+
+def test_cancel_queued_and_running_jobs(built):
+    """With room for one job at a time: a canceled queued job fails its poll
+    with ECANCELED at once; a canceled running job leaves its batch after the
+    current round and its memory admits the next job, which completes with
+    the same cross sections as its stand-alone run; an unknown id is EINVAL."""
+    th, ph = sweep.direction_grid(30.0)
+    jobs = _jobs(3, 3000, seed=11)
+    one = max(E.Problem.footprint(j.problem(E), E.FORM_FP32_FUSED) for j in jobs)
+    srv = E.Server(hbm_cap_bytes=int(one * 1.5), steps_per_round=10)
+    a, b, c = (srv.submit(j.problem(E), th, ph) for j in jobs)
+    deadline = time.time() + 60
+    while srv.stats()["running"] < 1 and time.time() < deadline:
+        time.sleep(0.005)
+    assert srv.stats()["running"] == 1 and srv.stats()["queued"] == 2
+    srv.cancel(c)                       # queued
+    with pytest.raises(E.MfdtdError) as ei:
+        srv.poll(c, 0)
+    assert E.STATUS[ei.value.code] == "ECANCELED"
+    srv.cancel(a)                       # running
+    with pytest.raises(E.MfdtdError) as ei:
+        srv.poll(a, 10000)
+    assert E.STATUS[ei.value.code] == "ECANCELED"
+    done, sig = False, None
+    while not done and time.time() < deadline + 120:
+        done, sig, _ = srv.poll(b, 100)
+    assert done
+    st = srv.stats()
+    assert st["device_bytes"] == 0 and st["running"] == 0 and st["queued"] == 0
+    with pytest.raises(E.MfdtdError) as ei:
+        srv.cancel(12345)
+    assert E.STATUS[ei.value.code] == "EINVAL"
+    srv.close()
+    want = _standalone(jobs[1], E.FORM_FP32_FUSED, th, ph, method=1)[..., 0]
+    assert np.max(np.abs(sig[..., 0] - want) / np.maximum(want, 1e-300)) < 1e-5
