@@ -614,7 +614,10 @@ def main():
                 "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom[1],
                 "traffic": traffic_per_launch(args.form, args.workload, dom[0], alg),
-                "kernel_times_ms": {n: m for n, m, c in kstats}}
+                "kernel_times_ms": {n: m for n, m, c in kstats},
+                # the same compulsory bytes over the whole step (every kernel of it)
+                "step_achieved": alg / (ms_step * 1e-3) / 1e9,
+                "step_frac": alg / (ms_step * 1e-3) / 1e9 / peak}
 
     # end to end through the public API from host buffers
     e2e = None

@@ -85,6 +85,10 @@ struct Args {
     // oblique incidence: auxiliary line (E in inc[][1], H in inc[][2])
     int oblique, M, ashift, lk_colocated;
     float kr[3], s0, ke[3], kh[3], chl, cel;   // chl = c2h/dl, cel = c2e0/dl
+    // Work done inside the step kernel (1) or by the kernels that follow it
+    // (0): the running DFT on the Huygens surface (k_fp32_ntf), the oblique
+    // TF/SF corrections (k_fp32_tfsf).  A batch keeps both inside.
+    int ntf_inline, obl_inline;
     // state
     float *E[2][3], *H[2][3], *J[3];
     float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
@@ -281,9 +285,12 @@ __device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
     bool c = a.doplate == 0;
     c = c && jlo >= L + 1 && jhi <= Ny - L - 2 && klo >= L + 1 && khi <= Nz - L - 2;
     c = c && jlo >= 1 && jhi <= Ny - 2 && klo >= 1 && khi <= Nz - 2;
-    const int sy[6] = {a.by1 - 1, a.by1, a.by2 - 1, a.by2, a.ntfb, Ny - a.ntfb};
-    const int sz[6] = {a.bz1 - 1, a.bz1, a.bz2 - 1, a.bz2, a.ntfb, Nz - a.ntfb};
-    for (int q = 0; q < 6; q++) c = c && !hits(jlo, jhi, sy[q]) && !hits(klo, khi, sz[q]);
+    auto clear = [&](int vy, int vz) { return !hits(jlo, jhi, vy) && !hits(klo, khi, vz); };
+    if (!a.oblique || a.obl_inline)  // TF/SF rows, when the corrections are made here
+        c = c && clear(a.by1 - 1, a.bz1 - 1) && clear(a.by1, a.bz1) && clear(a.by2 - 1, a.bz2 - 1) &&
+            clear(a.by2, a.bz2);
+    if (a.ntf_inline)  // Huygens rows, when the DFT is accumulated here
+        c = c && clear(a.ntfb, a.ntfb) && clear(Ny - a.ntfb, Nz - a.ntfb);
     // slices are written on record steps only
     c = c && !(record && (hits(jlo, jhi, a.ssy) || hits(klo, khi, a.ssz)));
     ti.clean = c;
@@ -328,7 +335,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                     if (k == a.bz1 - 1) h -= a.chz * eyi;
                     if (k == a.bz2 - 1) h += a.chz * eyi;
                 }
-            } else if (obl_shell(a, i, j, k)) {
+            } else if (a.obl_inline && obl_shell(a, i, j, k)) {
                 h += obl_corr<PAR, false, 0>(a, i, j, k);
             }
             if (a.dopml) {
@@ -361,7 +368,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                 if (i == a.bx1 - 1) h -= a.chx * a.inc[PAR][1][a.bx1];
                 if (i == a.bx2 - 1) h += a.chx * a.inc[PAR][1][a.bx2 - 1];
             }
-        } else if (obl_shell(a, i, j, k)) {
+        } else if (a.obl_inline && obl_shell(a, i, j, k)) {
             h += obl_corr<PAR, false, 1>(a, i, j, k);
         }
         if (sx >= 0) {
@@ -392,7 +399,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                 if (i == a.bx1 - 1) h += a.chx * a.inc[PAR][0][a.bx1];
                 if (i == a.bx2 - 1) h -= a.chx * a.inc[PAR][0][a.bx2 - 1];
             }
-        } else if (obl_shell(a, i, j, k)) {
+        } else if (a.obl_inline && obl_shell(a, i, j, k)) {
             h += obl_corr<PAR, false, 2>(a, i, j, k);
         }
         if (sx >= 0) {
@@ -633,12 +640,15 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
         // Interior fast path: a clean tile on a plane outside the x CPML slabs
         // and away from every x-special plane (TF/SF faces when the tile is in
-        // the box, NTF faces, the x slice on record steps).  No conditionals
+        // the box and the corrections are made here, NTF faces when the DFT
+        // is accumulated here, the x slice on record steps).  No conditionals
         // per cell; the arithmetic is the same as the general path's.
         const int xlo = a.dopml ? L + 1 : 1, xhi = a.dopml ? Nx - L - 2 : Nx - 2;
-        const bool fast = CLEAN && real && i >= xlo && i <= xhi && i != a.ntfb && i != Nx - a.ntfb &&
-                          !(record && i == a.ssx) &&
-                          !(tf_in && (i == a.bx1 - 1 || i == a.bx1 || i == a.bx2 - 1));
+        const bool x_tfsf = (!a.oblique || a.obl_inline) && tf_in &&
+                            (i == a.bx1 - 1 || i == a.bx1 || i == a.bx2 - 1);
+        const bool x_ntf = a.ntf_inline && (i == a.ntfb || i == Nx - a.ntfb);
+        const bool fast = CLEAN && real && i >= xlo && i <= xhi && !x_ntf && !(record && i == a.ssx) &&
+                          !x_tfsf;
         if (fast) {
             float jx = 0.f, jy = 0.f, jz = 0.f, exo = 0.f, eyo = 0.f, ezo = 0.f;
             if (tile) {
@@ -799,7 +809,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
                 if (!CLEAN) {
                     if (a.oblique) {
-                        if (obl_shell(a, i, j, k)) e += obl_corr<PAR, true, 0>(a, i, j, k);
+                        if (a.obl_inline && obl_shell(a, i, j, k)) e += obl_corr<PAR, true, 0>(a, i, j, k);
                     } else if (i >= a.bx1 && i < a.bx2 - 1) {
                         if (inby) {
                             if (k == a.bz1) e += a.cez * hyinc_new<PAR>(a, i);
@@ -841,7 +851,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
                         if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
                     }
-                } else if (obl_shell(a, i, j, k)) {
+                } else if (a.obl_inline && obl_shell(a, i, j, k)) {
                     e += obl_corr<PAR, true, 1>(a, i, j, k);
                 }
                 if (sxe >= 0) {
@@ -884,7 +894,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                         if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
                         if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
                     }
-                } else if (obl_shell(a, i, j, k)) {
+                } else if (a.obl_inline && obl_shell(a, i, j, k)) {
                     e += obl_corr<PAR, true, 2>(a, i, j, k);
                 }
                 if (ez_plate) e = 0.f;
@@ -926,7 +936,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             const bool fr = i == nb, bk = i == Nx - nb;
             const bool tp = !CLEAN && j == Ny - nb, bt = !CLEAN && j == nb;
             const bool lf = !CLEAN && k == nb, rt = !CLEAN && k == Nz - nb;
-            if (fr || bk || tp || bt || lf || rt) {
+            if (a.ntf_inline && (fr || bk || tp || bt || lf || rt)) {
                 const size_t n2 = 2 * (size_t)nf;
                 if (fr || bk) {
                     const size_t base = ((size_t)j * Nz + k) * n2;
@@ -1143,6 +1153,164 @@ __global__ void k_batch_advance(int *job_t, const int *job_end, int njobs, int *
     if (j == 0) *next = 0;
 }
 
+// ---------------------------------------------------------------------------
+// The running DFT on the Huygens surface as a kernel of its own (single
+// simulations): one thread per face cell of the six faces, reading the state
+// pass t wrote (set `cur`) -- E at the face node, H averaged over the face
+// node and the one behind it -- with the FP64 accumulation of the step
+// kernel's inline form (source/meteor-2.1.cpp:942-992, 1386-1438).  Taking
+// the sums' read-modify-writes out of the step kernel takes their latency off
+// the plane loop of the tiles that hold a face.
+// Face cells q0, q0 + dq, ... of the six faces (x faces, then y, then z).
+__device__ __forceinline__ void ntf_cells(const Args &a, int t, int cur, size_t q0, size_t dq) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, nb = a.ntfb, nf = a.nntf;
+    const size_t fx = (size_t)Ny * Nz, fy = (size_t)Nx * Nz, fz = (size_t)Nx * Ny;
+    const size_t total = 2 * (fx + fy + fz), n2 = 2 * (size_t)nf;
+    const size_t sJ = a.Nzp, sI = (size_t)Ny * a.Nzp;
+    const double *ph = a.phase + (size_t)t * nf * 2;
+    const float *E0 = a.E[cur][0], *E1 = a.E[cur][1], *E2 = a.E[cur][2];
+    const float *H0 = a.H[cur][0], *H1 = a.H[cur][1], *H2 = a.H[cur][2];
+    for (size_t q = q0; q < total; q += dq) {
+        size_t r = q;
+        if (r < 2 * fx) {  // x faces: front (i = nb), back (i = Nx - nb); r = j * Nz + k
+            const bool back = r >= fx;
+            if (back) r -= fx;
+            const int i = back ? Nx - nb : nb, j = (int)(r / Nz), k = (int)(r % Nz);
+            const size_t c = i * sI + j * sJ + k, base = r * n2;
+            const double hz = 0.5 * ((double)H2[c] + H2[c - sI]), hy = 0.5 * ((double)H1[c] + H1[c - sI]);
+            const float ey = E1[c], ez = E2[c];
+            if (!back) { acc2(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
+            else { acc2(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
+            continue;
+        }
+        r -= 2 * fx;
+        if (r < 2 * fy) {  // y faces: top (j = Ny - nb), bottom (j = nb); r = i * Nz + k
+            const bool bottom = r >= fy;
+            if (bottom) r -= fy;
+            const int j = bottom ? nb : Ny - nb, i = (int)(r / Nz), k = (int)(r % Nz);
+            const size_t c = i * sI + j * sJ + k, base = r * n2;
+            const double hz = 0.5 * ((double)H2[c] + H2[c - sJ]), hx = 0.5 * ((double)H0[c] + H0[c - sJ]);
+            const float ex = E0[c], ez = E2[c];
+            if (!bottom) { acc2(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
+            else { acc2(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
+            continue;
+        }
+        r -= 2 * fy;  // z faces: left (k = nb), right (k = Nz - nb); r = i * Ny + j
+        const bool right = r >= fz;
+        if (right) r -= fz;
+        const int k = right ? Nz - nb : nb, i = (int)(r / Ny), j = (int)(r % Ny);
+        const size_t c = i * sI + j * sJ + k, base = r * n2;
+        const double hy = 0.5 * ((double)H1[c] + H1[c - 1]), hx = 0.5 * ((double)H0[c] + H0[c - 1]);
+        const float ex = E0[c], ey = E1[c];
+        if (!right) { acc2(a.ntf[18], a.ntf[19], base, hy, -hx, ph, nf); acc2(a.ntf[16], a.ntf[17], base, -(double)ey, ex, ph, nf); }
+        else { acc2(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
+    }
+}
+__global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a, int t, int cur) {
+    ntf_cells(a, t, cur, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
+// The oblique TF/SF corrections as a pass of their own (single simulations
+// without a plate or a conducting sphere).  The step kernel updated H and E
+// of pass PAR without them.  They are linear in the fields' update, so each
+// cell of the band around the TF/SF surface adds here its H correction dH,
+// and to E its own correction plus the curl of the neighbouring dH with the
+// E update's coefficients -- what the inline form adds, up to rounding.  The
+// band is every cell of [b1-1, b2]^3 with a coordinate in {b1-1, b1, b2-1, b2}
+// (each enumerated once), which holds every node a correction reaches; with
+// tfsf_gap >= 2 it lies outside the CPML slabs, so no psi term is involved.
+// The line values are the ones of the pass's start (set PAR; the pass wrote
+// the next line into the other set).  On record steps the slice entries of
+// band cells get the same increments.
+template <int PAR>
+__device__ __forceinline__ void tfsf_band(const Args &a, int record, size_t q0, size_t dq) {
+    const int bx1 = a.bx1, bx2 = a.bx2, by1 = a.by1, by2 = a.by2, bz1 = a.bz1, bz2 = a.bz2;
+    const int Jr = by2 - by1 + 2, Kr = bz2 - bz1 + 2, Ir2 = bx2 - bx1 - 2, Jr2 = by2 - by1 - 2;
+    const size_t nX = 4 * (size_t)Jr * Kr, nY = 4 * (size_t)Ir2 * Kr, nZ = 4 * (size_t)Ir2 * Jr2;
+    const size_t plane = (size_t)a.Ny * a.Nzp;
+    auto pick = [](int b1, int b2, int s) { return s == 0 ? b1 - 1 : s == 1 ? b1 : s == 2 ? b2 - 1 : b2; };
+    for (size_t q = q0; q < nX + nY + nZ; q += dq) {
+        int i, j, k;
+        if (q < nX) {
+            const size_t r = q % ((size_t)Jr * Kr);
+            i = pick(bx1, bx2, (int)(q / ((size_t)Jr * Kr)));
+            j = by1 - 1 + (int)(r / Kr);
+            k = bz1 - 1 + (int)(r % Kr);
+        } else if (q < nX + nY) {
+            const size_t r0 = q - nX, r = r0 % ((size_t)Ir2 * Kr);
+            j = pick(by1, by2, (int)(r0 / ((size_t)Ir2 * Kr)));
+            i = bx1 + 1 + (int)(r / Kr);
+            k = bz1 - 1 + (int)(r % Kr);
+        } else {
+            const size_t r0 = q - nX - nY, r = r0 % ((size_t)Ir2 * Jr2);
+            k = pick(bz1, bz2, (int)(r0 / ((size_t)Ir2 * Jr2)));
+            i = bx1 + 1 + (int)(r / Jr2);
+            j = by1 + 1 + (int)(r % Jr2);
+        }
+        const float hx = obl_corr<PAR, false, 0>(a, i, j, k), hy = obl_corr<PAR, false, 1>(a, i, j, k),
+                    hz = obl_corr<PAR, false, 2>(a, i, j, k);
+        const float ex = a.cey * (hz - obl_corr<PAR, false, 2>(a, i, j - 1, k)) -
+                         a.cez * (hy - obl_corr<PAR, false, 1>(a, i, j, k - 1)) + obl_corr<PAR, true, 0>(a, i, j, k);
+        const float ey = a.cez * (hx - obl_corr<PAR, false, 0>(a, i, j, k - 1)) -
+                         a.cex * (hz - obl_corr<PAR, false, 2>(a, i - 1, j, k)) + obl_corr<PAR, true, 1>(a, i, j, k);
+        const float ez = a.cex * (hy - obl_corr<PAR, false, 1>(a, i - 1, j, k)) -
+                         a.cey * (hx - obl_corr<PAR, false, 0>(a, i, j - 1, k)) + obl_corr<PAR, true, 2>(a, i, j, k);
+        const size_t c = (size_t)i * plane + (size_t)j * a.Nzp + k;
+        if (hx != 0.f) a.H[PAR ^ 1][0][c] += hx;
+        if (hy != 0.f) a.H[PAR ^ 1][1][c] += hy;
+        if (hz != 0.f) a.H[PAR ^ 1][2][c] += hz;
+        if (ex != 0.f) a.E[PAR ^ 1][0][c] += ex;
+        if (ey != 0.f) a.E[PAR ^ 1][1][c] += ey;
+        if (ez != 0.f) a.E[PAR ^ 1][2][c] += ez;
+        if (record) {  // slices written by the pass (source/meteor-2.1.cpp:996-1013, 1322-1340)
+            const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
+            const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
+            if (k == a.ssz) {
+                a.slE[oz + (size_t)i * Ny + j] += ey;
+                a.slE[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] += ez;
+                if (j < Ny - 1) {
+                    a.slH[oz + (size_t)i * Ny + j] += hy;
+                    a.slH[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] += hz;
+                }
+            }
+            if (j == a.ssy) {
+                a.slE[oy + (size_t)i * Nz + k] += ey;
+                a.slE[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] += ez;
+                if (k < Nz - 1) {
+                    a.slH[oy + (size_t)i * Nz + k] += hy;
+                    a.slH[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] += hz;
+                }
+            }
+            if (i == a.ssx) {
+                a.slE[ox + (size_t)j * Nz + k] += ey;
+                a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] += ez;
+                if (j < Ny - 1 && k < Nz - 1) {
+                    a.slH[ox + (size_t)j * Nz + k] += hy;
+                    a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] += hz;
+                }
+            }
+        }
+    }
+}
+template <int PAR>
+__global__ void __launch_bounds__(256) k_fp32_tfsf(const __grid_constant__ Args a, int record) {
+    tfsf_band<PAR>(a, record, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+}
+
+// The same follow-up work for every member of a batch after its tick's pass
+// PAR (no record steps in a batch): grid row y = the member's slot.  Empty,
+// removed and finished slots (t >= end) return at once.
+template <int PAR>
+__global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_t, const int *__restrict__ job_end) {
+    const int q = blockIdx.y;
+    const int t = job_t[q];
+    if (t >= job_end[q]) return;
+    const Args &a = c_jobs[q];
+    const size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, dq = (size_t)gridDim.x * blockDim.x;
+    if (a.oblique && !a.obl_inline) tfsf_band<PAR>(a, 0, q0, dq);
+    if (!a.ntf_inline && a.nntf > 0) ntf_cells(a, t, PAR ^ 1, q0, dq);
+}
+
 // E probes of the final step (the per-step ones ride in the next pass).
 __global__ void k_fp32_flush(const Args a, int t_last, int par) {
     const int p = threadIdx.x;
@@ -1263,6 +1431,7 @@ struct Fp32Sim::Impl {
     size_t dtmp_len = 0;
     unsigned int *scan = nullptr;  // [0] max|Ex| bits, [1] bad flag
     int jm = 0;  // J method of the kernel variant
+    int sms = 148;                 // SM count (grids of the follow-up kernels)
     std::vector<int> tile_order;   // host copy: boundary tiles first
     int n_boundary = 0;            // how many of them are boundary tiles
 
@@ -1327,6 +1496,11 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     a.kappa_on = P.kappa_on;
     a.oblique = P.oblique;
     a.lk_colocated = P.ext.lk_colocated;
+    // A single simulation runs the DFT and (without a plate or sphere, whose
+    // per-cell coefficients the follow-up pass does not carry) the oblique
+    // TF/SF corrections as kernels of their own after each pass.
+    a.ntf_inline = 0;
+    a.obl_inline = (P.oblique && P.doplate != 0) ? 1 : 0;
     Tables T;
     std::memset(&T, 0, sizeof T);
     if (P.oblique) {
@@ -1455,6 +1629,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    m.sms = sms;
     const int tiles = (m.Nzp / TK) * ((P.Ny + TJ - 1) / TJ);
     const int want = sms * 2 * 8;
     int chunks = std::max(1, std::min(P.Nx / 16 > 0 ? P.Nx / 16 : 1, (want + tiles - 1) / tiles));
@@ -1474,7 +1649,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                           khi <= P.Nz - Lc - 2 && jlo >= 1 && jhi <= P.Ny - 2 && klo >= 1 && khi <= P.Nz - 2;
                 const int sy[6] = {P.by1 - 1, P.by1, P.by2 - 1, P.by2, P.ntfb, P.Ny - P.ntfb};
                 const int sz[6] = {P.bz1 - 1, P.bz1, P.bz2 - 1, P.bz2, P.ntfb, P.Nz - P.ntfb};
-                for (int q = 0; q < 6; q++) cl = cl && !hits(jlo, jhi, sy[q]) && !hits(klo, khi, sz[q]);
+                const int q0 = (a.oblique && !a.obl_inline) ? 4 : 0, q1 = a.ntf_inline ? 6 : 4;
+                for (int q = q0; q < q1; q++) cl = cl && !hits(jlo, jhi, sy[q]) && !hits(klo, khi, sz[q]);
                 (cl ? later : order).push_back(ty * ntk + tk);
             }
         m.n_boundary = (int)order.size();
@@ -1486,9 +1662,11 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     bytes_ = m.bytes;
 }
 
-int Fp32Sim::kernel_classes() { return 1; }
+int Fp32Sim::kernel_classes() { return 3; }
 int Fp32Sim::current_update() const { return impl_->jm; }
-const char *Fp32Sim::kernel_name(int) { return "k_fp32_step"; }
+const char *Fp32Sim::kernel_name(int which) {
+    return which == 0 ? "k_fp32_step" : which == 1 ? "k_fp32_tfsf" : "k_fp32_ntf";
+}
 
 int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     cudaStream_t s = (cudaStream_t)stream;
@@ -1506,8 +1684,19 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
         else if (m.jm == 1) go(k_fp32_step<1, 1>);
         else go(k_fp32_step<1, 2>);
     }
-    const int launches = 1;
+    int launches = 1;
     if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
+    if (m.a.oblique && !m.a.obl_inline) {
+        if (m_cur_ == 0) k_fp32_tfsf<0><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
+        else k_fp32_tfsf<1><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
+        launches++;
+    }
+    if (ev) cudaEventRecord((cudaEvent_t)ev[2], s);
+    if (!m.a.ntf_inline && m.a.nntf > 0) {
+        k_fp32_ntf<<<m.sms * 8, 256, 0, s>>>(m.a, t, m_cur_ ^ 1);
+        launches++;
+    }
+    if (ev) cudaEventRecord((cudaEvent_t)ev[3], s);
     m_cur_ ^= 1;
     return launches;
 }
@@ -1601,6 +1790,14 @@ double *const *Fp32Sim::ntf_arrays() const { return impl_->a.ntf; }
 // ---------------------------------------------------------------------------
 // Batch of FP32 simulations advanced by the persistent kernel.
 
+// A member's Args in the batch: its own, with the batch's slab depth.  The
+// follow-up work (DFT, oblique TF/SF corrections) is k_batch_post's.
+static Args batch_args(const Args &a0, int chunk) {
+    Args a = a0;
+    if (chunk > 0) a.chunk = chunk;
+    return a;
+}
+
 struct Fp32Batch::Impl {
     int device = 0, sms = 148, jm = -1;
     cudaStream_t stream = nullptr;
@@ -1679,7 +1876,8 @@ int Fp32Batch::add(Fp32Sim *sim, int t0) {
     // The state is all zeros in both sets, so the simulation can take the
     // parity of the current tick.
     sim->m_cur_ = (int)(b.tick & 1);
-    ck(cudaMemcpyToSymbolAsync(c_jobs, &m.a, sizeof(Args), sizeof(Args) * s, cudaMemcpyHostToDevice, b.stream),
+    const Args ba = batch_args(m.a, 0);
+    ck(cudaMemcpyToSymbolAsync(c_jobs, &ba, sizeof(Args), sizeof(Args) * s, cudaMemcpyHostToDevice, b.stream),
        "cudaMemcpyToSymbol");
     ck(cudaMemcpyAsync(b.d_maps + s, &m.maps, sizeof(Maps), cudaMemcpyHostToDevice, b.stream), "H2D");
     int zero = 0, end = m.tsteps;
@@ -1752,8 +1950,7 @@ static void apply_chunk(Fp32Batch::Impl &b) {
     for (int q = 0; q < kMaxBatch; q++) {
         Fp32Sim *sim = b.slot[q];
         if (!sim) continue;
-        Args a = sim->impl()->a;
-        if (b.chunk > 0) a.chunk = b.chunk;
+        const Args a = batch_args(sim->impl()->a, b.chunk);
         ck(cudaMemcpyToSymbolAsync(c_jobs, &a, sizeof(Args), sizeof(Args) * q, cudaMemcpyHostToDevice,
                                    b.stream), "cudaMemcpyToSymbol");
     }
@@ -1773,6 +1970,9 @@ static void launch_tick(Fp32Batch::Impl &b, int par) {
         else if (b.jm == 1) go(k_fp32_batch<1, 1>);
         else go(k_fp32_batch<1, 2>);
     }
+    const dim3 pgrid(b.sms, kMaxBatch);
+    if (par == 0) k_batch_post<0><<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);
+    else k_batch_post<1><<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);
     k_batch_advance<<<1, kMaxBatch, 0, b.stream>>>(b.d_t, b.d_end, kMaxBatch, b.d_next);
 }
 
@@ -1797,13 +1997,14 @@ int Fp32Batch::run(int nticks) {
     int launches = 0;
     int done = 0;
     // A tick of odd parity first, so that the graph (even, odd) starts even.
-    if (b.tick & 1) { launch_tick(b, 1); b.tick++; done++; launches += 2; }
+    constexpr int kPerTick = 3;  // batched pass, follow-up work, advance
+    if (b.tick & 1) { launch_tick(b, 1); b.tick++; done++; launches += kPerTick; }
     if (nticks - done >= 2) ensure_graph(b);
     while (nticks - done >= 2) {
         ck(cudaGraphLaunch(b.graph, b.stream), "cudaGraphLaunch");
-        b.tick += 2; done += 2; launches += 4;
+        b.tick += 2; done += 2; launches += 2 * kPerTick;
     }
-    if (done < nticks) { launch_tick(b, (int)(b.tick & 1)); b.tick++; done++; launches += 2; }
+    if (done < nticks) { launch_tick(b, (int)(b.tick & 1)); b.tick++; done++; launches += kPerTick; }
     ck(cudaGetLastError(), "batch launch");
     for (int q = 0; q < kMaxBatch; q++)
         if (b.slot[q]) {
