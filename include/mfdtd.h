@@ -200,6 +200,14 @@ int mfdtd_sim_read_ntf(mfdtd_sim *s, double *out, int64_t n);
 int mfdtd_sim_read_probes(mfdtd_sim *s, double *out, int64_t n);
 /* One field component as [Nx][Ny][Nz] doubles: comp 0..8 = Ex,Ey,Ez,Hx,Hy,Hz,Jx,Jy,Jz. */
 int mfdtd_sim_read_field(mfdtd_sim *s, int32_t comp, double *out, int64_t n);
+/* The record slices of the current state, computed on the device: E and H
+ * each hold n >= 2*(Nx*Ny + Nx*Nz + Ny*Nz) doubles in the layout of one
+ * output_E.dat / output_H.dat record without its incident arrays
+ * (source/meteor-2.1.cpp:996-1013, 1322-1340; Ez is the updated value).  With
+ * scattered != 0 the incident field is subtracted inside the total-field
+ * region, exactly where the TF/SF corrections put it -- the scattered field
+ * analysis/plotMresults.m:210-234 forms on the host for its movies. */
+int mfdtd_sim_read_slices(mfdtd_sim *s, int32_t scattered, double *E, double *H, int64_t n);
 /* Write output_{E,H,J}.dat (collected records), output_NTF.dat, Probe.dat
  * and the log.txt record lines into `dir`. */
 int mfdtd_sim_write_outputs(mfdtd_sim *s, const char *dir);

@@ -128,6 +128,9 @@ struct PlainArgs {
 int plain_launch_step(const PlainArgs &a, int t, int record, void *stream, void *const *ev);
 int plain_launch_flush(const PlainArgs &a, int t_last, void *stream);
 int plain_launch_emax(const PlainArgs &a, void *stream);
+// Slices of the current state (record layout) into device E[n], H[n], with the
+// incident field subtracted inside the total-field region when `scattered`.
+int plain_launch_slices(const PlainArgs &a, int scattered, double *E, double *H, void *stream);
 int plain_launch_guard(const PlainArgs &a, void *stream);
 
 // omega_p of a parametric trail at every cell, [Nx][Ny][Nz] doubles

@@ -27,6 +27,11 @@ public:
     void read_ntf(int q, double *out, void *stream);
     void read_probes(double *out, void *stream);
     void read_field(int comp, double *out, void *stream);
+    // Slices of the current state in the record layout (E and H blocks of
+    // the host arrays E[n], H[n]), minus the incident field inside the
+    // total-field region when `scattered`; the oblique geometry in FP64.
+    void read_slices(int scattered, double *E, double *H, const double kr[3], double s0,
+                     const double ke[3], const double kh[3], void *stream);
     // Throws if a kernel set the device error flag (a bounded wait ran out).
     void check(void *stream);
     // Device pointers of the 24 DFT arrays (output_NTF.dat order).

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "fp32.hpp"
+#include "incident.cuh"
 #include "trail.cuh"
 
 namespace mfdtd {
@@ -1311,6 +1312,29 @@ __global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_
     if (!a.ntf_inline && a.nntf > 0) ntf_cells(a, t, PAR ^ 1, q0, dq);
 }
 
+// Slices of the current state (set `cur`) in the record layout, E block
+// (is_h = 0) or H block, optionally minus the incident field inside the
+// total-field region.
+__global__ void k_fp32_slices(const __grid_constant__ Args a, IncidentWave<float> w, int cur, int is_h,
+                              int scattered, double *out, size_t n) {
+    const size_t plane = (size_t)a.Ny * a.Nzp;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        SliceCell c;
+        double v = 0.0;
+        if (slice_cell_of(q, a.Nx, a.Ny, a.Nz, a.ssx, a.ssy, a.ssz, is_h != 0, &c)) {
+            const size_t x = (size_t)c.i * plane + (size_t)c.j * a.Nzp + c.k;
+            if (is_h) {
+                v = (double)a.H[cur][1 + c.comp][x];
+                if (scattered) v -= w.h(1 + c.comp, c.i, c.j, c.k);
+            } else {
+                v = (double)a.E[cur][1 + c.comp][x];
+                if (scattered) v -= w.e(1 + c.comp, c.i, c.j, c.k);
+            }
+        }
+        out[q] = v;
+    }
+}
+
 // E probes of the final step (the per-step ones ride in the next pass).
 __global__ void k_fp32_flush(const Args a, int t_last, int par) {
     const int p = threadIdx.x;
@@ -1764,6 +1788,29 @@ void Fp32Sim::read_ntf(int q, double *out, void *stream) {
     const size_t nf2 = 2 * (size_t)m.nntf;
     const size_t n = q < 8 ? (size_t)m.Ny * m.Nz * nf2 : q < 16 ? (size_t)m.Nx * m.Nz * nf2 : (size_t)m.Nx * m.Ny * nf2;
     ck(cudaMemcpyAsync(out, m.a.ntf[q], n * 8, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "D2H");
+}
+
+void Fp32Sim::read_slices(int scattered, double *E, double *H, const double kr[3], double s0,
+                          const double ke[3], const double kh[3], void *stream) {
+    cudaStream_t s = (cudaStream_t)stream;
+    Impl &m = *impl_;
+    const int cur = m_cur_;
+    const Args &a = m.a;
+    IncidentWave<float> w{};
+    w.oblique = a.oblique;
+    w.b1[0] = a.bx1; w.b1[1] = a.by1; w.b1[2] = a.bz1;
+    w.b2[0] = a.bx2; w.b2[1] = a.by2; w.b2[2] = a.bz2;
+    w.ey = a.inc[cur][0]; w.ez = a.inc[cur][1]; w.hy = a.inc[cur][2]; w.hz = a.inc[cur][3];
+    w.eline = a.inc[cur][1]; w.hline = a.inc[cur][2];  // the auxiliary line's E and H (oblique)
+    for (int d = 0; d < 3; d++) { w.kr[d] = kr[d]; w.ke[d] = ke[d]; w.kh[d] = kh[d]; }
+    w.s0 = s0;
+    const size_t n = m.slice_len;
+    k_fp32_slices<<<m.sms * 4, 256, 0, s>>>(m.a, w, cur, 0, scattered, m.dtmp, n);
+    ck(cudaMemcpyAsync(E, m.dtmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
+    k_fp32_slices<<<m.sms * 4, 256, 0, s>>>(m.a, w, cur, 1, scattered, m.dtmp, n);
+    ck(cudaMemcpyAsync(H, m.dtmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    ck(cudaStreamSynchronize(s), "sync");
 }
 
 void Fp32Sim::read_probes(double *out, void *stream) {

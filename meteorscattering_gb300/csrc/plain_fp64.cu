@@ -24,6 +24,7 @@
 #include <cuda_runtime.h>
 
 #include "common.hpp"
+#include "incident.cuh"
 #include "trail.cuh"
 
 namespace mfdtd {
@@ -690,6 +691,40 @@ int plain_launch_step(const PlainArgs &a, int t, int record, void *stream, void 
 int plain_launch_flush(const PlainArgs &a, int t_last, void *stream) {
     if (a.nprobes <= 0) return 0;
     k_plain_flush<<<1, ((a.nprobes + 31) / 32) * 32, 0, (cudaStream_t)stream>>>(a, t_last);
+    return 1;
+}
+
+// Slices of the current state in the record layout, optionally with the
+// incident field subtracted inside the total-field region (scattered field).
+__global__ void k_plain_slices(const PlainArgs a, IncidentWave<double> w, int scattered, double *E,
+                               double *H, size_t n) {
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+        SliceCell c;
+        slice_cell_of(q, a.Nx, a.Ny, a.Nz, a.ssx, a.ssy, a.ssz, false, &c);
+        const size_t x = cidx(a, c.i, c.j, c.k);
+        double e = c.comp == 0 ? a.Ey[x] : a.Ez[x];
+        if (scattered) e -= w.e(1 + c.comp, c.i, c.j, c.k);
+        E[q] = e;
+        double h = 0.0;
+        if (slice_cell_of(q, a.Nx, a.Ny, a.Nz, a.ssx, a.ssy, a.ssz, true, &c)) {
+            h = c.comp == 0 ? a.Hy[x] : a.Hz[x];
+            if (scattered) h -= w.h(1 + c.comp, c.i, c.j, c.k);
+        }
+        H[q] = h;
+    }
+}
+
+int plain_launch_slices(const PlainArgs &a, int scattered, double *E, double *H, void *stream) {
+    IncidentWave<double> w{};
+    w.oblique = a.oblique;
+    w.b1[0] = a.bx1; w.b1[1] = a.by1; w.b1[2] = a.bz1;
+    w.b2[0] = a.bx2; w.b2[1] = a.by2; w.b2[2] = a.bz2;
+    w.ey = a.Eyinc; w.ez = a.Ezinc; w.hy = a.Hyinc; w.hz = a.Hzinc;
+    w.eline = a.Ezinc; w.hline = a.Hyinc;  // the auxiliary line's E and H (oblique)
+    for (int d = 0; d < 3; d++) { w.kr[d] = a.kr[d]; w.ke[d] = a.ke[d]; w.kh[d] = a.kh[d]; }
+    w.s0 = a.s0;
+    const size_t n = 2 * ((size_t)a.Nx * a.Ny + (size_t)a.Nx * a.Nz + (size_t)a.Ny * a.Nz);
+    k_plain_slices<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(a, w, scattered, E, H, n);
     return 1;
 }
 

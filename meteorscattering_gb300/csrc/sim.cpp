@@ -441,6 +441,22 @@ struct mfdtd_sim {
         wait();
     }
 
+    void read_slices(int scattered, double *E, double *H) {
+        if (batch) throw Error(MFDTD_ESTATE, "the simulation is a batch member (mfdtd_batch_remove first)");
+        if (form == MFDTD_FORM_FP64_PLAIN) {
+            double *d = nullptr;
+            mfdtd::ck(cudaMallocAsync(&d, 2 * slice_len * 8, stream), "cudaMallocAsync");
+            mfdtd::plain_launch_slices(pa, scattered, d, d + slice_len, stream);
+            mfdtd::ck(cudaMemcpyAsync(E, d, slice_len * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaMemcpyAsync(H, d + slice_len, slice_len * 8, cudaMemcpyDeviceToHost, stream), "D2H");
+            mfdtd::ck(cudaFreeAsync(d, stream), "cudaFreeAsync");
+        } else {
+            const double s0 = P.s0;
+            f32->read_slices(scattered, E, H, P.kr, s0, P.inc_e, P.inc_h, stream);
+        }
+        wait();
+    }
+
     void write_final(const std::string &dir) {
         mfdtd::FileSink fs{dir};
         std::vector<double> ntf((size_t)ntf_size());
@@ -669,6 +685,14 @@ int mfdtd_sim_read_field(mfdtd_sim *s, int32_t comp, double *out, int64_t n) {
         if (!s || !out) throw Error(MFDTD_EINVAL, "NULL argument");
         if (n < (int64_t)s->P.cells()) throw Error(MFDTD_EINVAL, "output buffer too small");
         s->read_field(comp, out);
+    });
+}
+
+int mfdtd_sim_read_slices(mfdtd_sim *s, int32_t scattered, double *E, double *H, int64_t n) {
+    return guarded([&] {
+        if (!s || !E || !H) throw Error(MFDTD_EINVAL, "NULL argument");
+        if (n < (int64_t)s->slice_len) throw Error(MFDTD_EINVAL, "output buffer too small");
+        s->read_slices(scattered != 0, E, H);
     });
 }
 

@@ -38,7 +38,7 @@ EXPORTS = (
     "mfdtd_batch_create", "mfdtd_batch_destroy", "mfdtd_batch_add", "mfdtd_batch_remove",
     "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune", "mfdtd_server_create",
     "mfdtd_server_destroy", "mfdtd_server_submit", "mfdtd_server_poll", "mfdtd_server_stats",
-    "mfdtd_server_cancel",
+    "mfdtd_server_cancel", "mfdtd_sim_read_slices",
 )
 
 
@@ -139,6 +139,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_server_poll": (C.c_int, [vp, i64, i32, dp, i64, dp, C.POINTER(i32)]),
         "mfdtd_server_stats": (C.c_int, [vp, C.POINTER(i64)]),
         "mfdtd_server_cancel": (C.c_int, [vp, i64]),
+        "mfdtd_sim_read_slices": (C.c_int, [vp, i32, dp, dp, i64]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -317,6 +318,22 @@ class Simulation:
         out = np.empty((Nx, Ny, Nz), dtype=np.float64)
         _check(load_library().mfdtd_sim_read_field(self._h, comp, _dp(out), out.size))
         return out
+
+    def read_slices(self, scattered: bool = False):
+        """(E, H) record slices of the current state, each a dict of planes
+        {"z": [2][Nx][Ny], "y": [2][Nx][Nz], "x": [2][Ny][Nz]} (y and z
+        components), total or scattered field."""
+        Nx, Ny, Nz = self.dims[:3]
+        n = 2 * (Nx * Ny + Nx * Nz + Ny * Nz)
+        E = np.empty(n, dtype=np.float64)
+        H = np.empty(n, dtype=np.float64)
+        _check(load_library().mfdtd_sim_read_slices(self._h, int(bool(scattered)), _dp(E), _dp(H), n))
+
+        def planes(v):
+            a, b = 2 * Nx * Ny, 2 * Nx * Nz
+            return {"z": v[:a].reshape(2, Nx, Ny), "y": v[a:a + b].reshape(2, Nx, Nz),
+                    "x": v[a + b:].reshape(2, Ny, Nz)}
+        return planes(E), planes(H)
 
     def write_outputs(self, path: str) -> None:
         _check(load_library().mfdtd_sim_write_outputs(self._h, os.fsencode(path)))
