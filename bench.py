@@ -152,8 +152,6 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
 TRAFFIC_RATIO = {
     # profiles/k_fp32_step_trailprof_full.md: 4.440 GB / 4.266 GB
     "trail768": 4.4400e9 / 4.2656e9,
-    # profiles/k_fp32_step_trailprof_refinputs_full.md: 4.30 GB / 3.99 GB
-    "trail768_refinputs": 4.3015e9 / 3.9909e9,
 }
 
 

@@ -20,8 +20,11 @@ public:
     // Lee-Kalluri, 2 tabulated Lee-Kalluri); batches group by it.
     int current_update() const;
     static const char *kernel_name(int which);
-    // Record-step outputs in the reference file layout (doubles).
-    void record(double *E, double *H, double *emax, void *stream);
+    // Record-step outputs in the reference file layout (doubles), staged in
+    // device memory without waiting: E and H blocks of slice_len + 2 Nx
+    // doubles each (slices, then the two incident arrays), and bits[0] the
+    // FP32 bits of max|Ex|.
+    void record_stage(double *dE, double *dH, unsigned int *bits, void *stream);
     double guard(void *stream);
     void flush(int t_last, void *stream);
     void read_ntf(int q, double *out, void *stream);

@@ -1732,35 +1732,23 @@ void Fp32Sim::check(void *stream) {
     if (err) throw Error(MFDTD_ETIMEOUT, "FP32 step: a TMA wait ran out (device error flag set)");
 }
 
-void Fp32Sim::record(double *E, double *H, double *emax, void *stream) {
+void Fp32Sim::record_stage(double *dE, double *dH, unsigned int *bits, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     Impl &m = *impl_;
     const size_t n = m.slice_len, Nx = m.Nx;
-    // After an odd number of passes the current state is in set 1, else set 0;
-    // the caller invokes this right after the step's pass, so the state is in
+    // The caller invokes this right after the step's pass: the state is in
     // the set that pass wrote.
     const int cur = m_cur_;
     ck(cudaMemsetAsync(m.scan, 0, 8, s), "memset");
     const size_t NC = (size_t)m.Nx * m.Ny * m.Nzp;
-    k_fp32_scan<<<152 * 8, 256, 0, s>>>(m.a.E[cur][0], m.a.E[cur][1], m.a.E[cur][2], NC, m.scan, m.scan + 1);
-    unsigned int bits[2];
-    ck(cudaMemcpyAsync(bits, m.scan, 8, cudaMemcpyDeviceToHost, s), "D2H");
-    k_f2d<<<256, 256, 0, s>>>(m.a.slE, m.dtmp, n);
-    ck(cudaMemcpyAsync(E, m.dtmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
-    std::vector<float> inc(2 * Nx);
-    ck(cudaMemcpyAsync(inc.data(), m.a.inc[cur][0], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
-    ck(cudaMemcpyAsync(inc.data() + Nx, m.a.inc[cur][1], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
-    ck(cudaStreamSynchronize(s), "sync");
-    for (size_t q = 0; q < 2 * Nx; q++) E[n + q] = inc[q];
-    k_f2d<<<256, 256, 0, s>>>(m.a.slH, m.dtmp, n);
-    ck(cudaMemcpyAsync(H, m.dtmp, n * 8, cudaMemcpyDeviceToHost, s), "D2H");
-    ck(cudaMemcpyAsync(inc.data(), m.a.inc[cur][2], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
-    ck(cudaMemcpyAsync(inc.data() + Nx, m.a.inc[cur][3], Nx * 4, cudaMemcpyDeviceToHost, s), "D2H");
-    ck(cudaStreamSynchronize(s), "sync");
-    for (size_t q = 0; q < 2 * Nx; q++) H[n + q] = inc[q];
-    float f;
-    std::memcpy(&f, &bits[0], 4);
-    *emax = f;
+    k_fp32_scan<<<m.sms * 8, 256, 0, s>>>(m.a.E[cur][0], m.a.E[cur][1], m.a.E[cur][2], NC, m.scan, m.scan + 1);
+    ck(cudaMemcpyAsync(bits, m.scan, 8, cudaMemcpyDeviceToDevice, s), "D2D");
+    k_f2d<<<256, 256, 0, s>>>(m.a.slE, dE, n);
+    k_f2d<<<8, 256, 0, s>>>(m.a.inc[cur][0], dE + n, Nx);
+    k_f2d<<<8, 256, 0, s>>>(m.a.inc[cur][1], dE + n + Nx, Nx);
+    k_f2d<<<256, 256, 0, s>>>(m.a.slH, dH, n);
+    k_f2d<<<8, 256, 0, s>>>(m.a.inc[cur][2], dH + n, Nx);
+    k_f2d<<<8, 256, 0, s>>>(m.a.inc[cur][3], dH + n + Nx, Nx);
 }
 
 double Fp32Sim::guard(void *stream) {

@@ -109,6 +109,21 @@ struct mfdtd_sim {
     std::vector<int64_t> kcount;
     std::vector<cudaEvent_t> kev;  // event pool, (classes+1) per profiled step
     size_t slice_len = 0;  // doubles in one slice block (3 planes x 2 comps)
+    // Record steps in flight, two deep: each is staged in device memory on
+    // the simulation's stream, copied to pinned host memory on copy_stream,
+    // and finished (log line, file appends, collection) when its slot comes
+    // round again or when the advance ends -- so the host's file writes
+    // overlap the following steps.
+    struct RecSlot {
+        double *dE = nullptr, *dH = nullptr, *hE = nullptr, *hH = nullptr;
+        unsigned long long *dbits = nullptr, *hbits = nullptr;
+        cudaEvent_t staged = nullptr, copied = nullptr;
+        int t = -1;
+        bool collect = false, busy = false;
+    };
+    RecSlot rslot[2];
+    int rnext = 0;  // slot of the next record
+    cudaStream_t copy_stream = nullptr;
 
     template <class T> T *dalloc(size_t n) {
         void *p = nullptr;
@@ -219,6 +234,14 @@ struct mfdtd_sim {
 
     ~mfdtd_sim() {
         if (stream) cudaStreamSynchronize(stream);
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
+        for (RecSlot &r : rslot) {
+            if (r.dE) cudaFree(r.dE);
+            if (r.hE) cudaFreeHost(r.hE);
+            if (r.staged) cudaEventDestroy(r.staged);
+            if (r.copied) cudaEventDestroy(r.copied);
+        }
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         for (cudaEvent_t e : kev) cudaEventDestroy(e);
         f32.reset();
         for (void *p : allocs) cudaFree(p);
@@ -251,27 +274,85 @@ struct mfdtd_sim {
 
     // Record step: max|Ex| and the slice/incident arrays after step t.
     void do_record(int tt, bool collect) {
-        mfdtd::Record r;
-        r.t = tt;
-        const size_t Nx = P.Nx;
-        unsigned long long bits = 0;
-        r.E.resize(slice_len + 2 * Nx);
-        r.H.resize(slice_len + 2 * Nx);
+        const size_t Nx = P.Nx, blk = slice_len + 2 * Nx;
+        if (!copy_stream) {
+            mfdtd::ck(cudaStreamCreateWithFlags(&copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+            for (RecSlot &r : rslot) {
+                mfdtd::ck(cudaMalloc(&r.dE, 2 * blk * 8 + 16), "cudaMalloc");
+                r.dH = r.dE + blk;
+                r.dbits = (unsigned long long *)(r.dH + blk);
+                mfdtd::ck(cudaMallocHost(&r.hE, 2 * blk * 8 + 16), "cudaMallocHost");
+                r.hH = r.hE + blk;
+                r.hbits = (unsigned long long *)(r.hH + blk);
+                mfdtd::ck(cudaEventCreateWithFlags(&r.staged, cudaEventDisableTiming), "cudaEventCreate");
+                mfdtd::ck(cudaEventCreateWithFlags(&r.copied, cudaEventDisableTiming), "cudaEventCreate");
+            }
+        }
+        RecSlot &r = rslot[rnext];
+        rnext ^= 1;
+        if (r.busy) finish_record(r);  // the older of the two in flight
+        const cudaMemcpyKind d2d = cudaMemcpyDeviceToDevice;
         if (form == MFDTD_FORM_FP64_PLAIN) {
             mfdtd::plain_launch_emax(pa, stream);
-            mfdtd::ck(cudaMemcpyAsync(&bits, pa.emax, 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            mfdtd::ck(cudaMemcpyAsync(r.E.data(), pa.slE, slice_len * 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            mfdtd::ck(cudaMemcpyAsync(r.E.data() + slice_len, pa.Eyinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            mfdtd::ck(cudaMemcpyAsync(r.E.data() + slice_len + Nx, pa.Ezinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            mfdtd::ck(cudaMemcpyAsync(r.H.data(), pa.slH, slice_len * 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            mfdtd::ck(cudaMemcpyAsync(r.H.data() + slice_len, pa.Hyinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            mfdtd::ck(cudaMemcpyAsync(r.H.data() + slice_len + Nx, pa.Hzinc, Nx * 8, cudaMemcpyDeviceToHost, stream), "D2H");
-            wait();
-            std::memcpy(&r.emax, &bits, 8);
+            mfdtd::ck(cudaMemcpyAsync(r.dbits, pa.emax, 8, d2d, stream), "D2D");
+            mfdtd::ck(cudaMemcpyAsync(r.dE, pa.slE, slice_len * 8, d2d, stream), "D2D");
+            mfdtd::ck(cudaMemcpyAsync(r.dE + slice_len, pa.Eyinc, Nx * 8, d2d, stream), "D2D");
+            mfdtd::ck(cudaMemcpyAsync(r.dE + slice_len + Nx, pa.Ezinc, Nx * 8, d2d, stream), "D2D");
+            mfdtd::ck(cudaMemcpyAsync(r.dH, pa.slH, slice_len * 8, d2d, stream), "D2D");
+            mfdtd::ck(cudaMemcpyAsync(r.dH + slice_len, pa.Hyinc, Nx * 8, d2d, stream), "D2D");
+            mfdtd::ck(cudaMemcpyAsync(r.dH + slice_len + Nx, pa.Hzinc, Nx * 8, d2d, stream), "D2D");
         } else {
-            f32->record(r.E.data(), r.H.data(), &r.emax, stream);
-            wait();
+            f32->record_stage(r.dE, r.dH, (unsigned int *)r.dbits, stream);
         }
+        mfdtd::ck(cudaEventRecord(r.staged, stream), "cudaEventRecord");
+        mfdtd::ck(cudaStreamWaitEvent(copy_stream, r.staged, 0), "cudaStreamWaitEvent");
+        mfdtd::ck(cudaMemcpyAsync(r.hE, r.dE, 2 * blk * 8 + 8, cudaMemcpyDeviceToHost, copy_stream), "D2H");
+        mfdtd::ck(cudaEventRecord(r.copied, copy_stream), "cudaEventRecord");
+        r.t = tt;
+        r.collect = collect;
+        r.busy = true;
+    }
+
+    // Wait (bounded by opts.timeout_s when set) for a record's copy and emit it.
+    void finish_record(RecSlot &rs) {
+        if (opts.timeout_s > 0) {
+            const double t0 = mfdtd::wall_s();
+            for (;;) {
+                cudaError_t q = cudaEventQuery(rs.copied);
+                if (q == cudaSuccess) break;
+                if (q != cudaErrorNotReady) mfdtd::ck(q, "record copy");
+                if (mfdtd::wall_s() - t0 > opts.timeout_s)
+                    throw Error(MFDTD_ETIMEOUT, "record copy did not finish within timeout_s");
+                std::this_thread::sleep_for(std::chrono::microseconds(200));
+            }
+        } else {
+            mfdtd::ck(cudaEventSynchronize(rs.copied), "record copy");
+        }
+        rs.busy = false;
+        const size_t blk = slice_len + 2 * (size_t)P.Nx;
+        mfdtd::Record r;
+        r.t = rs.t;
+        r.E.assign(rs.hE, rs.hE + blk);
+        r.H.assign(rs.hH, rs.hH + blk);
+        if (form == MFDTD_FORM_FP64_PLAIN) {
+            std::memcpy(&r.emax, rs.hbits, 8);
+        } else {
+            float f;
+            std::memcpy(&f, rs.hbits, 4);  // FP32 bits of max|Ex| in the low word
+            r.emax = f;
+        }
+        emit_record(r, rs.collect);
+    }
+
+    // Finish every record in flight, oldest first.
+    void drain_records() {
+        RecSlot &older = rslot[rnext], &newer = rslot[rnext ^ 1];
+        if (older.busy) finish_record(older);
+        if (newer.busy) finish_record(newer);
+    }
+
+    void emit_record(mfdtd::Record &r, bool collect) {
+        const int tt = r.t;
         if (sink) {
             char line[256];
             double partialtime = 100 * tt / P.tsteps;
@@ -327,6 +408,7 @@ struct mfdtd_sim {
             }
             if (t == 20 && sink) {
                 wait();
+                drain_records();
                 double runtimemin = (mfdtd::wall_s() - loop_start) / 60.0;
                 double totaltime = runtimemin * P.tsteps / 20.0;
                 sink->log("t = 20, time taken = " + mfdtd::fmt_g(runtimemin) + " minutes.\n");
@@ -340,6 +422,7 @@ struct mfdtd_sim {
         last_launches = launches;
         if (nsteps > 0) {
             wait();
+            drain_records();
             if (f32) f32->check(stream);
             float ms = 0;
             mfdtd::ck(cudaEventElapsedTime(&ms, ev0, ev1), "cudaEventElapsedTime");
