@@ -1649,7 +1649,12 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         if (uniform)
             for (int q = 0; q < 18; q++) a.lku[q] = (float)P.lk[q];
     }
-    // Split x into chunks so that the grid fills the machine several times over.
+    // Split x into chunks: enough work items to fill the machine several
+    // times over on small grids, and on long x extents chunks of about 160
+    // planes, so that the slower boundary tiles come as short items at the
+    // head of each chunk round rather than as full-length marches that all
+    // run side by side (768x768x1536: 16.44 ms per step in one chunk, 15.48
+    // in 4 to 6, 15.74 in 16 -- each chunk re-computes one warm-up plane).
     int dev = 0, sms = 148;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -1657,6 +1662,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     const int tiles = (m.Nzp / TK) * ((P.Ny + TJ - 1) / TJ);
     const int want = sms * 2 * 8;
     int chunks = std::max(1, std::min(P.Nx / 16 > 0 ? P.Nx / 16 : 1, (want + tiles - 1) / tiles));
+    chunks = std::max(chunks, (P.Nx + 159) / 160);
     a.chunk = (P.Nx + chunks - 1) / chunks;
     chunks = (P.Nx + a.chunk - 1) / a.chunk;
     m.grid = dim3(tiles, 1, chunks);

@@ -144,3 +144,51 @@ def test_fp32_trail_close_to_plain(built, tmp_path):
     golden_cases.write_trail_case(d, case)
     a, b = _sim(d, E.FORM_FP64_PLAIN).read_ntf(), _sim(d, E.FORM_FP32_FUSED).read_ntf()
     assert H.rel_l2(_faces(b, p), _faces(a, p)) < 1e-3
+
+
+@pytest.mark.parametrize("name", ["ext_oblique_trail", "ext_sphere"])
+def test_fp32_ext_record_slices_close_to_plain(built, tmp_path, name):
+    """Record slices at oblique incidence: the FP32 form makes the TF/SF
+    corrections in a pass after the step kernel and patches the slice
+    entries of the TF/SF band on record steps; its slices and incident
+    arrays match the FP64 plain form's within 1e-3 relative L2 (FP32 fields,
+    as for the other outputs)."""
+    case = EXT[name]
+    p = case[0]
+    d64, d32 = os.path.join(str(tmp_path), "f64"), os.path.join(str(tmp_path), "f32")
+    golden_cases.write_ext_case(d64, case)
+    golden_cases.write_ext_case(d32, case)
+    E.run_rundir(d64, form=E.FORM_FP64_PLAIN)
+    E.run_rundir(d32, form=E.FORM_FP32_FUSED)
+    for fname in ("output_E.dat", "output_H.dat"):
+        ra = rd.read_slices(os.path.join(d32, fname), p, True)
+        rb = rd.read_slices(os.path.join(d64, fname), p, True)
+        assert len(ra) == len(rb) == p.numfiles
+        a = np.concatenate([r[k].ravel() for r in ra for k in ("z", "y", "x")])
+        b = np.concatenate([r[k].ravel() for r in rb for k in ("z", "y", "x")])
+        assert np.abs(b).max() > 0
+        assert H.rel_l2(a, b) < 1e-3, (fname, H.rel_l2(a, b))
+
+
+@pytest.mark.parametrize("doplate", [1, 2])
+def test_fp32_oblique_with_plate_or_sphere(built, tmp_path, doplate):
+    """A plate or a conducting sphere (cells with their own E coefficients)
+    lit obliquely: the FP32 form keeps the oblique TF/SF corrections inside
+    the step kernel there (the follow-up pass carries the vacuum
+    coefficients only) and stays within its tolerance of the FP64 plain
+    form, which is bit-exact to the oracle on the same inputs."""
+    name = "plate" if doplate == 1 else "sphere"
+    p, wp, nu, B0 = golden_cases.cases()[name]
+    p = dataclasses.replace(p, dt=rd.stable_dt(p.dx, 0.9), tsteps=160, fsig=20.0, numfiles=8)
+    ext = rd.ExtParams(oblique=1, inc_theta=math.radians(50), inc_phi=math.radians(35))
+    case = (p, wp, nu, B0, ext, None, None)
+    d, dg, do = (os.path.join(str(tmp_path), x) for x in ("r", "gpu", "orc"))
+    for x in (d, dg, do):
+        golden_cases.write_ext_case(x, case)
+    s64, s32 = _sim(d, E.FORM_FP64_PLAIN), _sim(d, E.FORM_FP32_FUSED)
+    a, b = s64.read_ntf(), s32.read_ntf()
+    assert np.abs(_faces(a, p)).max() > 0
+    assert H.rel_l2(_faces(b, p), _faces(a, p)) < 1e-3
+    E.run_rundir(dg)
+    H.run_oracle(do)
+    assert H.diff_outputs(dg, do, p.nntf) == []
