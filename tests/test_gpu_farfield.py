@@ -94,3 +94,23 @@ def test_far_field_tensor_cores_match_fp64(built, name):
     err_db = np.abs(10 * np.log10(s1[mask] / s0[mask]))
     assert err_db.max() < 0.01, err_db.max()
     sim.close()
+
+
+def test_far_field_tensor_cores_large_projection(built):
+    """A large tensor-core projection: 20,000 random directions make every
+    direction cosine distinct, so each face of a 96^3 grid gives a GEMM of
+    about 470 128 x 128 tiles (more than two CTAs per SM).  Method 1 stays
+    within 0.01 dB of method 0."""
+    p, wp, nu, B0 = golden_cases._mk(N=(96, 96, 96), doplate=2, platesize=2.0, fntf=[50e6])
+    p = dataclasses.replace(p, dt=rd.stable_dt(p.dx, 0.9), tsteps=320, numfiles=1, savefields=0)
+    sim = _sim_for((p, wp, nu, B0), E.FORM_FP32_FUSED)
+    rng = np.random.default_rng(17)
+    th = np.arccos(rng.uniform(-1.0, 1.0, 20000))
+    ph = rng.uniform(0.0, 2 * math.pi, 20000)
+    s0 = sim.far_field(th, ph, method=0)[..., 0]
+    s1 = sim.far_field(th, ph, method=1)[..., 0]
+    mask = s0 > s0.max(axis=1, keepdims=True) * 1e-3
+    assert mask.sum() > 1000
+    err_db = np.abs(10 * np.log10(s1[mask] / s0[mask]))
+    assert err_db.max() < 0.01, err_db.max()
+    sim.close()
