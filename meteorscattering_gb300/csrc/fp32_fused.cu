@@ -533,6 +533,25 @@ __device__ __forceinline__ void acc2(double *A, double *B, size_t base, double v
         B[base + 2 * m + 1] += vb * c;
     }
 }
+// One face cell's running-DFT terms (the separate DFT kernel's form): A += va (sin, cos), B += vb (sin, cos)
+// per frequency.  The (sin, cos) pairs of the sums and of the phase table are
+// adjacent and 16-byte aligned (base and the phase row start are even), so
+// each pair moves as one double2.
+__device__ __forceinline__ void acc2v(double *A, double *B, size_t base, double va, double vb,
+                                     const double *ph, int nf) {
+    double2 *a2 = (double2 *)(A + base), *b2 = (double2 *)(B + base);
+    const double2 *p2 = (const double2 *)ph;
+    for (int m = 0; m < nf; m++) {
+        const double2 p = p2[m];
+        double2 x = a2[m], y = b2[m];
+        x.x += va * p.x;
+        x.y += va * p.y;
+        y.x += vb * p.x;
+        y.y += vb * p.y;
+        a2[m] = x;
+        b2[m] = y;
+    }
+}
 
 // Everything a marching CTA keeps between planes.
 struct MarchCtx {
@@ -1176,35 +1195,38 @@ __device__ __forceinline__ void ntf_cells(const Args &a, int t, int cur, size_t 
         if (r < 2 * fx) {  // x faces: front (i = nb), back (i = Nx - nb); r = j * Nz + k
             const bool back = r >= fx;
             if (back) r -= fx;
-            const int i = back ? Nx - nb : nb, j = (int)(r / Nz), k = (int)(r % Nz);
+            const int i = back ? Nx - nb : nb, j = (int)((unsigned)r / (unsigned)Nz),
+                      k = (int)((unsigned)r % (unsigned)Nz);
             const size_t c = i * sI + j * sJ + k, base = r * n2;
             const double hz = 0.5 * ((double)H2[c] + H2[c - sI]), hy = 0.5 * ((double)H1[c] + H1[c - sI]);
             const float ey = E1[c], ez = E2[c];
-            if (!back) { acc2(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
-            else { acc2(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
+            if (!back) { acc2v(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2v(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
+            else { acc2v(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2v(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
             continue;
         }
         r -= 2 * fx;
         if (r < 2 * fy) {  // y faces: top (j = Ny - nb), bottom (j = nb); r = i * Nz + k
             const bool bottom = r >= fy;
             if (bottom) r -= fy;
-            const int j = bottom ? nb : Ny - nb, i = (int)(r / Nz), k = (int)(r % Nz);
+            const int j = bottom ? nb : Ny - nb, i = (int)((unsigned)r / (unsigned)Nz),
+                      k = (int)((unsigned)r % (unsigned)Nz);
             const size_t c = i * sI + j * sJ + k, base = r * n2;
             const double hz = 0.5 * ((double)H2[c] + H2[c - sJ]), hx = 0.5 * ((double)H0[c] + H0[c - sJ]);
             const float ex = E0[c], ez = E2[c];
-            if (!bottom) { acc2(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
-            else { acc2(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
+            if (!bottom) { acc2v(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2v(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
+            else { acc2v(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2v(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
             continue;
         }
         r -= 2 * fy;  // z faces: left (k = nb), right (k = Nz - nb); r = i * Ny + j
         const bool right = r >= fz;
         if (right) r -= fz;
-        const int k = right ? Nz - nb : nb, i = (int)(r / Ny), j = (int)(r % Ny);
+        const int k = right ? Nz - nb : nb, i = (int)((unsigned)r / (unsigned)Ny),
+                  j = (int)((unsigned)r % (unsigned)Ny);
         const size_t c = i * sI + j * sJ + k, base = r * n2;
         const double hy = 0.5 * ((double)H1[c] + H1[c - 1]), hx = 0.5 * ((double)H0[c] + H0[c - 1]);
         const float ex = E0[c], ey = E1[c];
-        if (!right) { acc2(a.ntf[18], a.ntf[19], base, hy, -hx, ph, nf); acc2(a.ntf[16], a.ntf[17], base, -(double)ey, ex, ph, nf); }
-        else { acc2(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
+        if (!right) { acc2v(a.ntf[18], a.ntf[19], base, hy, -hx, ph, nf); acc2v(a.ntf[16], a.ntf[17], base, -(double)ey, ex, ph, nf); }
+        else { acc2v(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2v(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
     }
 }
 __global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a, int t, int cur) {
@@ -1230,23 +1252,27 @@ __device__ __forceinline__ void tfsf_band(const Args &a, int record, size_t q0, 
     const size_t nX = 4 * (size_t)Jr * Kr, nY = 4 * (size_t)Ir2 * Kr, nZ = 4 * (size_t)Ir2 * Jr2;
     const size_t plane = (size_t)a.Ny * a.Nzp;
     auto pick = [](int b1, int b2, int s) { return s == 0 ? b1 - 1 : s == 1 ? b1 : s == 2 ? b2 - 1 : b2; };
+    // band sizes stay far below 2^31 (four face layers), so the index
+    // decomposition runs in 32-bit arithmetic
+    const unsigned uKr = (unsigned)Kr, uJr2 = (unsigned)Jr2, aX = (unsigned)Jr * uKr,
+                   aY = (unsigned)Ir2 * uKr, aZ = (unsigned)Ir2 * uJr2;
     for (size_t q = q0; q < nX + nY + nZ; q += dq) {
         int i, j, k;
         if (q < nX) {
-            const size_t r = q % ((size_t)Jr * Kr);
-            i = pick(bx1, bx2, (int)(q / ((size_t)Jr * Kr)));
-            j = by1 - 1 + (int)(r / Kr);
-            k = bz1 - 1 + (int)(r % Kr);
+            const unsigned u = (unsigned)q, r = u % aX;
+            i = pick(bx1, bx2, (int)(u / aX));
+            j = by1 - 1 + (int)(r / uKr);
+            k = bz1 - 1 + (int)(r % uKr);
         } else if (q < nX + nY) {
-            const size_t r0 = q - nX, r = r0 % ((size_t)Ir2 * Kr);
-            j = pick(by1, by2, (int)(r0 / ((size_t)Ir2 * Kr)));
-            i = bx1 + 1 + (int)(r / Kr);
-            k = bz1 - 1 + (int)(r % Kr);
+            const unsigned u = (unsigned)(q - nX), r = u % aY;
+            j = pick(by1, by2, (int)(u / aY));
+            i = bx1 + 1 + (int)(r / uKr);
+            k = bz1 - 1 + (int)(r % uKr);
         } else {
-            const size_t r0 = q - nX - nY, r = r0 % ((size_t)Ir2 * Jr2);
-            k = pick(bz1, bz2, (int)(r0 / ((size_t)Ir2 * Jr2)));
-            i = bx1 + 1 + (int)(r / Jr2);
-            j = by1 + 1 + (int)(r % Jr2);
+            const unsigned u = (unsigned)(q - nX - nY), r = u % aZ;
+            k = pick(bz1, bz2, (int)(u / aZ));
+            i = bx1 + 1 + (int)(r / uJr2);
+            j = by1 + 1 + (int)(r % uJr2);
         }
         const float hx = obl_corr<PAR, false, 0>(a, i, j, k), hy = obl_corr<PAR, false, 1>(a, i, j, k),
                     hz = obl_corr<PAR, false, 2>(a, i, j, k);
