@@ -125,9 +125,12 @@ def make_problem(E, p, wp2, nu2, B0, ext, trail):
 
 
 def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
-                      per_cell_map: bool = False) -> float:
+                      per_cell_map: bool = False, plasma: float = 1.0) -> float:
     """Compulsory DRAM bytes of one launch of `kernel` (per cell-update figure
-    x cells, plus the CPML psi slabs each launch reads and writes)."""
+    x cells, plus the CPML psi slabs each launch reads and writes).  `plasma`
+    is the share of the FP32 pass's (plane, tile) blocks holding plasma: J
+    (and the per-cell plasma map) are read and written there only, since J is
+    identically zero where omega_p is."""
     cells = p.Nx * p.Ny * p.Nz
     psi = 2 * (2 * L * p.Ny * p.Nz + p.Nx * 2 * L * p.Nz + p.Nx * p.Ny * 2 * L)  # one half-step
     if form == "fp64":
@@ -137,21 +140,22 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
         if kernel == "k_plain_e":   # H r(3), E r/w(6), J r(3) ; psi r/w
             return cells * 12 * 8 + psi * 16
     else:
-        # FP32 single pass: E, H, J read and written (18 x 4 B), plus the
-        # per-cell E0 wp^2 map when the plasma is 3-D (4 B); every psi cell of
+        # FP32 single pass: E and H read and written (12 x 4 B) everywhere; J
+        # read and written (6 x 4 B) plus the per-cell E0 wp^2 map when the
+        # plasma is 3-D (4 B) in the blocks holding plasma; every psi cell of
         # both half-steps read and written once.
-        return cells * (18 * 4 + (4 if per_cell_map else 0)) + 2 * psi * 8
+        return cells * (12 * 4 + plasma * (6 * 4 + (4 if per_cell_map else 0))) + 2 * psi * 8
     raise KeyError(kernel)
 
 
-# DRAM traffic / algorithmic bytes of k_fp32_step measured by ncu on the
-# profiling-size case of each workload (profiles/): the full-size grids are too
-# large for a multi-pass capture, and the halo overhead per cell is a property
-# of the tile geometry, so a full launch's traffic is the ratio times its
-# algorithmic bytes.
+# DRAM traffic / the pass's own compulsory bytes (J and the plasma map in
+# plasma blocks only) of k_fp32_step, measured by ncu on the profiling-size
+# case of each workload (profiles/): the full-size grids are too large for a
+# multi-pass capture, and the halo overhead per cell is a property of the tile
+# geometry, so a full launch's traffic is the ratio times its own bytes.
 TRAFFIC_RATIO = {
-    # profiles/k_fp32_step_trailprof_full.md: 4.440 GB / 4.266 GB
-    "trail768": 4.4400e9 / 4.2656e9,
+    # profiles/k_fp32_step_trailprof_full.md: 3.026 GB / 2.908 GB
+    "trail768": 3.0262e9 / 2.9082e9,
 }
 
 
@@ -583,6 +587,7 @@ def main():
     device = local
     pb = make_problem(E, p, wp2, nu2, B0, ext, trail)
     sim = E.Simulation(pb, form=form, device=device, profile=True)
+    plasma = sim.plasma_fraction()
     if W:
         sim.advance(W)
     sim.sync()
@@ -606,12 +611,19 @@ def main():
     peak, peak_kind = load_peaks()
     roof = None
     if dom:
+        # achieved: the per-cell-update figure of the hot-path table (76 B for the
+        # FP32 pass: E, H, J read and written, plus the plasma map) x cells;
+        # own: the bytes this pass must move, J and the map in plasma blocks only
         alg = algorithmic_bytes(args.form, dom[0], p, L, per_cell)
+        alg_own = algorithmic_bytes(args.form, dom[0], p, L, per_cell, plasma)
         ach = alg / (dom[1] * 1e-3) / 1e9
         roof = {"kernel": dom[0], "bound": "hbm", "achieved": ach, "peak": peak,
                 "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom[1],
-                "traffic": traffic_per_launch(args.form, args.workload, dom[0], alg),
+                "traffic": traffic_per_launch(args.form, args.workload, dom[0], alg_own),
+                "own_bytes": {"plasma_block_fraction": plasma, "bytes_per_launch": alg_own,
+                              "achieved": alg_own / (dom[1] * 1e-3) / 1e9,
+                              "frac": alg_own / (dom[1] * 1e-3) / 1e9 / peak},
                 "kernel_times_ms": {n: m for n, m, c in kstats},
                 # the same compulsory bytes over the whole step (every kernel of it)
                 "step_achieved": alg / (ms_step * 1e-3) / 1e9,
@@ -652,7 +664,7 @@ def main():
                            "form": "fp32_fused" if args.form == "fp32" else "fp64_plain",
                            "parallelism": f"replicas x{world}",
                            "l2": "state larger than L2 (no flush needed)"},
-                "hbm_gbs": (algorithmic_bytes(args.form, dom[0], p, L, per_cell) / (dom[1] * 1e-3) / 1e9)
+                "hbm_gbs": (algorithmic_bytes(args.form, dom[0], p, L, per_cell, plasma) / (dom[1] * 1e-3) / 1e9)
                 if dom else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "host_wall_s": wall}

@@ -208,6 +208,11 @@ int mfdtd_sim_read_field(mfdtd_sim *s, int32_t comp, double *out, int64_t n);
  * region, exactly where the TF/SF corrections put it -- the scattered field
  * analysis/plotMresults.m:210-234 forms on the host for its movies. */
 int mfdtd_sim_read_slices(mfdtd_sim *s, int32_t scattered, double *E, double *H, int64_t n);
+/* Share of the FP32 pass's (plane, 8 x 32 tile) blocks that hold plasma;
+ * elsewhere J is identically zero and the pass neither loads nor stores it
+ * (1 for the FP64 plain form, which updates J everywhere as the reference
+ * does). */
+int mfdtd_sim_plasma_fraction(const mfdtd_sim *s, double *fraction);
 /* Write output_{E,H,J}.dat (collected records), output_NTF.dat, Probe.dat
  * and the log.txt record lines into `dir`. */
 int mfdtd_sim_write_outputs(mfdtd_sim *s, const char *dir);

@@ -35,6 +35,9 @@ public:
     // total-field region when `scattered`; the oblique geometry in FP64.
     void read_slices(int scattered, double *E, double *H, const double kr[3], double s0,
                      const double ke[3], const double kh[3], void *stream);
+    // Share of the pass's (plane, tile) blocks that hold plasma: J is loaded,
+    // updated and stored there only.
+    double plasma_fraction() const;
     // Throws if a kernel set the device error flag (a bounded wait ran out).
     void check(void *stream);
     // Device pointers of the 24 DFT arrays (output_NTF.dat order).

@@ -107,6 +107,12 @@ struct Args {
     const double *xc, *yc, *zc;
     const int *tile_order;  // CTA -> tile (ty * ntk + tk): boundary tiles first
     int ntk;                // tiles along k
+    // Per (plane, tile): 1 when any cell of the tile's 8 x 32 block in that
+    // plane holds plasma (omega_p > 0), else 0.  Elsewhere J is zero and stays
+    // zero (its update adds a term proportional to omega_p^2), so the pass
+    // neither loads, updates nor stores it there.  Null: plasma everywhere.
+    const unsigned char *plasma;
+    int ntiles;             // tiles per plane (row length of `plasma`)
     double *ntf[24];
     double *probe;       // [6][tsteps][nprobes]
     const int *probe_ijk;
@@ -561,17 +567,24 @@ struct MarchCtx {
     int tid, warp, lane, j0, k0, i_begin, i_end, p0, q_last, dj, dk, j, k;
     bool role_ok, in_grid, valid;
     int issued;
+    int tile_id;
 };
 
+// Does the tile's block of plane q hold plasma?  (See Args::plasma.)
+__device__ __forceinline__ bool plasma_at(const Args &a, const MarchCtx &c, int q) {
+    return !a.plasma || a.plasma[(size_t)q * a.ntiles + c.tile_id] != 0;
+}
+
+// Stage of plane q: E and H boxes, and the J box where the block holds plasma.
 template <int PAR>
-__device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q) {
+__device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q, bool with_j) {
     const int slot = (q - c.p0) % NS;
     Stage st = stage_at(c.smem + slot * STAGE_B);
-    mbar_arm(&c.bar[slot], STAGE_TX);
+    mbar_arm(&c.bar[slot], with_j ? STAGE_TX : STAGE_TX - 3 * J_B);
     for (int comp = 0; comp < 3; comp++) {
         tma3(st.e[comp], &maps.E[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
         tma3(st.h[comp], &maps.H[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
-        tma3(st.j[comp], &maps.J[comp], c.k0, c.j0, q, &c.bar[slot]);
+        if (with_j) tma3(st.j[comp], &maps.J[comp], c.k0, c.j0, q, &c.bar[slot]);
     }
 }
 
@@ -611,7 +624,8 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
     };
     float nwq = 0.f, nnu = 0.f;
-    pf_load(c.p0, nwq, nnu);
+    bool npl = plasma_at(a, c, c.p0);
+    if (npl) pf_load(c.p0, nwq, nnu);
 
     // One thread polls the stage mbarriers; the rest of the CTA sleeps in the
     // CTA barrier instead of spinning.  The poller's mbarrier acquire plus
@@ -638,7 +652,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         if (!okflag[q & 1]) return false;
         if (c.tid == PROD && q > c.p0 && q - 1 + NS <= c.q_last) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_stage<PAR>(maps, c, q - 1 + NS);
+            issue_stage<PAR>(maps, c, q - 1 + NS, plasma_at(a, c, q - 1 + NS));
             c.issued = q - 1 + NS;
         }
         return true;
@@ -648,7 +662,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     for (int q = c.p0; q < c.i_end; q++) {
         const int i = q;
         const float cwq = nwq, cnu = nnu;
-        pf_load(q + 1, nwq, nnu);
+        const bool pl = npl;  // this plane's block holds plasma
+        npl = q + 1 < c.i_end && plasma_at(a, c, q + 1);
+        if (npl) pf_load(q + 1, nwq, nnu);
         const int slot = (q - c.p0) % NS;
         float *hn = c.hn + (q & 1) * (align128(HN_B) / 4);  // this plane's new-H buffer
         // Stages q and q+1 are resident: the barrier of the previous plane
@@ -675,6 +691,8 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 exo = s.e[0][EIDX(dj, dk)];
                 eyo = s.e[1][EIDX(dj, dk)];
                 ezo = s.e[2][EIDX(dj, dk)];
+            }
+            if (tile && pl) {
                 jx = s.j[0][dj * TK + dk];
                 jy = s.j[1][dj * TK + dk];
                 jz = s.j[2][dj * TK + dk];
@@ -738,9 +756,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 a.E[PAR ^ 1][0][cg] = ex;
                 a.E[PAR ^ 1][1][cg] = ey;
                 a.E[PAR ^ 1][2][cg] = ez;
-                a.J[0][cg] = jx;
-                a.J[1][cg] = jy;
-                a.J[2][cg] = jz;
+                if (pl) {
+                    a.J[0][cg] = jx;
+                    a.J[1][cg] = jy;
+                    a.J[2][cg] = jz;
+                }
                 ex_prev = exo;
             }
             hy_prev = hv.y;
@@ -750,7 +770,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
         // ---- J of the previous step (lagged), source/meteor-fork.cpp:1523-1595
         float jx = 0.f, jy = 0.f, jz = 0.f;
-        if (valid && real) {
+        if (valid && real && pl) {
             jx = s.j[0][dj * TK + dk];
             jy = s.j[1][dj * TK + dk];
             jz = s.j[2][dj * TK + dk];
@@ -947,9 +967,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             a.E[PAR ^ 1][0][cg] = ex;
             a.E[PAR ^ 1][1][cg] = ey;
             a.E[PAR ^ 1][2][cg] = ez;
-            a.J[0][cg] = jx;
-            a.J[1][cg] = jy;
-            a.J[2][cg] = jz;
+            if (pl) {
+                a.J[0][cg] = jx;
+                a.J[1][cg] = jy;
+                a.J[2][cg] = jz;
+            }
 
             // ---- running DFT on the Huygens surface (FP64 sums)
             const int nb = a.ntfb;
@@ -1039,6 +1061,7 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     c.warp = c.tid >> 5;
     c.lane = c.tid & 31;
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
+    c.tile_id = tile_id;
     c.k0 = (tile_id % a.ntk) * TK;
     c.j0 = (tile_id / a.ntk) * TJ;
     c.i_begin = chunk * a.chunk;
@@ -1081,7 +1104,7 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     if (c.tid == PROD) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (int q = c.p0; q <= c.q_last && q < c.p0 + NS; q++) {
-            issue_stage<PAR>(maps, c, q);
+            issue_stage<PAR>(maps, c, q, plasma_at(a, c, q));
             c.issued = q;
         }
     }
@@ -1361,6 +1384,28 @@ __global__ void k_fp32_slices(const __grid_constant__ Args a, IncidentWave<float
     }
 }
 
+// The plasma table (Args::plasma): one thread per (plane, tile) block.  A
+// block counts as plasma when any cell has a nonzero E0 omega_p^2 and a
+// nonzero z factor (a superset of the cells whose J can leave zero).
+__global__ void k_plasma_blocks(const __grid_constant__ Args a, unsigned char *out) {
+    const size_t n = (size_t)a.Nx * a.ntiles;
+    for (size_t u = (size_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (size_t)gridDim.x * blockDim.x) {
+        const int q = (int)(u / a.ntiles), tile = (int)(u % a.ntiles);
+        const int k0 = (tile % a.ntk) * TK, j0 = (tile / a.ntk) * TJ;
+        bool any = false;
+        for (int dj = 0; dj < TJ && !any; dj++) {
+            const int j = j0 + dj;
+            if (j >= a.Ny) break;
+            const float w2 = a.wq3 ? 1.f : a.wq2[(size_t)q * a.Ny + j];
+            if (w2 == 0.f) continue;
+            const float *row = a.wq3 ? a.wq3 + ((size_t)q * a.Ny + j) * a.Nzp + k0 : nullptr;
+            for (int dk = 0; dk < TK && k0 + dk < a.Nz; dk++)
+                if (a.G2[k0 + dk] != 0.f && (!row || row[dk] != 0.f)) any = true;
+        }
+        out[u] = any ? 1 : 0;
+    }
+}
+
 // E probes of the final step (the per-step ones ride in the next pass).
 __global__ void k_fp32_flush(const Args a, int t_last, int par) {
     const int p = threadIdx.x;
@@ -1482,6 +1527,7 @@ struct Fp32Sim::Impl {
     unsigned int *scan = nullptr;  // [0] max|Ex| bits, [1] bad flag
     int jm = 0;  // J method of the kernel variant
     int sms = 148;                 // SM count (grids of the follow-up kernels)
+    double plasma_fraction = 1.0;  // share of (plane, tile) blocks holding plasma
     std::vector<int> tile_order;   // host copy: boundary tiles first
     int n_boundary = 0;            // how many of them are boundary tiles
 
@@ -1714,9 +1760,26 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         m.tile_order = order;
         a.tile_order = m.upload(order, s);
         a.ntk = ntk;
+        a.ntiles = ntk * nty;
+    }
+    {
+        // Which (plane, tile) blocks hold plasma; the pass skips J elsewhere.
+        const size_t nb = (size_t)P.Nx * a.ntiles;
+        unsigned char *d = m.alloc<unsigned char>(nb, s);
+        k_plasma_blocks<<<m.sms * 8, 256, 0, s>>>(a, d);
+        ck(cudaGetLastError(), "plasma blocks");
+        std::vector<unsigned char> h(nb);
+        ck(cudaMemcpyAsync(h.data(), d, nb, cudaMemcpyDeviceToHost, s), "D2H");
+        ck(cudaStreamSynchronize(s), "plasma blocks");
+        size_t np = 0;
+        for (unsigned char v : h) np += v;
+        m.plasma_fraction = nb ? (double)np / (double)nb : 0.0;
+        a.plasma = d;
     }
     bytes_ = m.bytes;
 }
+
+double Fp32Sim::plasma_fraction() const { return impl_->plasma_fraction; }
 
 int Fp32Sim::kernel_classes() { return 3; }
 int Fp32Sim::current_update() const { return impl_->jm; }

@@ -779,6 +779,13 @@ int mfdtd_sim_read_slices(mfdtd_sim *s, int32_t scattered, double *E, double *H,
     });
 }
 
+int mfdtd_sim_plasma_fraction(const mfdtd_sim *s, double *fraction) {
+    return guarded([&] {
+        if (!s || !fraction) throw Error(MFDTD_EINVAL, "NULL argument");
+        *fraction = s->f32 ? s->f32->plasma_fraction() : 1.0;
+    });
+}
+
 int mfdtd_sim_write_outputs(mfdtd_sim *s, const char *dir) {
     return guarded([&] {
         if (!s || !dir) throw Error(MFDTD_EINVAL, "NULL argument");

@@ -38,7 +38,7 @@ EXPORTS = (
     "mfdtd_batch_create", "mfdtd_batch_destroy", "mfdtd_batch_add", "mfdtd_batch_remove",
     "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune", "mfdtd_server_create",
     "mfdtd_server_destroy", "mfdtd_server_submit", "mfdtd_server_poll", "mfdtd_server_stats",
-    "mfdtd_server_cancel", "mfdtd_sim_read_slices",
+    "mfdtd_server_cancel", "mfdtd_sim_read_slices", "mfdtd_sim_plasma_fraction",
 )
 
 
@@ -140,6 +140,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_server_stats": (C.c_int, [vp, C.POINTER(i64)]),
         "mfdtd_server_cancel": (C.c_int, [vp, i64]),
         "mfdtd_sim_read_slices": (C.c_int, [vp, i32, dp, dp, i64]),
+        "mfdtd_sim_plasma_fraction": (C.c_int, [vp, dp]),
         "mfdtd_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
         "mfdtd_version": (C.c_char_p, []),
     }
@@ -318,6 +319,13 @@ class Simulation:
         out = np.empty((Nx, Ny, Nz), dtype=np.float64)
         _check(load_library().mfdtd_sim_read_field(self._h, comp, _dp(out), out.size))
         return out
+
+    def plasma_fraction(self) -> float:
+        """Share of the FP32 pass's (plane, tile) blocks that hold plasma (J is
+        loaded and stored there only); 1 for the FP64 plain form."""
+        f = C.c_double()
+        _check(load_library().mfdtd_sim_plasma_fraction(self._h, C.byref(f)))
+        return f.value
 
     def read_slices(self, scattered: bool = False):
         """(E, H) record slices of the current state, each a dict of planes
