@@ -10,9 +10,10 @@
 // One kernel launch advances one time step.  Each CTA owns a TJ x TK tile of
 // (j,k) columns and marches along x (the slowest axis, stride Ny*Nzp), one
 // plane per iteration:
-//   * the plane's E, H and J tiles (plus one-cell halos) arrive by TMA
+//   * the plane's E and H tiles (plus one-cell halos) arrive by TMA
 //     (cp.async.bulk.tensor.3d) into a ring of NS shared-memory stages, each
-//     guarded by an mbarrier; the producer runs NS-2 planes ahead;
+//     guarded by an mbarrier; the producer runs NS-2 planes ahead; J is read
+//     from global memory, only in blocks holding plasma (zero elsewhere);
 //   * J of the previous step is advanced first (it needs E of this step's
 //     start, which is read-only in this pass), then H of this plane (tile plus
 //     a low-side halo row and column, which the E update needs), then E;
@@ -43,9 +44,9 @@ constexpr int NS = 5;                      // pipeline stages
 constexpr int NTHREADS = 320;              // 8 tile warps + halo-row warp + halo-column warp
 constexpr int PROD = NTHREADS - 1;         // producer thread (idle lane of the halo-column warp)
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
-constexpr int E_B = align128(EJ * EK * 4), H_B = align128(HJ * HK * 4), J_B = TJ * TK * 4;
-constexpr int STAGE_B = 3 * E_B + 3 * H_B + 3 * J_B;
-constexpr int STAGE_TX = 3 * EJ * EK * 4 + 3 * HJ * HK * 4 + 3 * TJ * TK * 4;  // bytes per stage
+constexpr int E_B = align128(EJ * EK * 4), H_B = align128(HJ * HK * 4);
+constexpr int STAGE_B = 3 * E_B + 3 * H_B;
+constexpr int STAGE_TX = 3 * EJ * EK * 4 + 3 * HJ * HK * 4;  // bytes per stage
 constexpr int HN_COLS = TK + 1;            // new-H plane: cols k0-1..k0+TK-1
 constexpr int HN_B = 3 * HJ * HN_COLS * 4;
 // two new-H planes (alternating per x plane), NS stage barriers, two poll flags
@@ -53,7 +54,7 @@ constexpr int SMEM_B = NS * STAGE_B + 2 * align128(HN_B) + NS * 8 + 16 + 128;  /
 constexpr double kE0 = 8.85419e-12;
 
 struct Maps {
-    CUtensorMap E[2][3], H[2][3], J[3];
+    CUtensorMap E[2][3], H[2][3];
 };
 
 // CPML and auxiliary-line coefficient tables of one simulation, in global
@@ -179,14 +180,13 @@ __device__ __forceinline__ int eslab(int n, int N, int L, int shift) {
 
 // Views of one stage.
 struct Stage {
-    float *e[3], *h[3], *j[3];
+    float *e[3], *h[3];
 };
 __device__ __forceinline__ Stage stage_at(unsigned char *base) {
     Stage s;
     for (int c = 0; c < 3; c++) {
         s.e[c] = (float *)(base + c * E_B);
         s.h[c] = (float *)(base + 3 * E_B + c * H_B);
-        s.j[c] = (float *)(base + 3 * E_B + 3 * H_B + c * J_B);
     }
     return s;
 }
@@ -575,16 +575,17 @@ __device__ __forceinline__ bool plasma_at(const Args &a, const MarchCtx &c, int 
     return !a.plasma || a.plasma[(size_t)q * a.ntiles + c.tile_id] != 0;
 }
 
-// Stage of plane q: E and H boxes, and the J box where the block holds plasma.
+// Stage of plane q: the E and H boxes.  (J is read from global memory, and
+// only in blocks holding plasma: keeping it out of the stages leaves 15 KB of
+// each CTA's shared memory to L1, which measured faster than staging it.)
 template <int PAR>
-__device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q, bool with_j) {
+__device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q) {
     const int slot = (q - c.p0) % NS;
     Stage st = stage_at(c.smem + slot * STAGE_B);
-    mbar_arm(&c.bar[slot], with_j ? STAGE_TX : STAGE_TX - 3 * J_B);
+    mbar_arm(&c.bar[slot], STAGE_TX);
     for (int comp = 0; comp < 3; comp++) {
         tma3(st.e[comp], &maps.E[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
         tma3(st.h[comp], &maps.H[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
-        if (with_j) tma3(st.j[comp], &maps.J[comp], c.k0, c.j0, q, &c.bar[slot]);
     }
 }
 
@@ -652,7 +653,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         if (!okflag[q & 1]) return false;
         if (c.tid == PROD && q > c.p0 && q - 1 + NS <= c.q_last) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_stage<PAR>(maps, c, q - 1 + NS, plasma_at(a, c, q - 1 + NS));
+            issue_stage<PAR>(maps, c, q - 1 + NS);
             c.issued = q - 1 + NS;
         }
         return true;
@@ -693,9 +694,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 ezo = s.e[2][EIDX(dj, dk)];
             }
             if (tile && pl) {
-                jx = s.j[0][dj * TK + dk];
-                jy = s.j[1][dj * TK + dk];
-                jz = s.j[2][dj * TK + dk];
+                jx = a.J[0][cg];
+                jy = a.J[1][cg];
+                jz = a.J[2][cg];
                 if (t > 0) {
                     const float wq = cwq * G2k;
                     if (JM == 0) {
@@ -771,9 +772,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         // ---- J of the previous step (lagged), source/meteor-fork.cpp:1523-1595
         float jx = 0.f, jy = 0.f, jz = 0.f;
         if (valid && real && pl) {
-            jx = s.j[0][dj * TK + dk];
-            jy = s.j[1][dj * TK + dk];
-            jz = s.j[2][dj * TK + dk];
+            jx = a.J[0][cg];
+            jy = a.J[1][cg];
+            jz = a.J[2][cg];
             const bool jdom = CLEAN ? (i >= 1 && i < Nx - 1)
                                     : (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1);
             if (t > 0 && jdom) {
@@ -1104,7 +1105,7 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     if (c.tid == PROD) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (int q = c.p0; q <= c.q_last && q < c.p0 + NS; q++) {
-            issue_stage<PAR>(maps, c, q, plasma_at(a, c, q));
+            issue_stage<PAR>(maps, c, q);
             c.issued = q;
         }
     }
@@ -1703,7 +1704,6 @@ void Fp32Sim::init(const Problem &P, void *stream) {
             make_map(&m.maps.E[b][c], a.E[b][c], P.Nx, P.Ny, P.Nz, m.Nzp, EK, EJ);
             make_map(&m.maps.H[b][c], a.H[b][c], P.Nx, P.Ny, P.Nz, m.Nzp, HK, HJ);
         }
-    for (int c = 0; c < 3; c++) make_map(&m.maps.J[c], a.J[c], P.Nx, P.Ny, P.Nz, m.Nzp, TK, TJ);
 
     {
         auto attr = [](const void *f) {
