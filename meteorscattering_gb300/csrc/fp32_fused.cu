@@ -1385,25 +1385,26 @@ __global__ void k_fp32_slices(const __grid_constant__ Args a, IncidentWave<float
     }
 }
 
-// The plasma table (Args::plasma): one thread per (plane, tile) block.  A
-// block counts as plasma when any cell has a nonzero E0 omega_p^2 and a
-// nonzero z factor (a superset of the cells whose J can leave zero).
+// The plasma table (Args::plasma): one warp per (plane, tile) block, lane =
+// k column (coalesced rows of the map).  A block counts as plasma when any
+// cell has a nonzero E0 omega_p^2 and a nonzero z factor (a superset of the
+// cells whose J can leave zero).
 __global__ void k_plasma_blocks(const __grid_constant__ Args a, unsigned char *out) {
     const size_t n = (size_t)a.Nx * a.ntiles;
-    for (size_t u = (size_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (size_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const size_t w0 = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5,
+                 dw = ((size_t)gridDim.x * blockDim.x) >> 5;
+    for (size_t u = w0; u < n; u += dw) {
         const int q = (int)(u / a.ntiles), tile = (int)(u % a.ntiles);
-        const int k0 = (tile % a.ntk) * TK, j0 = (tile / a.ntk) * TJ;
+        const int k = (tile % a.ntk) * TK + lane, j0 = (tile / a.ntk) * TJ;
         bool any = false;
-        for (int dj = 0; dj < TJ && !any; dj++) {
-            const int j = j0 + dj;
-            if (j >= a.Ny) break;
-            const float w2 = a.wq3 ? 1.f : a.wq2[(size_t)q * a.Ny + j];
-            if (w2 == 0.f) continue;
-            const float *row = a.wq3 ? a.wq3 + ((size_t)q * a.Ny + j) * a.Nzp + k0 : nullptr;
-            for (int dk = 0; dk < TK && k0 + dk < a.Nz; dk++)
-                if (a.G2[k0 + dk] != 0.f && (!row || row[dk] != 0.f)) any = true;
-        }
-        out[u] = any ? 1 : 0;
+        if (k < a.Nz && a.G2[k] != 0.f)
+            for (int dj = 0; dj < TJ && j0 + dj < a.Ny; dj++) {
+                const size_t ij = (size_t)q * a.Ny + j0 + dj;
+                if ((a.wq3 ? a.wq3[ij * a.Nzp + k] : a.wq2[ij]) != 0.f) any = true;
+            }
+        any = __any_sync(0xffffffffu, any);
+        if (lane == 0) out[u] = any ? 1 : 0;
     }
 }
 
