@@ -38,23 +38,32 @@ namespace mfdtd {
 namespace {
 
 constexpr int TJ = 8, TK = 32;             // tile rows (j) x columns (k)
-constexpr int EJ = TJ + 2, EK = TK + 8;    // E box: rows j0-1..j0+TJ, cols k0-4..k0+TK+3
-constexpr int HJ = TJ + 1, HK = TK + 4;    // H box: rows j0-1..j0+TJ-1, cols k0-4..k0+TK-1
+// One stage is one x plane of the six field components of one parity, a box
+// of rows j0-1..j0+TJ and cols k0-4..k0+TK+3 each, loaded by ONE TMA copy:
+// the components of a parity are one allocation, [Ex Ey Ez Hx Hy Hz][Nx][Ny][Nzp],
+// addressed by a 4-D tensor map.  (Six 3-D copies per plane, one per
+// component, kept the producer thread issuing for about 1100 cycles after
+// each plane's barrier; it was the last thread to reach the next one.)  The
+// H update uses rows j0-1..j0+TJ-1 and cols k0-4..k0+TK-1 of its box.
+constexpr int EJ = TJ + 2, EK = TK + 8;
+constexpr int HJ = TJ + 1;                 // rows of the new-H plane: j0-1..j0+TJ-1
 constexpr int NS = 5;                      // pipeline stages
 constexpr int NTHREADS = 320;              // 8 tile warps + halo-row warp + halo-column warp
 constexpr int PROD = NTHREADS - 1;         // producer thread (idle lane of the halo-column warp)
 constexpr int align128(int b) { return (b + 127) / 128 * 128; }
-constexpr int E_B = align128(EJ * EK * 4), H_B = align128(HJ * HK * 4);
-constexpr int STAGE_B = 3 * E_B + 3 * H_B;
-constexpr int STAGE_TX = 3 * EJ * EK * 4 + 3 * HJ * HK * 4;  // bytes per stage
+constexpr int C_B = EJ * EK * 4;           // one component's box (dense in the stage)
+constexpr int STAGE_B = align128(6 * C_B);
+constexpr int STAGE_TX = 6 * C_B;          // bytes per stage
 constexpr int HN_COLS = TK + 1;            // new-H plane: cols k0-1..k0+TK-1
 constexpr int HN_B = 3 * HJ * HN_COLS * 4;
-// two new-H planes (alternating per x plane), NS stage barriers, two poll flags
-constexpr int SMEM_B = NS * STAGE_B + 2 * align128(HN_B) + NS * 8 + 16 + 128;  // flags: 3 ints
+constexpr int PF_CAP = 256;                // plasma flags of up to this many planes in shared memory
+// two new-H planes (alternating per x plane), NS stage barriers, two poll
+// flags, the plasma flags of the CTA's planes
+constexpr int SMEM_B = NS * STAGE_B + 2 * align128(HN_B) + NS * 8 + 16 + PF_CAP + 128;  // flags: 3 ints
 constexpr double kE0 = 8.85419e-12;
 
 struct Maps {
-    CUtensorMap E[2][3], H[2][3];
+    CUtensorMap F[2];  // the six components of parity 0 and 1
 };
 
 // CPML and auxiliary-line coefficient tables of one simulation, in global
@@ -158,12 +167,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
         if (globaltimer() - t0 > 2000000000ull) return false;
     }
 }
-__device__ __forceinline__ void tma3(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+__device__ __forceinline__ void tma4(void *dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
                                      uint64_t *bar) {
     asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
-        "%3, %4}], [%5];" ::"r"(smem_u32(dst)),
-        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+        "%3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"((uint64_t)map), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
         : "memory");
 }
 
@@ -185,14 +194,14 @@ struct Stage {
 __device__ __forceinline__ Stage stage_at(unsigned char *base) {
     Stage s;
     for (int c = 0; c < 3; c++) {
-        s.e[c] = (float *)(base + c * E_B);
-        s.h[c] = (float *)(base + 3 * E_B + c * H_B);
+        s.e[c] = (float *)(base + c * C_B);
+        s.h[c] = (float *)(base + (3 + c) * C_B);
     }
     return s;
 }
-// E box element at (j,k) relative to the tile origin: row j - (j0-1), col k - (k0-4)
+// Box element at (j,k) relative to the tile origin: row j - (j0-1), col k - (k0-4)
 #define EIDX(dj, dk) (((dj) + 1) * EK + (dk) + 4)
-#define HIDX(dj, dk) (((dj) + 1) * HK + (dk) + 4)
+#define HIDX(dj, dk) EIDX(dj, dk)
 #define HN(c, dj, dk) hn[((c) * HJ + (dj) + 1) * HN_COLS + (dk) + 1]
 
 struct HVal {
@@ -570,23 +579,32 @@ struct MarchCtx {
     int tile_id;
 };
 
-// Does the tile's block of plane q hold plasma?  (See Args::plasma.)
-__device__ __forceinline__ bool plasma_at(const Args &a, const MarchCtx &c, int q) {
-    return !a.plasma || a.plasma[(size_t)q * a.ntiles + c.tile_id] != 0;
+// Shared-memory layout after the stages and new-H planes: NS stage barriers,
+// three poll flags (16 bytes), then the plasma flags of planes p0, p0+1, ...
+__device__ __forceinline__ unsigned char *pflags(const MarchCtx &c) {
+    return (unsigned char *)(c.bar + NS) + 16;
 }
 
-// Stage of plane q: the E and H boxes.  (J is read from global memory, and
-// only in blocks holding plasma: keeping it out of the stages leaves 15 KB of
-// each CTA's shared memory to L1, which measured faster than staging it.)
+// Does the tile's block of plane q hold plasma?  (See Args::plasma.)  The
+// flags of the CTA's first PF_CAP planes are copied to shared memory when the
+// item starts: read from global memory, the flag's latency (about 500 cycles
+// from L2) sat at the start of every plane.
+__device__ __forceinline__ bool plasma_at(const Args &a, const MarchCtx &c, int q) {
+    if (!a.plasma) return true;
+    const int r = q - c.p0;
+    return r < PF_CAP ? pflags(c)[r] != 0 : a.plasma[(size_t)q * a.ntiles + c.tile_id] != 0;
+}
+
+// Stage of plane q: the six field boxes, one copy.  (J is read from global
+// memory, and only in blocks holding plasma: keeping it out of the stages
+// leaves 15 KB of each CTA's shared memory to L1, which measured faster than
+// staging it.)
 template <int PAR>
 __device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q) {
     const int slot = (q - c.p0) % NS;
-    Stage st = stage_at(c.smem + slot * STAGE_B);
+    unsigned char *dst = c.smem + slot * STAGE_B;
     mbar_arm(&c.bar[slot], STAGE_TX);
-    for (int comp = 0; comp < 3; comp++) {
-        tma3(st.e[comp], &maps.E[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
-        tma3(st.h[comp], &maps.H[PAR][comp], c.k0 - 4, c.j0 - 1, q, &c.bar[slot]);
-    }
+    tma4(dst, &maps.F[PAR], c.k0 - 4, c.j0 - 1, q, 0, &c.bar[slot]);
 }
 
 // The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
@@ -1100,6 +1118,9 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
         for (int s = 0; s < NS; s++) mbar_init(&c.bar[s], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    // Plasma flags of the item's planes, read through plasma_at after the barrier.
+    if (a.plasma && c.tid < PF_CAP && c.tid < c.i_end - c.p0)
+        pflags(c)[c.tid] = a.plasma[(size_t)(c.p0 + c.tid) * a.ntiles + tile_id];
     __syncthreads();
     c.issued = c.p0 - 1;
     if (c.tid == PROD) {
@@ -1499,12 +1520,16 @@ EncodeFn encoder() {
     return fn;
 }
 
+// 4-D map of the six field components of one parity, [6][Nx][Ny][Nzp] floats
+// (k fastest), read as boxes of bk x bj x 1 plane x 6 components.  Elements
+// at k >= Nz or outside the grid read as zero.
 void make_map(CUtensorMap *m, float *base, int Nx, int Ny, int Nz, int Nzp, int bk, int bj) {
-    cuuint64_t dims[3] = {(cuuint64_t)Nz, (cuuint64_t)Ny, (cuuint64_t)Nx};
-    cuuint64_t strides[2] = {(cuuint64_t)Nzp * 4, (cuuint64_t)Ny * Nzp * 4};
-    cuuint32_t box[3] = {(cuuint32_t)bk, (cuuint32_t)bj, 1};
-    cuuint32_t es[3] = {1, 1, 1};
-    CUresult r = encoder()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, es,
+    const cuuint64_t NC = (cuuint64_t)Nx * Ny * Nzp;
+    cuuint64_t dims[4] = {(cuuint64_t)Nz, (cuuint64_t)Ny, (cuuint64_t)Nx, 6};
+    cuuint64_t strides[3] = {(cuuint64_t)Nzp * 4, (cuuint64_t)Ny * Nzp * 4, NC * 4};
+    cuuint32_t box[4] = {(cuuint32_t)bk, (cuuint32_t)bj, 1, 6};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = encoder()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, dims, strides, box, es,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw Error(MFDTD_ECUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
@@ -1626,11 +1651,13 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         a.tb = d;
     }
     const size_t NC = (size_t)P.Nx * P.Ny * m.Nzp;
-    for (int b = 0; b < 2; b++)
+    for (int b = 0; b < 2; b++) {  // one block per parity: Ex Ey Ez Hx Hy Hz (one TMA map)
+        float *f = m.alloc<float>(6 * NC, s);
         for (int c = 0; c < 3; c++) {
-            a.E[b][c] = m.alloc<float>(NC, s);
-            a.H[b][c] = m.alloc<float>(NC, s);
+            a.E[b][c] = f + c * NC;
+            a.H[b][c] = f + (3 + c) * NC;
         }
+    }
     for (int c = 0; c < 3; c++) a.J[c] = m.alloc<float>(NC, s);
     const size_t L2 = 2 * (size_t)P.L;
     const size_t nxs = L2 * P.Ny * P.Nz, nys = (size_t)P.Nx * L2 * P.Nz, nzs = (size_t)P.Nx * P.Ny * L2;
@@ -1700,11 +1727,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     m.dtmp_len = std::max(m.slice_len, (size_t)1);
     m.dtmp = m.alloc<double>(m.dtmp_len, s);
 
-    for (int b = 0; b < 2; b++)
-        for (int c = 0; c < 3; c++) {
-            make_map(&m.maps.E[b][c], a.E[b][c], P.Nx, P.Ny, P.Nz, m.Nzp, EK, EJ);
-            make_map(&m.maps.H[b][c], a.H[b][c], P.Nx, P.Ny, P.Nz, m.Nzp, HK, HJ);
-        }
+    for (int b = 0; b < 2; b++) make_map(&m.maps.F[b], a.E[b][0], P.Nx, P.Ny, P.Nz, m.Nzp, EK, EJ);
 
     {
         auto attr = [](const void *f) {
