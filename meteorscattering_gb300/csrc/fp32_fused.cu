@@ -100,6 +100,10 @@ struct Args {
     // (0): the running DFT on the Huygens surface (k_fp32_ntf), the oblique
     // TF/SF corrections (k_fp32_tfsf).  A batch keeps both inside.
     int ntf_inline, obl_inline;
+    // 1: the pass treats CPML and domain-edge cells like interior ones and the
+    // band kernels (k_fp32_band_h, k_fp32_band_e) recompute them afterwards;
+    // 0: the pass makes the CPML corrections itself (a batch).
+    int band;
     // state
     float *E[2][3], *H[2][3], *J[3];
     float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
@@ -299,8 +303,10 @@ __device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
     const int jlo = j0 - 1, jhi = j0 + TJ, klo = k0 - 1, khi = k0 + TK;
     const int Ny = a.Ny, Nz = a.Nz, L = a.dopml ? a.L : 0;
     bool c = a.doplate == 0;
-    c = c && jlo >= L + 1 && jhi <= Ny - L - 2 && klo >= L + 1 && khi <= Nz - L - 2;
-    c = c && jlo >= 1 && jhi <= Ny - 2 && klo >= 1 && khi <= Nz - 2;
+    if (!a.band) {  // (with the band kernels, CPML and edge rows are fixed after the pass)
+        c = c && jlo >= L + 1 && jhi <= Ny - L - 2 && klo >= L + 1 && khi <= Nz - L - 2;
+        c = c && jlo >= 1 && jhi <= Ny - 2 && klo >= 1 && khi <= Nz - 2;
+    }
     auto clear = [&](int vy, int vz) { return !hits(jlo, jhi, vy) && !hits(klo, khi, vz); };
     if (!a.oblique || a.obl_inline)  // TF/SF rows, when the corrections are made here
         c = c && clear(a.by1 - 1, a.bz1 - 1) && clear(a.by1, a.bz1) && clear(a.by2 - 1, a.bz2 - 1) &&
@@ -314,30 +320,70 @@ __device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
     return ti;
 }
 
-// H half-step of one cell (source/meteor-2.1.cpp:656-937 in FP32).  `dj,dk`
-// are relative to the tile origin; the E box of this plane and of the next
-// plane, and the old H box, are in shared memory.  Components outside their
-// update domain keep their old value.  `store_psi` is false for halo cells
-// computed on behalf of a neighbouring tile.  In a clean tile only the
-// x-dependent special cases (uniform across the CTA) can occur.
-template <int PAR, bool CLEAN>
-__device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int dj, int dk,
-                                       const Stage &s, const Stage &s1, bool store_psi,
-                                       bool want_y, bool want_z, bool tf_in) {
+// Where h_cell reads the old fields of a cell and of its +j, +k and +i
+// neighbours: the stage boxes in shared memory (the pass), or global memory
+// (the CPML band kernels).  A neighbour is read only where the update uses it.
+struct StageSrc {
+    const Stage &s, &s1;
+    int dj, dk;
+    __device__ __forceinline__ float h(int c) const { return s.h[c][HIDX(dj, dk)]; }
+    __device__ __forceinline__ float e(int c) const { return s.e[c][EIDX(dj, dk)]; }
+    __device__ __forceinline__ float ej(int c) const { return s.e[c][EIDX(dj + 1, dk)]; }
+    __device__ __forceinline__ float ek(int c) const { return s.e[c][EIDX(dj, dk + 1)]; }
+    __device__ __forceinline__ float ei(int c) const { return s1.e[c][EIDX(dj, dk)]; }
+};
+struct GlobalSrc {
+    const float *const *E, *const *H;  // the set holding the current state
+    size_t cg, row, plane;
+    __device__ __forceinline__ float h(int c) const { return H[c][cg]; }
+    __device__ __forceinline__ float e(int c) const { return E[c][cg]; }
+    __device__ __forceinline__ float ej(int c) const { return E[c][cg + row]; }
+    __device__ __forceinline__ float ek(int c) const { return E[c][cg + 1]; }
+    __device__ __forceinline__ float ei(int c) const { return E[c][cg + plane]; }
+};
+
+// H half-step of one cell (source/meteor-2.1.cpp:656-937 in FP32), reading
+// the old fields through `src`.  Components outside their update domain keep
+// their old value.  `store_psi` is false for halo cells computed on behalf of
+// a neighbouring tile; `pml` says whether the CPML corrections are made here
+// (the pass leaves them to the band kernels).  In a clean tile only the
+// x-dependent special cases (uniform across the CTA) can occur.  With HOIST
+// the cell's psi values are all loaded before its first update, so that the
+// loads overlap (a psi load placed after another component's psi store cannot
+// be moved above it: the two may alias); the band kernels use it, the pass
+// does not (the registers it holds made the pass spill).
+template <int PAR, bool CLEAN, bool HOIST = false, class Src>
+__device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, const Src &src, bool store_psi,
+                                       bool want_y, bool want_z, bool tf_in, bool pml) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
     HVal o;
-    o.x = s.h[0][HIDX(dj, dk)];
-    o.y = s.h[1][HIDX(dj, dk)];
-    o.z = s.h[2][HIDX(dj, dk)];
-    const float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
+    o.x = src.h(0);
+    o.y = src.h(1);
+    o.z = src.h(2);
+    const float ex = src.e(0), ey = src.e(1), ez = src.e(2);
     const bool xin = i < Nx - 1;
-    const int sx = a.dopml ? hslab(i, Nx, L, a.xshift) : -1;
+    const int sx = pml ? hslab(i, Nx, L, a.xshift) : -1;
     const bool inbx = i >= a.bx1 && i < a.bx2;
     const bool inby = CLEAN ? tf_in : (j >= a.by1 && j < a.by2);
     const bool inbz = CLEAN ? tf_in : (k >= a.bz1 && k < a.bz2);
+    float pp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // HOIST: Ph[PAR][0..5] of this cell
+    if (HOIST && pml) {
+        const int sy = CLEAN ? -1 : hslab(j, Ny, L, a.yshift), sz = CLEAN ? -1 : hslab(k, Nz, L, a.zshift);
+        const bool ux = CLEAN || (j < Ny - 1 && k < Nz - 1);
+        const bool uy = want_y && xin && (CLEAN || k < Nz - 1);
+        const bool uz = want_z && xin && (CLEAN || j < Ny - 1);
+        const size_t oy = ((size_t)i * (2 * L) + sy) * Nz + k, oz = ((size_t)i * Ny + j) * (2 * L) + sz,
+                     ox = ((size_t)sx * Ny + j) * Nz + k;
+        if (ux && sy >= 0) pp[0] = a.Ph[PAR][0][oy];
+        if (ux && sz >= 0) pp[1] = a.Ph[PAR][1][oz];
+        if (uy && sx >= 0) pp[2] = a.Ph[PAR][2][ox];
+        if (uy && sz >= 0) pp[3] = a.Ph[PAR][3][oz];
+        if (uz && sx >= 0) pp[4] = a.Ph[PAR][4][ox];
+        if (uz && sy >= 0) pp[5] = a.Ph[PAR][5][oy];
+    }
     if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
-        const float dEz = s.e[2][EIDX(dj + 1, dk)] - ez;
-        const float dEy = s.e[1][EIDX(dj, dk + 1)] - ey;
+        const float dEz = src.ej(2) - ez;
+        const float dEy = src.ek(1) - ey;
         float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
         if (!CLEAN) {
             if (!a.oblique) {
@@ -354,11 +400,11 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
             } else if (a.obl_inline && obl_shell(a, i, j, k)) {
                 h += obl_corr<PAR, false, 0>(a, i, j, k);
             }
-            if (a.dopml) {
+            if (pml) {
                 const int sy = hslab(j, Ny, L, a.yshift);
                 if (sy >= 0) {
                     const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                    const float p = a.tb->Bh[sy] * a.Ph[PAR][0][o2] + a.tb->Ahy[sy] * dEz;
+                    const float p = a.tb->Bh[sy] * (HOIST ? pp[0] : a.Ph[PAR][0][o2]) + a.tb->Ahy[sy] * dEz;
                     if (store_psi) a.Ph[PAR ^ 1][0][o2] = p;
                     h -= a.c2h * p;
                     if (a.kappa_on) h -= a.c2h * (a.tb->Khy[sy] * dEz);
@@ -366,7 +412,7 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
                 const int sz = hslab(k, Nz, L, a.zshift);
                 if (sz >= 0) {
                     const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                    const float p = a.tb->Bh[sz] * a.Ph[PAR][1][o2] + a.tb->Ahz[sz] * dEy;
+                    const float p = a.tb->Bh[sz] * (HOIST ? pp[1] : a.Ph[PAR][1][o2]) + a.tb->Ahz[sz] * dEy;
                     if (store_psi) a.Ph[PAR ^ 1][1][o2] = p;
                     h += a.c2h * p;
                     if (a.kappa_on) h += a.c2h * (a.tb->Khz[sz] * dEy);
@@ -376,8 +422,8 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         o.x = h;
     }
     if (want_y && xin && (CLEAN || k < Nz - 1)) {
-        const float dEx = s.e[0][EIDX(dj, dk + 1)] - ex;
-        const float dEz = s1.e[2][EIDX(dj, dk)] - ez;
+        const float dEx = src.ek(0) - ex;
+        const float dEz = src.ei(2) - ez;
         float h = a.c1h * o.y - (a.chz * dEx - a.chx * dEz);
         if (!a.oblique) {
             if (inby && inbz) {
@@ -389,16 +435,16 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-            const float p = a.tb->Bh[sx] * a.Ph[PAR][2][o2] + a.tb->Ahx[sx] * dEz;
+            const float p = a.tb->Bh[sx] * (HOIST ? pp[2] : a.Ph[PAR][2][o2]) + a.tb->Ahx[sx] * dEz;
             if (store_psi) a.Ph[PAR ^ 1][2][o2] = p;
             h += a.c2h * p;
             if (a.kappa_on) h += a.c2h * (a.tb->Khx[sx] * dEz);
         }
-        if (!CLEAN && a.dopml) {
+        if (!CLEAN && pml) {
             const int sz = hslab(k, Nz, L, a.zshift);
             if (sz >= 0) {
                 const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                const float p = a.tb->Bh[sz] * a.Ph[PAR][3][o2] + a.tb->Ahz[sz] * dEx;
+                const float p = a.tb->Bh[sz] * (HOIST ? pp[3] : a.Ph[PAR][3][o2]) + a.tb->Ahz[sz] * dEx;
                 if (store_psi) a.Ph[PAR ^ 1][3][o2] = p;
                 h -= a.c2h * p;
                 if (a.kappa_on) h -= a.c2h * (a.tb->Khz[sz] * dEx);
@@ -407,8 +453,8 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         o.y = h;
     }
     if (want_z && xin && (CLEAN || j < Ny - 1)) {
-        const float dEy = s1.e[1][EIDX(dj, dk)] - ey;
-        const float dEx = s.e[0][EIDX(dj + 1, dk)] - ex;
+        const float dEy = src.ei(1) - ey;
+        const float dEx = src.ej(0) - ex;
         float h = a.c1h * o.z - (a.chx * dEy - a.chy * dEx);
         if (!a.oblique) {
             if (inby && inbz) {
@@ -420,16 +466,16 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, int d
         }
         if (sx >= 0) {
             const size_t o2 = ((size_t)sx * Ny + j) * Nz + k;
-            const float p = a.tb->Bh[sx] * a.Ph[PAR][4][o2] + a.tb->Ahx[sx] * dEy;
+            const float p = a.tb->Bh[sx] * (HOIST ? pp[4] : a.Ph[PAR][4][o2]) + a.tb->Ahx[sx] * dEy;
             if (store_psi) a.Ph[PAR ^ 1][4][o2] = p;
             h -= a.c2h * p;
             if (a.kappa_on) h -= a.c2h * (a.tb->Khx[sx] * dEy);
         }
-        if (!CLEAN && a.dopml) {
+        if (!CLEAN && pml) {
             const int sy = hslab(j, Ny, L, a.yshift);
             if (sy >= 0) {
                 const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                const float p = a.tb->Bh[sy] * a.Ph[PAR][5][o2] + a.tb->Ahy[sy] * dEx;
+                const float p = a.tb->Bh[sy] * (HOIST ? pp[5] : a.Ph[PAR][5][o2]) + a.tb->Ahy[sy] * dEx;
                 if (store_psi) a.Ph[PAR ^ 1][5][o2] = p;
                 h += a.c2h * p;
                 if (a.kappa_on) h += a.c2h * (a.tb->Khy[sy] * dEx);
@@ -452,6 +498,191 @@ template <int PAR>
 __device__ __forceinline__ float hzinc_new(const Args &a, int i) {
     const float *ey = a.inc[PAR][0];
     return a.c1h * a.inc[PAR][3][i] - a.chx * (ey[i + 1] - ey[i]);
+}
+
+// Where e_cell reads the new H of the cell's -j, -k and -i neighbours: the
+// new-H planes in shared memory and the previous plane's values kept in
+// registers (the pass), or global memory (the CPML band kernels).
+struct StageHSrc {
+    const float *hn;
+    int dj, dk;
+    float hy_prev, hz_prev;
+    __device__ __forceinline__ float hj(int c) const { return HN(c, dj - 1, dk); }
+    __device__ __forceinline__ float hk(int c) const { return HN(c, dj, dk - 1); }
+    __device__ __forceinline__ float hyi() const { return hy_prev; }
+    __device__ __forceinline__ float hzi() const { return hz_prev; }
+};
+struct GlobalHSrc {
+    const float *const *H;  // the set the pass writes
+    size_t cg, row, plane;
+    __device__ __forceinline__ float hj(int c) const { return H[c][cg - row]; }
+    __device__ __forceinline__ float hk(int c) const { return H[c][cg - 1]; }
+    __device__ __forceinline__ float hyi() const { return H[1][cg - plane]; }
+    __device__ __forceinline__ float hzi() const { return H[2][cg - plane]; }
+};
+
+struct EVal {
+    float x, y, z, z_slice;  // z_slice: Ez before its CPML corrections (the slice value)
+};
+
+// E half-step of one cell (source/meteor-2.1.cpp:1020-1374 in FP32): the old
+// E (ex, ey, ez), the cell's new H (hv), the neighbours' new H through `hs`,
+// the current (jx, jy, jz).  `pml` as in h_cell.
+template <int PAR, bool CLEAN, bool HOIST = false, class HS>
+__device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float ex, float ey, float ez, const HVal &hv,
+                                       const HS &hs, float jx, float jy, float jz, bool tf_in, bool pml) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
+    bool sphere = false;
+    if (!CLEAN && a.doplate == 2) {
+        const double x = a.xc[i], y = a.yc[j], z = a.zc[k];
+        sphere = sqrt(x * x + y * y + z * z) < a.platesize;
+    }
+    const float c1 = sphere ? a.c1s : a.c1e0, c2 = sphere ? a.c2s : a.c2e0;
+    const float cx = sphere ? a.csx : a.cex, cy = sphere ? a.csy : a.cey,
+                cz = sphere ? a.csz : a.cez;
+    const bool plate_row = !CLEAN && a.doplate == 1 && i == a.ssx;
+    const int sxe = pml ? eslab(i, Nx, L, a.xshift) : -1;
+    const bool inby = CLEAN ? tf_in : (j >= a.by1 && j < a.by2);
+    const bool inbz = CLEAN ? tf_in : (k >= a.bz1 && k < a.bz2);
+    float pp[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // HOIST (see h_cell): Pe[0..5] of this cell
+    if (HOIST && pml) {
+        const int sy = CLEAN ? -1 : eslab(j, Ny, L, a.yshift), sz = CLEAN ? -1 : eslab(k, Nz, L, a.zshift);
+        const bool ux = i < Nx - 1 && (CLEAN || (j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1));
+        const bool uy = i >= 1 && i < Nx - 1 && (CLEAN || k >= 1);
+        const bool uz = i >= 1 && i < Nx - 1 && (CLEAN || j >= 1);
+        const bool xp = sxe >= 0 && (CLEAN || (j < Ny - 1 && k < Nz - 1));
+        const size_t oy = ((size_t)i * (2 * L) + sy) * Nz + k, oz = ((size_t)i * Ny + j) * (2 * L) + sz,
+                     ox = ((size_t)sxe * Ny + j) * Nz + k;
+        if (ux && sy >= 0) pp[0] = a.Pe[0][oy];
+        if (ux && sz >= 0) pp[1] = a.Pe[1][oz];
+        if (uy && xp) pp[2] = a.Pe[2][ox];
+        if (uy && sz >= 0 && j < Ny - 1) pp[3] = a.Pe[3][oz];
+        if (uz && xp) pp[4] = a.Pe[4][ox];
+        if (uz && sy >= 0 && k < Nz - 1) pp[5] = a.Pe[5][oy];
+    }
+    // Ex
+    if (i < Nx - 1 && (CLEAN || (j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1))) {
+        const float dHz = hv.z - hs.hj(2);
+        const float dHy = hv.y - hs.hk(1);
+        float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
+        if (!CLEAN) {
+            if (a.oblique) {
+                if (a.obl_inline && obl_shell(a, i, j, k)) e += obl_corr<PAR, true, 0>(a, i, j, k);
+            } else if (i >= a.bx1 && i < a.bx2 - 1) {
+                if (inby) {
+                    if (k == a.bz1) e += a.cez * hyinc_new<PAR>(a, i);
+                    if (k == a.bz2) e -= a.cez * hyinc_new<PAR>(a, i);
+                }
+                if (inbz) {
+                    if (j == a.by1) e -= a.cey * hzinc_new<PAR>(a, i);
+                    if (j == a.by2) e += a.cey * hzinc_new<PAR>(a, i);
+                }
+            }
+            if (pml) {
+                const int sy = eslab(j, Ny, L, a.yshift);
+                if (sy >= 0) {
+                    const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                    const float p = a.tb->Be[sy] * (HOIST ? pp[0] : a.Pe[0][o2]) + a.tb->Aey[sy] * dHz;
+                    a.Pe[0][o2] = p;
+                    e += a.c2e0 * p;
+                    if (a.kappa_on) e += a.c2e0 * (a.tb->Key[sy] * dHz);
+                }
+                const int sz = eslab(k, Nz, L, a.zshift);
+                if (sz >= 0) {
+                    const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                    const float p = a.tb->Be[sz] * (HOIST ? pp[1] : a.Pe[1][o2]) + a.tb->Aez[sz] * dHy;
+                    a.Pe[1][o2] = p;
+                    e -= a.c2e0 * p;
+                    if (a.kappa_on) e -= a.c2e0 * (a.tb->Kez[sz] * dHy);
+                }
+            }
+        }
+        ex = e;
+    }
+    // Ey
+    if (i >= 1 && i < Nx - 1 && (CLEAN || k >= 1)) {
+        const float dHx = hv.x - hs.hk(0);
+        const float dHz = hv.z - hs.hzi();
+        float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
+        if (!a.oblique) {
+            if (inby && inbz) {
+                if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
+                if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
+            }
+        } else if (a.obl_inline && obl_shell(a, i, j, k)) {
+            e += obl_corr<PAR, true, 1>(a, i, j, k);
+        }
+        if (sxe >= 0) {
+            float p = 0.f;
+            if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
+                const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
+                p = a.tb->Be[sxe] * (HOIST ? pp[2] : a.Pe[2][o2]) + a.tb->Aex[sxe] * dHz;
+                a.Pe[2][o2] = p;
+            }
+            e -= a.c2e0 * p;
+            if (a.kappa_on) e -= a.c2e0 * (a.tb->Kex[sxe] * dHz);
+        }
+        if (!CLEAN && pml) {
+            const int sz = eslab(k, Nz, L, a.zshift);
+            if (sz >= 0) {
+                float p = 0.f;
+                if (j < Ny - 1) {
+                    const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
+                    p = a.tb->Be[sz] * (HOIST ? pp[3] : a.Pe[3][o2]) + a.tb->Aez[sz] * dHx;
+                    a.Pe[3][o2] = p;
+                }
+                e += a.c2e0 * p;
+                if (a.kappa_on) e += a.c2e0 * (a.tb->Kez[sz] * dHx);
+            }
+        }
+        ey = e;
+    }
+    if (plate_row && j >= a.plate_lo && j < a.plate_up - 1 && k >= a.plate_lo && k < a.plate_up)
+        ey = 0.f;
+    // Ez
+    const bool ez_plate = plate_row && j >= a.plate_lo && j < a.plate_up &&
+                          k >= a.plate_lo && k < a.plate_up - 1;
+    float ez_slice = ez;
+    if (i >= 1 && i < Nx - 1 && (CLEAN || j >= 1)) {
+        const float dHy = hv.y - hs.hyi();
+        const float dHx = hv.x - hs.hj(0);
+        float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
+        if (!a.oblique) {
+            if (inby && inbz) {
+                if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
+                if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
+            }
+        } else if (a.obl_inline && obl_shell(a, i, j, k)) {
+            e += obl_corr<PAR, true, 2>(a, i, j, k);
+        }
+        if (ez_plate) e = 0.f;
+        ez_slice = e;
+        if (sxe >= 0) {
+            float p = 0.f;
+            if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
+                const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
+                p = a.tb->Be[sxe] * (HOIST ? pp[4] : a.Pe[4][o2]) + a.tb->Aex[sxe] * dHy;
+                a.Pe[4][o2] = p;
+            }
+            e += a.c2e0 * p;
+            if (a.kappa_on) e += a.c2e0 * (a.tb->Kex[sxe] * dHy);
+        }
+        if (!CLEAN && pml) {
+            const int sy = eslab(j, Ny, L, a.yshift);
+            if (sy >= 0 && k < Nz - 1) {
+                const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
+                const float p = a.tb->Be[sy] * (HOIST ? pp[5] : a.Pe[5][o2]) + a.tb->Aey[sy] * dHx;
+                a.Pe[5][o2] = p;
+                e -= a.c2e0 * p;
+                if (a.kappa_on) e -= a.c2e0 * (a.tb->Key[sy] * dHx);
+            }
+        }
+        ez = e;
+    } else if (ez_plate) {
+        ez = 0.f;
+        ez_slice = 0.f;
+    }
+    return EVal{ex, ey, ez, ez_slice};
 }
 
 // The whole 1-D incident line for this step, written to set PAR^1 (one CTA).
@@ -608,8 +839,11 @@ __device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q
 }
 
 // The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
-// or -1.
-template <int PAR, int JM, bool CLEAN>
+// or -1.  FASTONLY (a clean tile whose every plane is an interior one, as
+// with the band kernels, oblique TF/SF corrections after the pass and no
+// record step): the warm-up plane also takes the fast path (its H only), and
+// the general path is not compiled in.
+template <int PAR, int JM, bool CLEAN, bool FASTONLY = false>
 __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &c, int t, int record,
                                      bool tf_in) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
@@ -698,24 +932,27 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         // the box and the corrections are made here, NTF faces when the DFT
         // is accumulated here, the x slice on record steps).  No conditionals
         // per cell; the arithmetic is the same as the general path's.
-        const int xlo = a.dopml ? L + 1 : 1, xhi = a.dopml ? Nx - L - 2 : Nx - 2;
+        const int xlo = a.band ? 0 : a.dopml ? L + 1 : 1, xhi = a.band ? Nx - 1 : a.dopml ? Nx - L - 2 : Nx - 2;
         const bool x_tfsf = (!a.oblique || a.obl_inline) && tf_in &&
                             (i == a.bx1 - 1 || i == a.bx1 || i == a.bx2 - 1);
         const bool x_ntf = a.ntf_inline && (i == a.ntfb || i == Nx - a.ntfb);
-        const bool fast = CLEAN && real && i >= xlo && i <= xhi && !x_ntf && !(record && i == a.ssx) &&
-                          !x_tfsf;
+        const bool fast = FASTONLY || (CLEAN && real && i >= xlo && i <= xhi && !x_ntf &&
+                                        !(record && i == a.ssx) && !x_tfsf);
         if (fast) {
+            // With the band kernels a clean tile may reach past the grid
+            // (`valid` false) or hold domain-edge cells, where J is not
+            // advanced (their E and H are recomputed by the band kernels).
             float jx = 0.f, jy = 0.f, jz = 0.f, exo = 0.f, eyo = 0.f, ezo = 0.f;
             if (tile) {
                 exo = s.e[0][EIDX(dj, dk)];
                 eyo = s.e[1][EIDX(dj, dk)];
                 ezo = s.e[2][EIDX(dj, dk)];
             }
-            if (tile && pl) {
+            if (valid && real && pl) {
                 jx = a.J[0][cg];
                 jy = a.J[1][cg];
                 jz = a.J[2][cg];
-                if (t > 0) {
+                if (t > 0 && (!a.band || (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1))) {
                     const float wq = cwq * G2k;
                     if (JM == 0) {
                         const float nue = cnu * Gk;
@@ -761,24 +998,26 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                     HN(2, dj, dk) = hv.z;
                 }
             }
-            if (tile) {
+            if (valid && real) {
                 a.H[PAR ^ 1][0][cg] = hv.x;
                 a.H[PAR ^ 1][1][cg] = hv.y;
                 a.H[PAR ^ 1][2][cg] = hv.z;
             }
             if (!mid_plane(q)) return q + 2;
-            if (tile) {
-                const float c1 = a.c1e0, c2 = a.c2e0;
-                const float ex = c1 * exo + (a.cey * (hv.z - HN(2, dj - 1, dk)) - a.cez * (hv.y - HN(1, dj, dk - 1))) - c2 * jx;
-                const float ey = c1 * eyo + (a.cez * (hv.x - HN(0, dj, dk - 1)) - a.cex * (hv.z - hz_prev)) - c2 * jy;
-                const float ez = c1 * ezo + (a.cex * (hv.y - hy_prev) - a.cey * (hv.x - HN(0, dj - 1, dk))) - c2 * jz;
-                a.E[PAR ^ 1][0][cg] = ex;
-                a.E[PAR ^ 1][1][cg] = ey;
-                a.E[PAR ^ 1][2][cg] = ez;
-                if (pl) {
-                    a.J[0][cg] = jx;
-                    a.J[1][cg] = jy;
-                    a.J[2][cg] = jz;
+            if (valid) {
+                if (real) {
+                    const float c1 = a.c1e0, c2 = a.c2e0;
+                    const float ex = c1 * exo + (a.cey * (hv.z - HN(2, dj - 1, dk)) - a.cez * (hv.y - HN(1, dj, dk - 1))) - c2 * jx;
+                    const float ey = c1 * eyo + (a.cez * (hv.x - HN(0, dj, dk - 1)) - a.cex * (hv.z - hz_prev)) - c2 * jy;
+                    const float ez = c1 * ezo + (a.cex * (hv.y - hy_prev) - a.cey * (hv.x - HN(0, dj - 1, dk))) - c2 * jz;
+                    a.E[PAR ^ 1][0][cg] = ex;
+                    a.E[PAR ^ 1][1][cg] = ey;
+                    a.E[PAR ^ 1][2][cg] = ez;
+                    if (pl) {
+                        a.J[0][cg] = jx;
+                        a.J[1][cg] = jy;
+                        a.J[2][cg] = jz;
+                    }
                 }
                 ex_prev = exo;
             }
@@ -793,8 +1032,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             jx = a.J[0][cg];
             jy = a.J[1][cg];
             jz = a.J[2][cg];
-            const bool jdom = CLEAN ? (i >= 1 && i < Nx - 1)
-                                    : (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1);
+            const bool jdom = (CLEAN && !a.band)
+                                  ? (i >= 1 && i < Nx - 1)
+                                  : (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1);
             if (t > 0 && jdom) {
                 const float exc = s.e[0][EIDX(dj, dk)], eyc = s.e[1][EIDX(dj, dk)],
                             ezc = s.e[2][EIDX(dj, dk)];
@@ -831,8 +1071,8 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         // ---- H of this plane: tile (all comps), halo row (Hx, Hz), halo column (Hx, Hy)
         HVal hv = {0.f, 0.f, 0.f};
         if (in_grid)
-            hv = h_cell<PAR, CLEAN>(a, i, j, k, dj, dk, s, s1, tile && real, warp != TJ,
-                                    warp != TJ + 1, tf_in);
+            hv = h_cell<PAR, CLEAN>(a, i, j, k, StageSrc{s, s1, dj, dk}, tile && real, warp != TJ,
+                                    warp != TJ + 1, tf_in, a.dopml && !a.band);
         if (c.role_ok) {
             HN(0, dj, dk) = hv.x;
             if (warp != TJ) HN(1, dj, dk) = hv.y;
@@ -847,142 +1087,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
         // ---- E of this plane (tile), source/meteor-2.1.cpp:1020-1374
         if (valid && real) {
-            bool sphere = false;
-            if (!CLEAN && a.doplate == 2) {
-                const double x = a.xc[i], y = a.yc[j], z = a.zc[k];
-                sphere = sqrt(x * x + y * y + z * z) < a.platesize;
-            }
-            const float c1 = sphere ? a.c1s : a.c1e0, c2 = sphere ? a.c2s : a.c2e0;
-            const float cx = sphere ? a.csx : a.cex, cy = sphere ? a.csy : a.cey,
-                        cz = sphere ? a.csz : a.cez;
-            const bool plate_row = !CLEAN && a.doplate == 1 && i == a.ssx;
-            float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
-            const float ex_old = ex;
-            const int sxe = a.dopml ? eslab(i, Nx, L, a.xshift) : -1;
-            const bool inby = CLEAN ? tf_in : (j >= a.by1 && j < a.by2);
-            const bool inbz = CLEAN ? tf_in : (k >= a.bz1 && k < a.bz2);
-            // Ex
-            if (i < Nx - 1 && (CLEAN || (j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1))) {
-                const float dHz = hv.z - HN(2, dj - 1, dk);
-                const float dHy = hv.y - HN(1, dj, dk - 1);
-                float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
-                if (!CLEAN) {
-                    if (a.oblique) {
-                        if (a.obl_inline && obl_shell(a, i, j, k)) e += obl_corr<PAR, true, 0>(a, i, j, k);
-                    } else if (i >= a.bx1 && i < a.bx2 - 1) {
-                        if (inby) {
-                            if (k == a.bz1) e += a.cez * hyinc_new<PAR>(a, i);
-                            if (k == a.bz2) e -= a.cez * hyinc_new<PAR>(a, i);
-                        }
-                        if (inbz) {
-                            if (j == a.by1) e -= a.cey * hzinc_new<PAR>(a, i);
-                            if (j == a.by2) e += a.cey * hzinc_new<PAR>(a, i);
-                        }
-                    }
-                    if (a.dopml) {
-                        const int sy = eslab(j, Ny, L, a.yshift);
-                        if (sy >= 0) {
-                            const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                            const float p = a.tb->Be[sy] * a.Pe[0][o2] + a.tb->Aey[sy] * dHz;
-                            a.Pe[0][o2] = p;
-                            e += a.c2e0 * p;
-                            if (a.kappa_on) e += a.c2e0 * (a.tb->Key[sy] * dHz);
-                        }
-                        const int sz = eslab(k, Nz, L, a.zshift);
-                        if (sz >= 0) {
-                            const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                            const float p = a.tb->Be[sz] * a.Pe[1][o2] + a.tb->Aez[sz] * dHy;
-                            a.Pe[1][o2] = p;
-                            e -= a.c2e0 * p;
-                            if (a.kappa_on) e -= a.c2e0 * (a.tb->Kez[sz] * dHy);
-                        }
-                    }
-                }
-                ex = e;
-            }
-            // Ey
-            if (i >= 1 && i < Nx - 1 && (CLEAN || k >= 1)) {
-                const float dHx = hv.x - HN(0, dj, dk - 1);
-                const float dHz = hv.z - hz_prev;
-                float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
-                if (!a.oblique) {
-                    if (inby && inbz) {
-                        if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
-                        if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
-                    }
-                } else if (a.obl_inline && obl_shell(a, i, j, k)) {
-                    e += obl_corr<PAR, true, 1>(a, i, j, k);
-                }
-                if (sxe >= 0) {
-                    float p = 0.f;
-                    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
-                        const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
-                        p = a.tb->Be[sxe] * a.Pe[2][o2] + a.tb->Aex[sxe] * dHz;
-                        a.Pe[2][o2] = p;
-                    }
-                    e -= a.c2e0 * p;
-                    if (a.kappa_on) e -= a.c2e0 * (a.tb->Kex[sxe] * dHz);
-                }
-                if (!CLEAN && a.dopml) {
-                    const int sz = eslab(k, Nz, L, a.zshift);
-                    if (sz >= 0) {
-                        float p = 0.f;
-                        if (j < Ny - 1) {
-                            const size_t o2 = ((size_t)i * Ny + j) * (2 * L) + sz;
-                            p = a.tb->Be[sz] * a.Pe[3][o2] + a.tb->Aez[sz] * dHx;
-                            a.Pe[3][o2] = p;
-                        }
-                        e += a.c2e0 * p;
-                        if (a.kappa_on) e += a.c2e0 * (a.tb->Kez[sz] * dHx);
-                    }
-                }
-                ey = e;
-            }
-            if (plate_row && j >= a.plate_lo && j < a.plate_up - 1 && k >= a.plate_lo && k < a.plate_up)
-                ey = 0.f;
-            // Ez
-            const bool ez_plate = plate_row && j >= a.plate_lo && j < a.plate_up &&
-                                  k >= a.plate_lo && k < a.plate_up - 1;
-            float ez_slice = ez;
-            if (i >= 1 && i < Nx - 1 && (CLEAN || j >= 1)) {
-                const float dHy = hv.y - hy_prev;
-                const float dHx = hv.x - HN(0, dj - 1, dk);
-                float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
-                if (!a.oblique) {
-                    if (inby && inbz) {
-                        if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
-                        if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
-                    }
-                } else if (a.obl_inline && obl_shell(a, i, j, k)) {
-                    e += obl_corr<PAR, true, 2>(a, i, j, k);
-                }
-                if (ez_plate) e = 0.f;
-                ez_slice = e;
-                if (sxe >= 0) {
-                    float p = 0.f;
-                    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
-                        const size_t o2 = ((size_t)sxe * Ny + j) * Nz + k;
-                        p = a.tb->Be[sxe] * a.Pe[4][o2] + a.tb->Aex[sxe] * dHy;
-                        a.Pe[4][o2] = p;
-                    }
-                    e += a.c2e0 * p;
-                    if (a.kappa_on) e += a.c2e0 * (a.tb->Kex[sxe] * dHy);
-                }
-                if (!CLEAN && a.dopml) {
-                    const int sy = eslab(j, Ny, L, a.yshift);
-                    if (sy >= 0 && k < Nz - 1) {
-                        const size_t o2 = ((size_t)i * (2 * L) + sy) * Nz + k;
-                        const float p = a.tb->Be[sy] * a.Pe[5][o2] + a.tb->Aey[sy] * dHx;
-                        a.Pe[5][o2] = p;
-                        e -= a.c2e0 * p;
-                        if (a.kappa_on) e -= a.c2e0 * (a.tb->Key[sy] * dHx);
-                    }
-                }
-                ez = e;
-            } else if (ez_plate) {
-                ez = 0.f;
-                ez_slice = 0.f;
-            }
+            const float ex_old = s.e[0][EIDX(dj, dk)];
+            const EVal ev = e_cell<PAR, CLEAN>(a, i, j, k, ex_old, s.e[1][EIDX(dj, dk)], s.e[2][EIDX(dj, dk)], hv,
+                                               StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, tf_in,
+                                               a.dopml && !a.band);
+            const float ex = ev.x, ey = ev.y, ez = ev.z, ez_slice = ev.z_slice;
             a.E[PAR ^ 1][0][cg] = ex;
             a.E[PAR ^ 1][1][cg] = ey;
             a.E[PAR ^ 1][2][cg] = ez;
@@ -1043,7 +1152,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 if (i == a.ssx) {
                     a.slE[ox + (size_t)j * Nz + k] = ey;
                     a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = ez_slice;
-                    if (CLEAN || (j < Ny - 1 && k < Nz - 1)) {
+                    if ((CLEAN && !a.band) || (j < Ny - 1 && k < Nz - 1)) {
                         a.slH[ox + (size_t)j * Nz + k] = hv.y;
                         a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = hv.z;
                     }
@@ -1066,7 +1175,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 // whether the CTA's stage mbarriers hold an earlier item's objects (they are
 // invalidated and re-initialised).  Returns false when a bounded wait ran out
 // (the simulation's error flag is then set).
-template <int PAR, int JM>
+template <int PAR, int JM, bool FASTONLY = false>
 __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int tile_id, int chunk,
                                          bool first, int t, int record, unsigned char *smem_raw,
                                          bool inited) {
@@ -1142,8 +1251,12 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     c.valid = tile && c.in_grid;
 
     const TileInfo ti = classify(a, c.j0, c.k0, record);
-    const int fail_q = ti.clean ? march<PAR, JM, true>(maps, a, c, t, record, ti.tf_in)
-                                : march<PAR, JM, false>(maps, a, c, t, record, false);
+    int fail_q;
+    if constexpr (FASTONLY)
+        fail_q = march<PAR, JM, true, true>(maps, a, c, t, 0, ti.tf_in);
+    else
+        fail_q = ti.clean ? march<PAR, JM, true>(maps, a, c, t, record, ti.tf_in)
+                          : march<PAR, JM, false>(maps, a, c, t, record, false);
     if (fail_q >= 0 && c.tid == PROD) {
         atomicOr(a.err, 1u);
         // Let the copies already issued land (bounded) before the CTA exits.
@@ -1170,6 +1283,18 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const bool first = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
     run_item<PAR, JM>(maps, a, a.tile_order[blockIdx.x], blockIdx.z, first, t, record, smem_raw, false);
+}
+
+// The same pass when every tile and plane takes the fast path (Args::band,
+// oblique TF/SF corrections after the pass, no plate or sphere, no record
+// step; see march): without the general path the kernel fits 48 registers,
+// four CTAs per SM.
+template <int PAR, int JM>
+__global__ void __launch_bounds__(NTHREADS, 4)
+    k_fp32_step_fast(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const bool first = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
+    run_item<PAR, JM, true>(maps, a, a.tile_order[blockIdx.x], blockIdx.z, first, t, 0, smem_raw, false);
 }
 
 // ---------------------------------------------------------------------------
@@ -1383,6 +1508,196 @@ __global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_
     if (!a.ntf_inline && a.nntf > 0) ntf_cells(a, t, PAR ^ 1, q0, dq);
 }
 
+// ---------------------------------------------------------------------------
+// CPML band (Args::band).  The pass updates every cell as an interior one; the
+// band kernels then recompute, from the state the pass read, the cells with a
+// coordinate in the first or last `w` indices of an axis (w = L + 1 with the
+// CPML, else 1): the CPML slabs of H and E and the domain edges.  They use
+// h_cell and e_cell with the CPML corrections, so every cell gets the same
+// arithmetic as in the pass's general path, and the results are those of a
+// pass that makes the corrections itself.  Interior cells never read a band
+// H value (E at index n reads H at n and n-1, and H at L-1 and N-L-1 are the
+// first band H cells), so only band cells are rewritten.  The H psi is double
+// buffered and the pass does not touch the E psi, so the recomputation reads
+// the psi of the previous step.
+//
+// Work unit: one warp, up to 32 cells of one (i, j) row: rows (i in band, any
+// j) and (interior i, j in band) in 32-cell segments along k; rows (interior
+// i, interior j) over their 2w band cells k in [0, w) and [Nz-w, Nz), in
+// 32-cell segments of that list.
+struct BandUnits {
+    int w, nseg, nsegz, nx, ny, nz;  // units in the three parts
+};
+__device__ __forceinline__ BandUnits band_units(const Args &a) {
+    BandUnits b;
+    b.w = a.dopml ? a.L + 1 : 1;
+    b.nseg = (a.Nz + 31) / 32;
+    b.nsegz = (2 * b.w + 31) / 32;
+    b.nx = 2 * b.w * a.Ny * b.nseg;
+    b.ny = (a.Nx - 2 * b.w) * 2 * b.w * b.nseg;
+    b.nz = (a.Nx - 2 * b.w) * (a.Ny - 2 * b.w) * b.nsegz;
+    return b;
+}
+// Cell of lane `lane` in unit u; false when the lane has none.
+__device__ __forceinline__ bool band_cell(const Args &a, const BandUnits &b, int u, int lane, int &i, int &j,
+                                          int &k) {
+    const int w = b.w;
+    if (u < b.nx) {
+        const int r = u / b.nseg, sg = u - r * b.nseg, p = r / a.Ny;
+        j = r - p * a.Ny;
+        i = p < w ? p : a.Nx - 2 * w + p;
+        k = sg * 32 + lane;
+        return k < a.Nz;
+    }
+    if ((u -= b.nx) < b.ny) {
+        const int r = u / b.nseg, sg = u - r * b.nseg, p = r / (2 * w), jb = r - p * (2 * w);
+        i = w + p;
+        j = jb < w ? jb : a.Ny - 2 * w + jb;
+        k = sg * 32 + lane;
+        return k < a.Nz;
+    }
+    u -= b.ny;
+    const int r = u / b.nsegz, sg = u - r * b.nsegz, p = r / (a.Ny - 2 * w);
+    i = w + p;
+    j = w + (r - p * (a.Ny - 2 * w));
+    const int m = sg * 32 + lane;  // index in the row's band list
+    k = m < w ? m : a.Nz - 2 * w + m;
+    return m < 2 * w;
+}
+
+// Record-step slice entries of a recomputed cell (the pass's layout and
+// conditions, general path).
+__device__ __forceinline__ void band_slices_e(const Args &a, int i, int j, int k, float ey, float ez_slice) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
+    const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
+    if (k == a.ssz) {
+        a.slE[oz + (size_t)i * Ny + j] = ey;
+        a.slE[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] = ez_slice;
+    }
+    if (j == a.ssy) {
+        a.slE[oy + (size_t)i * Nz + k] = ey;
+        a.slE[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] = ez_slice;
+    }
+    if (i == a.ssx) {
+        a.slE[ox + (size_t)j * Nz + k] = ey;
+        a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = ez_slice;
+    }
+}
+__device__ __forceinline__ void band_slices_h(const Args &a, int i, int j, int k, float hy, float hz) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
+    const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
+    if (k == a.ssz && j < Ny - 1) {
+        a.slH[oz + (size_t)i * Ny + j] = hy;
+        a.slH[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] = hz;
+    }
+    if (j == a.ssy && k < Nz - 1) {
+        a.slH[oy + (size_t)i * Nz + k] = hy;
+        a.slH[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] = hz;
+    }
+    if (i == a.ssx && j < Ny - 1 && k < Nz - 1) {
+        a.slH[ox + (size_t)j * Nz + k] = hy;
+        a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] = hz;
+    }
+}
+
+// Values of a band cell loaded before its update (every load of the cell is
+// then in flight at once; read where h_cell and e_cell use them, a load would
+// wait behind the previous component's psi store, which may alias it).  A
+// neighbour outside the grid reads as zero; the updates never use it.
+struct PreSrc {
+    float hv[3], ev[3], ej[3], ek[3], ei[3];
+    __device__ __forceinline__ float h(int c) const { return hv[c]; }
+    __device__ __forceinline__ float e(int c) const { return ev[c]; }
+};
+struct PreSrcView {
+    const PreSrc &p;
+    __device__ __forceinline__ float h(int c) const { return p.hv[c]; }
+    __device__ __forceinline__ float e(int c) const { return p.ev[c]; }
+    __device__ __forceinline__ float ej(int c) const { return p.ej[c]; }
+    __device__ __forceinline__ float ek(int c) const { return p.ek[c]; }
+    __device__ __forceinline__ float ei(int c) const { return p.ei[c]; }
+};
+struct PreHSrc {
+    float hj[3], hk[3], hyi_, hzi_;
+};
+struct PreHSrcView {
+    const PreHSrc &p;
+    __device__ __forceinline__ float hj(int c) const { return p.hj[c]; }
+    __device__ __forceinline__ float hk(int c) const { return p.hk[c]; }
+    __device__ __forceinline__ float hyi() const { return p.hyi_; }
+    __device__ __forceinline__ float hzi() const { return p.hzi_; }
+};
+
+template <int PAR>
+__global__ void __launch_bounds__(256) k_fp32_band_h(const __grid_constant__ Args a, int record) {
+    const BandUnits b = band_units(a);
+    const int lane = threadIdx.x & 31, total = b.nx + b.ny + b.nz;
+    const size_t row = a.Nzp, plane = (size_t)a.Ny * a.Nzp;
+    for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < total; u += (gridDim.x * blockDim.x) >> 5) {
+        int i, j, k;
+        if (!band_cell(a, b, u, lane, i, j, k)) continue;
+        const size_t cg = (size_t)i * plane + (size_t)j * row + k;
+        const float *const *E = a.E[PAR], *const *H = a.H[PAR];
+        PreSrc ps;
+        for (int c = 0; c < 3; c++) {
+            ps.hv[c] = H[c][cg];
+            ps.ev[c] = E[c][cg];
+        }
+        // neighbours the H update reads: Ez, Ex at +j; Ex, Ey at +k; Ey, Ez at +i
+        const bool jn = j < a.Ny - 1, kn = k < a.Nz - 1, in = i < a.Nx - 1;
+        ps.ej[1] = ps.ek[2] = ps.ei[0] = 0.f;
+        ps.ej[0] = jn ? E[0][cg + row] : 0.f;
+        ps.ej[2] = jn ? E[2][cg + row] : 0.f;
+        ps.ek[0] = kn ? E[0][cg + 1] : 0.f;
+        ps.ek[1] = kn ? E[1][cg + 1] : 0.f;
+        ps.ei[1] = in ? E[1][cg + plane] : 0.f;
+        ps.ei[2] = in ? E[2][cg + plane] : 0.f;
+        const HVal hv = h_cell<PAR, false, true>(a, i, j, k, PreSrcView{ps}, true, true, true, false, a.dopml != 0);
+        a.H[PAR ^ 1][0][cg] = hv.x;
+        a.H[PAR ^ 1][1][cg] = hv.y;
+        a.H[PAR ^ 1][2][cg] = hv.z;
+        if (record) band_slices_h(a, i, j, k, hv.y, hv.z);
+    }
+}
+
+template <int PAR>
+__global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Args a, int record) {
+    const BandUnits b = band_units(a);
+    const int lane = threadIdx.x & 31, total = b.nx + b.ny + b.nz;
+    const size_t row = a.Nzp, plane = (size_t)a.Ny * a.Nzp;
+    for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < total; u += (gridDim.x * blockDim.x) >> 5) {
+        int i, j, k;
+        if (!band_cell(a, b, u, lane, i, j, k)) continue;
+        const size_t cg = (size_t)i * plane + (size_t)j * row + k;
+        const float *const *Hn = a.H[PAR ^ 1];
+        const HVal hv = {Hn[0][cg], Hn[1][cg], Hn[2][cg]};
+        const float ex = a.E[PAR][0][cg], ey = a.E[PAR][1][cg], ez = a.E[PAR][2][cg];
+        // neighbours the E update reads: new Hz, Hx at -j; Hy, Hx at -k; Hy, Hz at -i
+        PreHSrc hs;
+        hs.hj[1] = hs.hk[2] = 0.f;
+        hs.hj[0] = j >= 1 ? Hn[0][cg - row] : 0.f;
+        hs.hj[2] = j >= 1 ? Hn[2][cg - row] : 0.f;
+        hs.hk[0] = k >= 1 ? Hn[0][cg - 1] : 0.f;
+        hs.hk[1] = k >= 1 ? Hn[1][cg - 1] : 0.f;
+        hs.hyi_ = i >= 1 ? Hn[1][cg - plane] : 0.f;
+        hs.hzi_ = i >= 1 ? Hn[2][cg - plane] : 0.f;
+        // J as the pass left it: advanced where the block holds plasma, zero
+        // elsewhere (read only where the block holds plasma).
+        float jx = 0.f, jy = 0.f, jz = 0.f;
+        if (!a.plasma || a.plasma[(size_t)i * a.ntiles + (j / TJ) * a.ntk + k / TK]) {
+            jx = a.J[0][cg];
+            jy = a.J[1][cg];
+            jz = a.J[2][cg];
+        }
+        const EVal ev = e_cell<PAR, false, true>(a, i, j, k, ex, ey, ez, hv, PreHSrcView{hs}, jx, jy, jz, false,
+                                                 a.dopml != 0);
+        a.E[PAR ^ 1][0][cg] = ev.x;
+        a.E[PAR ^ 1][1][cg] = ev.y;
+        a.E[PAR ^ 1][2][cg] = ev.z;
+        if (record) band_slices_e(a, i, j, k, ev.y, ev.z_slice);
+    }
+}
+
 // Slices of the current state (set `cur`) in the record layout, E block
 // (is_h = 0) or H block, optionally minus the incident field inside the
 // total-field region.
@@ -1557,6 +1872,7 @@ struct Fp32Sim::Impl {
     double plasma_fraction = 1.0;  // share of (plane, tile) blocks holding plasma
     std::vector<int> tile_order;   // host copy: boundary tiles first
     int n_boundary = 0;            // how many of them are boundary tiles
+    bool fast_ok = false;          // non-record passes may use k_fp32_step_fast
 
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
@@ -1624,6 +1940,12 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     // TF/SF corrections as kernels of their own after each pass.
     a.ntf_inline = 0;
     a.obl_inline = (P.oblique && P.doplate != 0) ? 1 : 0;
+    // The CPML slabs and domain edges are recomputed by the band kernels
+    // after each pass, where the grid has an interior on every axis.
+    {
+        const int w = P.dopml ? P.L + 1 : 1;
+        a.band = (P.Nx > 2 * w && P.Ny > 2 * w && P.Nz > 2 * w) ? 1 : 0;
+    }
     Tables T;
     std::memset(&T, 0, sizeof T);
     if (P.oblique) {
@@ -1736,6 +2058,14 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         attr((const void *)k_fp32_step<0, 0>); attr((const void *)k_fp32_step<1, 0>);
         attr((const void *)k_fp32_step<0, 1>); attr((const void *)k_fp32_step<1, 1>);
         attr((const void *)k_fp32_step<0, 2>); attr((const void *)k_fp32_step<1, 2>);
+        // Four CTAs of the fast pass need 226 KB of shared memory: ask for the
+        // largest carve-out.
+        auto attr4 = [&](const void *f) {
+            attr(f);
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100), "attr");
+        };
+        attr4((const void *)k_fp32_step_fast<0, 0>); attr4((const void *)k_fp32_step_fast<1, 0>);
+        attr4((const void *)k_fp32_step_fast<0, 1>); attr4((const void *)k_fp32_step_fast<1, 1>);
     }
     m.jm = 0;
     if (P.doB0) {
@@ -1771,8 +2101,10 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         for (int ty = 0; ty < nty; ty++)
             for (int tk = 0; tk < ntk; tk++) {
                 const int jlo = ty * TJ - 1, jhi = ty * TJ + TJ, klo = tk * TK - 1, khi = tk * TK + TK;
-                bool cl = P.doplate == 0 && jlo >= Lc + 1 && jhi <= P.Ny - Lc - 2 && klo >= Lc + 1 &&
-                          khi <= P.Nz - Lc - 2 && jlo >= 1 && jhi <= P.Ny - 2 && klo >= 1 && khi <= P.Nz - 2;
+                bool cl = P.doplate == 0;
+                if (!a.band)
+                    cl = cl && jlo >= Lc + 1 && jhi <= P.Ny - Lc - 2 && klo >= Lc + 1 && khi <= P.Nz - Lc - 2 &&
+                         jlo >= 1 && jhi <= P.Ny - 2 && klo >= 1 && khi <= P.Nz - 2;
                 const int sy[6] = {P.by1 - 1, P.by1, P.by2 - 1, P.by2, P.ntfb, P.Ny - P.ntfb};
                 const int sz[6] = {P.bz1 - 1, P.bz1, P.bz2 - 1, P.bz2, P.ntfb, P.Nz - P.ntfb};
                 const int q0 = (a.oblique && !a.obl_inline) ? 4 : 0, q1 = a.ntf_inline ? 6 : 4;
@@ -1780,6 +2112,11 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                 (cl ? later : order).push_back(ty * ntk + tk);
             }
         m.n_boundary = (int)order.size();
+        // Every tile clean and every plane interior on non-record steps: the
+        // fast pass applies (k_fp32_step_fast; not with the per-k or per-cell
+        // Lee-Kalluri table, whose 18 coefficients do not fit its registers).
+        m.fast_ok = a.band && a.oblique && !a.obl_inline && !a.ntf_inline && P.doplate == 0 && m.jm != 2 &&
+                    m.n_boundary == 0;
         order.insert(order.end(), later.begin(), later.end());
         m.tile_order = order;
         a.tile_order = m.upload(order, s);
@@ -1817,8 +2154,17 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     if (ev) cudaEventRecord((cudaEvent_t)ev[0], s);
     const int rec = record ? 1 : 0;
     auto go = [&](auto kern) { kern<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t, rec); };
+    auto go_fast = [&](auto kern) { kern<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t); };
     // The pass reads the set holding the current state and writes the other.
-    if (m_cur_ == 0) {
+    if (m.fast_ok && !record) {
+        if (m_cur_ == 0) {
+            if (m.jm == 0) go_fast(k_fp32_step_fast<0, 0>);
+            else go_fast(k_fp32_step_fast<0, 1>);
+        } else {
+            if (m.jm == 0) go_fast(k_fp32_step_fast<1, 0>);
+            else go_fast(k_fp32_step_fast<1, 1>);
+        }
+    } else if (m_cur_ == 0) {
         if (m.jm == 0) go(k_fp32_step<0, 0>);
         else if (m.jm == 1) go(k_fp32_step<0, 1>);
         else go(k_fp32_step<0, 2>);
@@ -1828,6 +2174,17 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
         else go(k_fp32_step<1, 2>);
     }
     int launches = 1;
+    if (m.a.band) {
+        const int g = m.sms * 8;
+        if (m_cur_ == 0) {
+            k_fp32_band_h<0><<<g, 256, 0, s>>>(m.a, rec);
+            k_fp32_band_e<0><<<g, 256, 0, s>>>(m.a, rec);
+        } else {
+            k_fp32_band_h<1><<<g, 256, 0, s>>>(m.a, rec);
+            k_fp32_band_e<1><<<g, 256, 0, s>>>(m.a, rec);
+        }
+        launches += 2;
+    }
     if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
     if (m.a.oblique && !m.a.obl_inline) {
         if (m_cur_ == 0) k_fp32_tfsf<0><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
@@ -1949,6 +2306,7 @@ double *const *Fp32Sim::ntf_arrays() const { return impl_->a.ntf; }
 static Args batch_args(const Args &a0, int chunk) {
     Args a = a0;
     if (chunk > 0) a.chunk = chunk;
+    a.band = 0;  // the batched pass makes the CPML corrections itself
     return a;
 }
 
