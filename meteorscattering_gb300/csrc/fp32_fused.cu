@@ -127,6 +127,10 @@ struct Args {
     // neither loads, updates nor stores it there.  Null: plasma everywhere.
     const unsigned char *plasma;
     int ntiles;             // tiles per plane (row length of `plasma`)
+    // Work units of the band kernels (Args::band), one per warp at a time:
+    // x = i | j << 16; y = first cell | count << 16 | band-list flag << 24.
+    const int2 *band_units;
+    int n_band_units;
     double *ntf[24];
     double *probe;       // [6][tsteps][nprobes]
     const int *probe_ijk;
@@ -912,20 +916,24 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     };
 
     float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
-    for (int q = c.p0; q < c.i_end; q++) {
+    // The stage slot of plane q and the cell offset advance with q (no
+    // modulo or 64-bit multiply per plane).
+    int slot = 0;
+    size_t cg = (size_t)c.p0 * plane + col;
+    for (int q = c.p0; q < c.i_end; q++, cg += plane) {
         const int i = q;
         const float cwq = nwq, cnu = nnu;
         const bool pl = npl;  // this plane's block holds plasma
         npl = q + 1 < c.i_end && plasma_at(a, c, q + 1);
         if (npl) pf_load(q + 1, nwq, nnu);
-        const int slot = (q - c.p0) % NS;
+        const int slot1 = slot == NS - 1 ? 0 : slot + 1;
         float *hn = c.hn + (q & 1) * (align128(HN_B) / 4);  // this plane's new-H buffer
         // Stages q and q+1 are resident: the barrier of the previous plane
         // (or the one before the loop) guarantees it.
         const Stage s = stage_at(c.smem + slot * STAGE_B);
-        const Stage s1 = stage_at(c.smem + ((q + 1 - c.p0) % NS) * STAGE_B);
+        const Stage s1 = stage_at(c.smem + slot1 * STAGE_B);
+        slot = slot1;
         const bool real = q >= c.i_begin;
-        const size_t cg = (size_t)i * plane + col;
 
         // Interior fast path: a clean tile on a plane outside the x CPML slabs
         // and away from every x-special plane (TF/SF faces when the tile is in
@@ -1521,48 +1529,22 @@ __global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_
 // buffered and the pass does not touch the E psi, so the recomputation reads
 // the psi of the previous step.
 //
-// Work unit: one warp, up to 32 cells of one (i, j) row: rows (i in band, any
-// j) and (interior i, j in band) in 32-cell segments along k; rows (interior
-// i, interior j) over their 2w band cells k in [0, w) and [Nz-w, Nz), in
-// 32-cell segments of that list.
-struct BandUnits {
-    int w, nseg, nsegz, nx, ny, nz;  // units in the three parts
-};
-__device__ __forceinline__ BandUnits band_units(const Args &a) {
-    BandUnits b;
-    b.w = a.dopml ? a.L + 1 : 1;
-    b.nseg = (a.Nz + 31) / 32;
-    b.nsegz = (2 * b.w + 31) / 32;
-    b.nx = 2 * b.w * a.Ny * b.nseg;
-    b.ny = (a.Nx - 2 * b.w) * 2 * b.w * b.nseg;
-    b.nz = (a.Nx - 2 * b.w) * (a.Ny - 2 * b.w) * b.nsegz;
-    return b;
-}
-// Cell of lane `lane` in unit u; false when the lane has none.
-__device__ __forceinline__ bool band_cell(const Args &a, const BandUnits &b, int u, int lane, int &i, int &j,
-                                          int &k) {
-    const int w = b.w;
-    if (u < b.nx) {
-        const int r = u / b.nseg, sg = u - r * b.nseg, p = r / a.Ny;
-        j = r - p * a.Ny;
-        i = p < w ? p : a.Nx - 2 * w + p;
-        k = sg * 32 + lane;
-        return k < a.Nz;
+// Work unit: one warp, up to 32 cells of one (i, j) row, from a table built
+// at set-up (consecutive units are consecutive segments, so the grid sweeps
+// memory in order): rows (i in band, any j) and (interior i, j in band) in
+// 32-cell segments along k; rows (interior i, interior j) over their 2w band
+// cells k in [0, w) and [Nz-w, Nz) (the band-list flag), in 32-cell segments
+// of that list.
+template <class F>
+__device__ __forceinline__ void for_band_cells(const Args &a, F &&f) {
+    const int lane = threadIdx.x & 31, w = a.dopml ? a.L + 1 : 1;
+    for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < a.n_band_units;
+         u += (gridDim.x * blockDim.x) >> 5) {
+        const int2 e = a.band_units[u];
+        const int i = e.x & 0xffff, j = (unsigned)e.x >> 16, m = (e.y & 0xffff) + lane, n = (e.y >> 16) & 0xff;
+        if (lane >= n) continue;
+        f(i, j, (e.y >> 24) ? (m < w ? m : a.Nz - 2 * w + m) : m);
     }
-    if ((u -= b.nx) < b.ny) {
-        const int r = u / b.nseg, sg = u - r * b.nseg, p = r / (2 * w), jb = r - p * (2 * w);
-        i = w + p;
-        j = jb < w ? jb : a.Ny - 2 * w + jb;
-        k = sg * 32 + lane;
-        return k < a.Nz;
-    }
-    u -= b.ny;
-    const int r = u / b.nsegz, sg = u - r * b.nsegz, p = r / (a.Ny - 2 * w);
-    i = w + p;
-    j = w + (r - p * (a.Ny - 2 * w));
-    const int m = sg * 32 + lane;  // index in the row's band list
-    k = m < w ? m : a.Nz - 2 * w + m;
-    return m < 2 * w;
 }
 
 // Record-step slice entries of a recomputed cell (the pass's layout and
@@ -1630,12 +1612,8 @@ struct PreHSrcView {
 
 template <int PAR>
 __global__ void __launch_bounds__(256) k_fp32_band_h(const __grid_constant__ Args a, int record) {
-    const BandUnits b = band_units(a);
-    const int lane = threadIdx.x & 31, total = b.nx + b.ny + b.nz;
     const size_t row = a.Nzp, plane = (size_t)a.Ny * a.Nzp;
-    for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < total; u += (gridDim.x * blockDim.x) >> 5) {
-        int i, j, k;
-        if (!band_cell(a, b, u, lane, i, j, k)) continue;
+    for_band_cells(a, [&](int i, int j, int k) {
         const size_t cg = (size_t)i * plane + (size_t)j * row + k;
         const float *const *E = a.E[PAR], *const *H = a.H[PAR];
         PreSrc ps;
@@ -1657,17 +1635,13 @@ __global__ void __launch_bounds__(256) k_fp32_band_h(const __grid_constant__ Arg
         a.H[PAR ^ 1][1][cg] = hv.y;
         a.H[PAR ^ 1][2][cg] = hv.z;
         if (record) band_slices_h(a, i, j, k, hv.y, hv.z);
-    }
+    });
 }
 
 template <int PAR>
 __global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Args a, int record) {
-    const BandUnits b = band_units(a);
-    const int lane = threadIdx.x & 31, total = b.nx + b.ny + b.nz;
     const size_t row = a.Nzp, plane = (size_t)a.Ny * a.Nzp;
-    for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < total; u += (gridDim.x * blockDim.x) >> 5) {
-        int i, j, k;
-        if (!band_cell(a, b, u, lane, i, j, k)) continue;
+    for_band_cells(a, [&](int i, int j, int k) {
         const size_t cg = (size_t)i * plane + (size_t)j * row + k;
         const float *const *Hn = a.H[PAR ^ 1];
         const HVal hv = {Hn[0][cg], Hn[1][cg], Hn[2][cg]};
@@ -1695,7 +1669,7 @@ __global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Arg
         a.E[PAR ^ 1][1][cg] = ev.y;
         a.E[PAR ^ 1][2][cg] = ev.z;
         if (record) band_slices_e(a, i, j, k, ev.y, ev.z_slice);
-    }
+    });
 }
 
 // Slices of the current state (set `cur`) in the record layout, E block
@@ -1902,7 +1876,12 @@ int64_t Fp32Sim::footprint(const Problem &P) {
     const int64_t nf2 = 2 * P.nntf();
     const int64_t ntf = 8 * nf2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz + (int64_t)P.Nx * P.Ny);
     const int64_t maps = cells * 4 * ((P.wp3.empty() && !P.has_trail ? 0 : 1) + (P.nu3.empty() ? 0 : 1));
-    return cells * 4 * 15 + maps + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2);
+    // band kernels' unit table (an upper bound) and the plasma-block table
+    const int64_t w = P.dopml ? P.L + 1 : 1, nseg = (P.Nz + 31) / 32, nsegz = (2 * w + 31) / 32;
+    const int64_t band = 8 * (2 * w * P.Ny * nseg + (int64_t)P.Nx * 2 * w * nseg + (int64_t)P.Nx * P.Ny * nsegz);
+    const int64_t ptab = (int64_t)P.Nx * (Nzp / TK) * ((P.Ny + TJ - 1) / TJ);
+    return cells * 4 * 15 + maps + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2) + band +
+           ptab;
 }
 
 void Fp32Sim::init(const Problem &P, void *stream) {
@@ -1944,7 +1923,29 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     // after each pass, where the grid has an interior on every axis.
     {
         const int w = P.dopml ? P.L + 1 : 1;
-        a.band = (P.Nx > 2 * w && P.Ny > 2 * w && P.Nz > 2 * w) ? 1 : 0;
+        a.band = (P.Nx > 2 * w && P.Ny > 2 * w && P.Nz > 2 * w && P.Nx < 65536 && P.Ny < 65536 && P.Nz < 65536)
+                     ? 1 : 0;
+        a.band_units = nullptr;
+        a.n_band_units = 0;
+        if (a.band) {  // the band kernels' work units (see for_band_cells)
+            std::vector<int2> u;
+            auto unit = [&](int i, int j, int m0, int n, int list) {
+                u.push_back(make_int2((int)((unsigned)i | ((unsigned)j << 16)),
+                                      m0 | (n << 16) | (list << 24)));
+            };
+            auto full_row = [&](int i, int j) {
+                for (int k0 = 0; k0 < P.Nz; k0 += 32) unit(i, j, k0, std::min(32, P.Nz - k0), 0);
+            };
+            for (int p = 0; p < 2 * w; p++)
+                for (int j = 0; j < P.Ny; j++) full_row(p < w ? p : P.Nx - 2 * w + p, j);
+            for (int i = w; i < P.Nx - w; i++)
+                for (int jb = 0; jb < 2 * w; jb++) full_row(i, jb < w ? jb : P.Ny - 2 * w + jb);
+            for (int i = w; i < P.Nx - w; i++)
+                for (int j = w; j < P.Ny - w; j++)
+                    for (int m0 = 0; m0 < 2 * w; m0 += 32) unit(i, j, m0, std::min(32, 2 * w - m0), 1);
+            a.band_units = m.upload(u, s);
+            a.n_band_units = (int)u.size();
+        }
     }
     Tables T;
     std::memset(&T, 0, sizeof T);
