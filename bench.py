@@ -148,22 +148,33 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
     raise KeyError(kernel)
 
 
-# DRAM traffic / the pass's own compulsory bytes (J and the plasma map in
-# plasma blocks only) of k_fp32_step, measured by ncu on the profiling-size
-# case of each workload (profiles/): the full-size grids are too large for a
-# multi-pass capture, and the halo overhead per cell is a property of the tile
-# geometry, so a full launch's traffic is the ratio times its own bytes.
-TRAFFIC_RATIO = {
-    # profiles/k_fp32_step_trailprof_full.md: 3.026 GB / 2.908 GB
-    "trail768": 3.0262e9 / 2.9082e9,
-}
+# DRAM traffic of one FP32 step (the pass and the two CPML band kernels),
+# measured by ncu on the 128 x 384 x 1024 profiling case of the large-trail
+# workload (profiles/k_fp32_step_trailprof_full.md); the full-size grid is too
+# large for a multi-pass capture.  The pass moves a fixed multiple of its own
+# bytes (E and H everywhere, J and the plasma map in plasma blocks: the tile
+# boxes' halo rows and columns are the excess), a property of the tile shape;
+# the band kernels move a fixed number of bytes per band cell.  A full launch's
+# traffic is both scaled to its grid.
+PASS_TRAFFIC_RATIO = 2.58545e9 / (128 * 384 * 1024 * (48 + 0.0368245 * 28))
+BAND_BYTES_PER_CELL = (0.792253e9 + 0.790285e9) / (26 * 384 * 1024 + 102 * 26 * 1024 + 102 * 358 * 26)
+TRAFFIC_WORKLOADS = ("trail768", "trailprof")
 
 
-def traffic_per_launch(form: str, workload: str, kernel: str, alg: float):
-    """DRAM traffic (read + write bytes) of one launch, or None when no ncu
-    capture of this workload's kernel is recorded."""
-    if form == "fp32" and kernel == "k_fp32_step" and workload in TRAFFIC_RATIO:
-        return alg * TRAFFIC_RATIO[workload]
+def band_cells(p: rd.RunParams, L: int) -> int:
+    """Cells the band kernels recompute: a coordinate in the first or last
+    L + 1 indices of an axis."""
+    w = L + 1
+    return (2 * w * p.Ny * p.Nz + (p.Nx - 2 * w) * 2 * w * p.Nz + (p.Nx - 2 * w) * (p.Ny - 2 * w) * 2 * w)
+
+
+def traffic_per_launch(form: str, workload: str, kernel: str, p: rd.RunParams, L: int, plasma: float,
+                       per_cell_map: bool):
+    """DRAM traffic (read + write bytes) of one step's pass, or None when no
+    ncu capture of this workload's kernels is recorded."""
+    if form == "fp32" and kernel == "k_fp32_step" and workload in TRAFFIC_WORKLOADS:
+        own = p.Nx * p.Ny * p.Nz * (48 + plasma * (24 + (4 if per_cell_map else 0)))
+        return PASS_TRAFFIC_RATIO * own + BAND_BYTES_PER_CELL * band_cells(p, L)
     return None
 
 
@@ -620,7 +631,7 @@ def main():
         roof = {"kernel": dom[0], "bound": "hbm", "achieved": ach, "peak": peak,
                 "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
                 "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom[1],
-                "traffic": traffic_per_launch(args.form, args.workload, dom[0], alg_own),
+                "traffic": traffic_per_launch(args.form, args.workload, dom[0], p, L, plasma, per_cell),
                 "own_bytes": {"plasma_block_fraction": plasma, "bytes_per_launch": alg_own,
                               "achieved": alg_own / (dom[1] * 1e-3) / 1e9,
                               "frac": alg_own / (dom[1] * 1e-3) / 1e9 / peak},
