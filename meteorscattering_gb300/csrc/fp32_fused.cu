@@ -951,7 +951,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             // (`valid` false) or hold domain-edge cells, where J is not
             // advanced (their E and H are recomputed by the band kernels).
             float jx = 0.f, jy = 0.f, jz = 0.f, exo = 0.f, eyo = 0.f, ezo = 0.f;
-            if (tile) {
+            if (c.role_ok) {  // the cell's old E, for J, H and E
                 exo = s.e[0][EIDX(dj, dk)];
                 eyo = s.e[1][EIDX(dj, dk)];
                 ezo = s.e[2][EIDX(dj, dk)];
@@ -991,7 +991,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             }
             HVal hv = {0.f, 0.f, 0.f};
             if (c.role_ok) {
-                const float ex = s.e[0][EIDX(dj, dk)], ey = s.e[1][EIDX(dj, dk)], ez = s.e[2][EIDX(dj, dk)];
+                const float ex = exo, ey = eyo, ez = ezo;
                 hv.x = a.c1h * s.h[0][HIDX(dj, dk)] -
                        (a.chy * (s.e[2][EIDX(dj + 1, dk)] - ez) - a.chz * (s.e[1][EIDX(dj, dk + 1)] - ey));
                 HN(0, dj, dk) = hv.x;
