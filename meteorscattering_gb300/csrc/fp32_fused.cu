@@ -100,6 +100,10 @@ struct Args {
     // (0): the running DFT on the Huygens surface (k_fp32_ntf), the oblique
     // TF/SF corrections (k_fp32_tfsf).  A batch keeps both inside.
     int ntf_inline, obl_inline;
+    // Planes [xbeg, xend) are marched by the pass (x-chunks of `chunk` planes
+    // from xbeg).  The fast pass leaves the band's x planes to the band
+    // kernels (xbeg = L + 1); otherwise 0 and Nx.
+    int xbeg, xend;
     // 1: the pass treats CPML and domain-edge cells like interior ones and the
     // band kernels (k_fp32_band_h, k_fp32_band_e) recompute them afterwards;
     // 0: the pass makes the CPML corrections itself (a batch).
@@ -842,6 +846,36 @@ __device__ __forceinline__ void issue_stage(const Maps &maps, MarchCtx &c, int q
     tma4(dst, &maps.F[PAR], c.k0 - 4, c.j0 - 1, q, 0, &c.bar[slot]);
 }
 
+// Lagged current update of one cell (source/meteor-fork.cpp:1539-1595), the
+// form the fast pass and the band kernels share: J of step t-1 advanced from
+// the E at the start of pass t (exo, eyo, ezo; exim, eyjm, ezkm are Ex at
+// i-1, Ey at j-1, Ez at k-1, used by the node-averaged Lee-Kalluri update).
+// `m`: the 18 Lee-Kalluri coefficients (JM 1, 2).
+template <int JM>
+__device__ __forceinline__ void j_advance(const Args &a, const float *m, float cwq, float cnu, float Gk, float G2k,
+                                          float exo, float eyo, float ezo, float exim, float eyjm, float ezkm,
+                                          float &jx, float &jy, float &jz) {
+    const float wq = cwq * G2k;
+    if (JM == 0) {
+        const float nue = cnu * Gk;
+        const float den = 2.f + nue * a.dtf;
+        const float ca = (2.f - nue * a.dtf) / den;
+        const float cb = (2.f * a.dtf) * wq / den;
+        jx = ca * jx + cb * exo;
+        jy = ca * jy + cb * eyo;
+        jz = ca * jz + cb * ezo;
+    } else {
+        const bool co = a.lk_colocated;
+        const float m0 = co ? exo : 0.5f * (exo + exim);
+        const float m1 = co ? eyo : 0.5f * (eyo + eyjm);
+        const float m2 = co ? ezo : 0.5f * (ezo + ezkm);
+        const float nx = m[0] * jx + m[1] * jy + m[2] * jz + wq * (m[9] * m0 + m[10] * m1 + m[11] * m2);
+        const float ny = m[3] * jx + m[4] * jy + m[5] * jz + wq * (m[12] * m0 + m[13] * m1 + m[14] * m2);
+        const float nz = m[6] * jx + m[7] * jy + m[8] * jz + wq * (m[15] * m0 + m[16] * m1 + m[17] * m2);
+        jx = nx; jy = ny; jz = nz;
+    }
+}
+
 // The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
 // or -1.  FASTONLY (a clean tile whose every plane is an interior one, as
 // with the band kernels, oblique TF/SF corrections after the pass and no
@@ -961,32 +995,15 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 jy = a.J[1][cg];
                 jz = a.J[2][cg];
                 if (t > 0 && (!a.band || (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1))) {
-                    const float wq = cwq * G2k;
-                    if (JM == 0) {
-                        const float nue = cnu * Gk;
-                        const float den = 2.f + nue * a.dtf;
-                        const float ca = (2.f - nue * a.dtf) / den;
-                        const float cb = (2.f * a.dtf) * wq / den;
-                        jx = ca * jx + cb * exo;
-                        jy = ca * jy + cb * eyo;
-                        jz = ca * jz + cb * ezo;
-                    } else {
-                        const bool co = a.lk_colocated;
-                        const float m0 = co ? exo : 0.5f * (exo + ex_prev);
-                        const float m1 = co ? eyo : 0.5f * (eyo + s.e[1][EIDX(dj - 1, dk)]);
-                        const float m2 = co ? ezo : 0.5f * (ezo + s.e[2][EIDX(dj, dk - 1)]);
-                        const float *m = JM == 1 ? a.lku : lkm;
-                        float tbl[JM == 2 ? 18 : 1];
-                        if (JM == 2 && a.lk_mode != LK_PER_K) {
-                            const size_t e = a.lk_mode == LK_PER_IJ ? (size_t)i * Ny + j : cg;
-                            for (int u = 0; u < 18; u++) tbl[u] = a.lk[e * 18 + u];
-                            m = tbl;
-                        }
-                        const float nx = m[0] * jx + m[1] * jy + m[2] * jz + wq * (m[9] * m0 + m[10] * m1 + m[11] * m2);
-                        const float ny = m[3] * jx + m[4] * jy + m[5] * jz + wq * (m[12] * m0 + m[13] * m1 + m[14] * m2);
-                        const float nz = m[6] * jx + m[7] * jy + m[8] * jz + wq * (m[15] * m0 + m[16] * m1 + m[17] * m2);
-                        jx = nx; jy = ny; jz = nz;
+                    const float *m = JM == 1 ? a.lku : lkm;
+                    float tbl[JM == 2 ? 18 : 1];
+                    if (JM == 2 && a.lk_mode != LK_PER_K) {
+                        const size_t e = a.lk_mode == LK_PER_IJ ? (size_t)i * Ny + j : cg;
+                        for (int u = 0; u < 18; u++) tbl[u] = a.lk[e * 18 + u];
+                        m = tbl;
                     }
+                    j_advance<JM>(a, m, cwq, cnu, Gk, G2k, exo, eyo, ezo, ex_prev, s.e[1][EIDX(dj - 1, dk)],
+                                  s.e[2][EIDX(dj, dk - 1)], jx, jy, jz);
                 }
             }
             HVal hv = {0.f, 0.f, 0.f};
@@ -1200,9 +1217,9 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     c.tile_id = tile_id;
     c.k0 = (tile_id % a.ntk) * TK;
     c.j0 = (tile_id / a.ntk) * TJ;
-    c.i_begin = chunk * a.chunk;
-    c.i_end = min(Nx, c.i_begin + a.chunk);
-    if (c.i_begin >= Nx) return true;
+    c.i_begin = a.xbeg + chunk * a.chunk;
+    c.i_end = min(a.xend, c.i_begin + a.chunk);
+    if (c.i_begin >= a.xend) return true;
     c.p0 = max(c.i_begin - 1, 0);
     c.q_last = min(c.i_end, Nx - 1);  // last plane loaded
     const size_t plane = (size_t)Ny * a.Nzp;
@@ -1638,9 +1655,12 @@ __global__ void __launch_bounds__(256) k_fp32_band_h(const __grid_constant__ Arg
     });
 }
 
-template <int PAR>
-__global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Args a, int record) {
+// `xskip`: the pass (k_fp32_step_fast) did not march the band's x planes;
+// their J is advanced here, before their E update, as the pass would.
+template <int PAR, int JM>
+__global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Args a, int record, int t, int xskip) {
     const size_t row = a.Nzp, plane = (size_t)a.Ny * a.Nzp;
+    const int w = a.dopml ? a.L + 1 : 1;
     for_band_cells(a, [&](int i, int j, int k) {
         const size_t cg = (size_t)i * plane + (size_t)j * row + k;
         const float *const *Hn = a.H[PAR ^ 1];
@@ -1662,6 +1682,17 @@ __global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Arg
             jx = a.J[0][cg];
             jy = a.J[1][cg];
             jz = a.J[2][cg];
+            if (JM != 2 && xskip && (i < w || i >= a.Nx - w) && t > 0 && i >= 1 && i < a.Nx - 1 && j >= 1 &&
+                j < a.Ny - 1 && k >= 1 && k < a.Nz - 1) {
+                const size_t ij = (size_t)i * a.Ny + j;
+                const float cwq = a.wq3 ? a.wq3[cg] : a.wq2[ij];
+                const float cnu = JM == 0 ? (a.nu3 ? a.nu3[cg] : a.nu2[ij]) : 0.f;
+                j_advance<JM>(a, a.lku, cwq, cnu, a.G[k], a.G2[k], ex, ey, ez, a.E[PAR][0][cg - plane],
+                              a.E[PAR][1][cg - row], a.E[PAR][2][cg - 1], jx, jy, jz);
+                a.J[0][cg] = jx;
+                a.J[1][cg] = jy;
+                a.J[2][cg] = jz;
+            }
         }
         const EVal ev = e_cell<PAR, false, true>(a, i, j, k, ex, ey, ez, hv, PreHSrcView{hs}, jx, jy, jz, false,
                                                  a.dopml != 0);
@@ -1832,6 +1863,8 @@ void ck(cudaError_t e, const char *what) {
 
 struct Fp32Sim::Impl {
     Args a;
+    Args af;        // the fast pass's Args: the same, over the planes [L + 1, Nx - L - 1)
+    dim3 grid_fast;
     Maps maps;
     std::vector<void *> allocs;
     int64_t bytes = 0;
@@ -2093,6 +2126,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     a.chunk = (P.Nx + chunks - 1) / chunks;
     chunks = (P.Nx + a.chunk - 1) / a.chunk;
     m.grid = dim3(tiles, 1, chunks);
+    a.xbeg = 0;
+    a.xend = P.Nx;
     {
         // Same test as the device's tile classification on non-record steps.
         const int ntk = m.Nzp / TK, nty = (P.Ny + TJ - 1) / TJ;
@@ -2138,6 +2173,18 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         m.plasma_fraction = nb ? (double)np / (double)nb : 0.0;
         a.plasma = d;
     }
+    if (m.fast_ok) {
+        // The fast pass leaves the band's x planes to the band kernels.
+        const int w = P.dopml ? P.L + 1 : 1, len = P.Nx - 2 * w;
+        m.af = a;
+        m.af.xbeg = w;
+        m.af.xend = P.Nx - w;
+        int cf = std::max(1, std::min(len / 16 > 0 ? len / 16 : 1, (want + tiles - 1) / tiles));
+        cf = std::max(cf, (len + 159) / 160);
+        m.af.chunk = (len + cf - 1) / cf;
+        cf = (len + m.af.chunk - 1) / m.af.chunk;
+        m.grid_fast = dim3(tiles, 1, cf);
+    }
     bytes_ = m.bytes;
 }
 
@@ -2155,9 +2202,10 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     if (ev) cudaEventRecord((cudaEvent_t)ev[0], s);
     const int rec = record ? 1 : 0;
     auto go = [&](auto kern) { kern<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t, rec); };
-    auto go_fast = [&](auto kern) { kern<<<m.grid, NTHREADS, SMEM_B, s>>>(m.maps, m.a, t); };
+    auto go_fast = [&](auto kern) { kern<<<m.grid_fast, NTHREADS, SMEM_B, s>>>(m.maps, m.af, t); };
     // The pass reads the set holding the current state and writes the other.
-    if (m.fast_ok && !record) {
+    const bool fast = m.fast_ok && !record;
+    if (fast) {
         if (m_cur_ == 0) {
             if (m.jm == 0) go_fast(k_fp32_step_fast<0, 0>);
             else go_fast(k_fp32_step_fast<0, 1>);
@@ -2176,13 +2224,18 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     }
     int launches = 1;
     if (m.a.band) {
-        const int g = m.sms * 8;
+        const int g = m.sms * 8, xs = fast ? 1 : 0;
+        auto band_e = [&](auto kern) { kern<<<g, 256, 0, s>>>(m.a, rec, t, xs); };
         if (m_cur_ == 0) {
             k_fp32_band_h<0><<<g, 256, 0, s>>>(m.a, rec);
-            k_fp32_band_e<0><<<g, 256, 0, s>>>(m.a, rec);
+            if (m.jm == 0) band_e(k_fp32_band_e<0, 0>);
+            else if (m.jm == 1) band_e(k_fp32_band_e<0, 1>);
+            else band_e(k_fp32_band_e<0, 2>);
         } else {
             k_fp32_band_h<1><<<g, 256, 0, s>>>(m.a, rec);
-            k_fp32_band_e<1><<<g, 256, 0, s>>>(m.a, rec);
+            if (m.jm == 0) band_e(k_fp32_band_e<1, 0>);
+            else if (m.jm == 1) band_e(k_fp32_band_e<1, 1>);
+            else band_e(k_fp32_band_e<1, 2>);
         }
         launches += 2;
     }
