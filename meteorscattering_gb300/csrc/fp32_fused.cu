@@ -1655,8 +1655,9 @@ __global__ void __launch_bounds__(256) k_fp32_band_h(const __grid_constant__ Arg
     });
 }
 
-// `xskip`: the pass (k_fp32_step_fast) did not march the band's x planes;
-// their J is advanced here, before their E update, as the pass would.
+// `xskip`: the pass (k_fp32_step_fast) did not march the band's x planes
+// nor the tile rows wholly inside its y rows; their J is advanced here,
+// before their E update, as the pass would.
 template <int PAR, int JM>
 __global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Args a, int record, int t, int xskip) {
     const size_t row = a.Nzp, plane = (size_t)a.Ny * a.Nzp;
@@ -1682,8 +1683,9 @@ __global__ void __launch_bounds__(256) k_fp32_band_e(const __grid_constant__ Arg
             jx = a.J[0][cg];
             jy = a.J[1][cg];
             jz = a.J[2][cg];
-            if (JM != 2 && xskip && (i < w || i >= a.Nx - w) && t > 0 && i >= 1 && i < a.Nx - 1 && j >= 1 &&
-                j < a.Ny - 1 && k >= 1 && k < a.Nz - 1) {
+            const int j0 = (j / TJ) * TJ;  // the cell's tile row (skipped by the fast pass when in the band)
+            if (JM != 2 && xskip && (i < w || i >= a.Nx - w || j0 + TJ <= w || j0 >= a.Ny - w) && t > 0 &&
+                i >= 1 && i < a.Nx - 1 && j >= 1 && j < a.Ny - 1 && k >= 1 && k < a.Nz - 1) {
                 const size_t ij = (size_t)i * a.Ny + j;
                 const float cwq = a.wq3 ? a.wq3[cg] : a.wq2[ij];
                 const float cnu = JM == 0 ? (a.nu3 ? a.nu3[cg] : a.nu2[ij]) : 0.f;
@@ -2174,16 +2176,24 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         a.plasma = d;
     }
     if (m.fast_ok) {
-        // The fast pass leaves the band's x planes to the band kernels.
+        // The fast pass leaves the band's x planes, and the tile rows lying
+        // wholly in the band's y rows, to the band kernels.
         const int w = P.dopml ? P.L + 1 : 1, len = P.Nx - 2 * w;
         m.af = a;
         m.af.xbeg = w;
         m.af.xend = P.Nx - w;
-        int cf = std::max(1, std::min(len / 16 > 0 ? len / 16 : 1, (want + tiles - 1) / tiles));
+        std::vector<int> inner;
+        for (int tl : m.tile_order) {
+            const int j0 = (tl / a.ntk) * TJ;
+            if (!(j0 + TJ <= w || j0 >= P.Ny - w)) inner.push_back(tl);
+        }
+        m.af.tile_order = m.upload(inner, s);
+        const int tf = std::max(1, (int)inner.size());
+        int cf = std::max(1, std::min(len / 16 > 0 ? len / 16 : 1, (want + tf - 1) / tf));
         cf = std::max(cf, (len + 159) / 160);
         m.af.chunk = (len + cf - 1) / cf;
         cf = (len + m.af.chunk - 1) / m.af.chunk;
-        m.grid_fast = dim3(tiles, 1, cf);
+        m.grid_fast = dim3((unsigned)inner.size(), 1, cf);
     }
     bytes_ = m.bytes;
 }
