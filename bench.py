@@ -152,12 +152,13 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
 # measured by ncu on the 128 x 384 x 1024 profiling case of the large-trail
 # workload (profiles/k_fp32_step_trailprof_full.md); the full-size grid is too
 # large for a multi-pass capture.  The pass moves a fixed multiple of its own
-# bytes (E and H everywhere, J and the plasma map in plasma blocks: the tile
-# boxes' halo rows and columns are the excess), a property of the tile shape;
-# the band kernels move a fixed number of bytes per band cell.  A full launch's
-# traffic is both scaled to its grid.
-PASS_TRAFFIC_RATIO = 2.58545e9 / (128 * 384 * 1024 * (48 + 0.0368245 * 28))
-BAND_BYTES_PER_CELL = (0.792253e9 + 0.790285e9) / (26 * 384 * 1024 + 102 * 26 * 1024 + 102 * 358 * 26)
+# bytes over the cells it marches (E and H, plus J and the plasma map in
+# plasma blocks: the tile boxes' halo rows and columns are the excess), a
+# property of the tile shape; the band kernels move a fixed number of bytes
+# per band cell.  A full launch's traffic is both scaled to its grid.
+TILE_J = 8            # tile rows of the pass
+PASS_TRAFFIC_RATIO = (1.060137e9 + 0.903979e9) / (102 * 368 * 1024 * (48 + 0.0368245 * 28))
+BAND_BYTES_PER_CELL = (0.791891e9 + 0.796273e9) / (26 * 384 * 1024 + 102 * 26 * 1024 + 102 * 358 * 26)
 TRAFFIC_WORKLOADS = ("trail768", "trailprof")
 
 
@@ -168,12 +169,21 @@ def band_cells(p: rd.RunParams, L: int) -> int:
     return (2 * w * p.Ny * p.Nz + (p.Nx - 2 * w) * 2 * w * p.Nz + (p.Nx - 2 * w) * (p.Ny - 2 * w) * 2 * w)
 
 
+def marched_cells(p: rd.RunParams, L: int) -> int:
+    """Cells the fast pass marches: the planes between the band's x planes,
+    without the tile rows lying wholly in the band's y rows."""
+    w = L + 1
+    lo = TILE_J * (w // TILE_J)
+    hi = p.Ny - TILE_J * (-(-(p.Ny - w) // TILE_J))
+    return (p.Nx - 2 * w) * (p.Ny - lo - max(hi, 0)) * p.Nz
+
+
 def traffic_per_launch(form: str, workload: str, kernel: str, p: rd.RunParams, L: int, plasma: float,
                        per_cell_map: bool):
     """DRAM traffic (read + write bytes) of one step's pass, or None when no
     ncu capture of this workload's kernels is recorded."""
     if form == "fp32" and kernel == "k_fp32_step" and workload in TRAFFIC_WORKLOADS:
-        own = p.Nx * p.Ny * p.Nz * (48 + plasma * (24 + (4 if per_cell_map else 0)))
+        own = marched_cells(p, L) * (48 + plasma * (24 + (4 if per_cell_map else 0)))
         return PASS_TRAFFIC_RATIO * own + BAND_BYTES_PER_CELL * band_cells(p, L)
     return None
 
