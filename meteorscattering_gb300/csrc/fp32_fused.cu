@@ -229,10 +229,6 @@ __device__ __forceinline__ bool hits(int lo, int hi, int v) { return v >= lo && 
 // value.  H targets use the line's E of this pass's start; E targets use the
 // line's H of this step, computed here from the start-of-pass line (the line
 // itself is advanced by the first CTA into the other buffer).
-__device__ __forceinline__ bool obl_in(const Args &a, int p0, int p1, int p2) {
-    return p0 >= 2 * a.bx1 && p0 <= 2 * (a.bx2 - 1) && p1 >= 2 * a.by1 && p1 <= 2 * (a.by2 - 1) &&
-           p2 >= 2 * a.bz1 && p2 <= 2 * (a.bz2 - 1);
-}
 __device__ __forceinline__ bool obl_shell(const Args &a, int i, int j, int k) {
     return i >= a.bx1 - 1 && i <= a.bx2 && j >= a.by1 - 1 && j <= a.by2 && k >= a.bz1 - 1 &&
            k <= a.bz2 &&
@@ -329,8 +325,9 @@ __device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
 }
 
 // Where h_cell reads the old fields of a cell and of its +j, +k and +i
-// neighbours: the stage boxes in shared memory (the pass), or global memory
-// (the CPML band kernels).  A neighbour is read only where the update uses it.
+// neighbours: the stage boxes in shared memory (the pass), or the values the
+// CPML band kernels load before the update (PreSrcView).  A neighbour is used
+// only where the update needs it.
 struct StageSrc {
     const Stage &s, &s1;
     int dj, dk;
@@ -339,15 +336,6 @@ struct StageSrc {
     __device__ __forceinline__ float ej(int c) const { return s.e[c][EIDX(dj + 1, dk)]; }
     __device__ __forceinline__ float ek(int c) const { return s.e[c][EIDX(dj, dk + 1)]; }
     __device__ __forceinline__ float ei(int c) const { return s1.e[c][EIDX(dj, dk)]; }
-};
-struct GlobalSrc {
-    const float *const *E, *const *H;  // the set holding the current state
-    size_t cg, row, plane;
-    __device__ __forceinline__ float h(int c) const { return H[c][cg]; }
-    __device__ __forceinline__ float e(int c) const { return E[c][cg]; }
-    __device__ __forceinline__ float ej(int c) const { return E[c][cg + row]; }
-    __device__ __forceinline__ float ek(int c) const { return E[c][cg + 1]; }
-    __device__ __forceinline__ float ei(int c) const { return E[c][cg + plane]; }
 };
 
 // H half-step of one cell (source/meteor-2.1.cpp:656-937 in FP32), reading
@@ -380,8 +368,9 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, const
         const bool ux = CLEAN || (j < Ny - 1 && k < Nz - 1);
         const bool uy = want_y && xin && (CLEAN || k < Nz - 1);
         const bool uz = want_z && xin && (CLEAN || j < Ny - 1);
-        const size_t oy = ((size_t)i * (2 * L) + sy) * Nz + k, oz = ((size_t)i * Ny + j) * (2 * L) + sz,
-                     ox = ((size_t)sx * Ny + j) * Nz + k;
+        // (indices of absent slabs clamped to 0: never used)
+        const size_t oy = ((size_t)i * (2 * L) + max(sy, 0)) * Nz + k,
+                     oz = ((size_t)i * Ny + j) * (2 * L) + max(sz, 0), ox = ((size_t)max(sx, 0) * Ny + j) * Nz + k;
         if (ux && sy >= 0) pp[0] = a.Ph[PAR][0][oy];
         if (ux && sz >= 0) pp[1] = a.Ph[PAR][1][oz];
         if (uy && sx >= 0) pp[2] = a.Ph[PAR][2][ox];
@@ -510,7 +499,8 @@ __device__ __forceinline__ float hzinc_new(const Args &a, int i) {
 
 // Where e_cell reads the new H of the cell's -j, -k and -i neighbours: the
 // new-H planes in shared memory and the previous plane's values kept in
-// registers (the pass), or global memory (the CPML band kernels).
+// registers (the pass), or the values the CPML band kernels load before the
+// update (PreHSrcView).
 struct StageHSrc {
     const float *hn;
     int dj, dk;
@@ -519,14 +509,6 @@ struct StageHSrc {
     __device__ __forceinline__ float hk(int c) const { return HN(c, dj, dk - 1); }
     __device__ __forceinline__ float hyi() const { return hy_prev; }
     __device__ __forceinline__ float hzi() const { return hz_prev; }
-};
-struct GlobalHSrc {
-    const float *const *H;  // the set the pass writes
-    size_t cg, row, plane;
-    __device__ __forceinline__ float hj(int c) const { return H[c][cg - row]; }
-    __device__ __forceinline__ float hk(int c) const { return H[c][cg - 1]; }
-    __device__ __forceinline__ float hyi() const { return H[1][cg - plane]; }
-    __device__ __forceinline__ float hzi() const { return H[2][cg - plane]; }
 };
 
 struct EVal {
@@ -559,8 +541,9 @@ __device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float
         const bool uy = i >= 1 && i < Nx - 1 && (CLEAN || k >= 1);
         const bool uz = i >= 1 && i < Nx - 1 && (CLEAN || j >= 1);
         const bool xp = sxe >= 0 && (CLEAN || (j < Ny - 1 && k < Nz - 1));
-        const size_t oy = ((size_t)i * (2 * L) + sy) * Nz + k, oz = ((size_t)i * Ny + j) * (2 * L) + sz,
-                     ox = ((size_t)sxe * Ny + j) * Nz + k;
+        // (indices of absent slabs clamped to 0: never used)
+        const size_t oy = ((size_t)i * (2 * L) + max(sy, 0)) * Nz + k,
+                     oz = ((size_t)i * Ny + j) * (2 * L) + max(sz, 0), ox = ((size_t)max(sxe, 0) * Ny + j) * Nz + k;
         if (ux && sy >= 0) pp[0] = a.Pe[0][oy];
         if (ux && sz >= 0) pp[1] = a.Pe[1][oz];
         if (uy && xp) pp[2] = a.Pe[2][ox];
@@ -1605,8 +1588,6 @@ __device__ __forceinline__ void band_slices_h(const Args &a, int i, int j, int k
 // neighbour outside the grid reads as zero; the updates never use it.
 struct PreSrc {
     float hv[3], ev[3], ej[3], ek[3], ei[3];
-    __device__ __forceinline__ float h(int c) const { return hv[c]; }
-    __device__ __forceinline__ float e(int c) const { return ev[c]; }
 };
 struct PreSrcView {
     const PreSrc &p;
