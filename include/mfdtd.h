@@ -258,8 +258,10 @@ int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t Nx, int32_t 
 
 /* Per-kernel-class device time of the last mfdtd_sim_advance when the
  * simulation was created with opts.profile set: for class `which` (0, 1, ...)
- * its name, mean duration of one launch in ms, and launch count.  Returns
- * MFDTD_EINVAL when `which` is past the last class. */
+ * its name, mean duration of one launch in ms, and launch count.  A class
+ * may time consecutive launches together: the FP32 form's class 0
+ * ("k_fp32_step") is the pass with the two CPML band kernels that complete
+ * it.  Returns MFDTD_EINVAL when `which` is past the last class. */
 int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t name_len,
                            double *avg_ms, int64_t *launches);
 
