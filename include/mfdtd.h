@@ -239,13 +239,17 @@ int mfdtd_sim_far_field(mfdtd_sim *s, int32_t ndir, const double *theta, const d
  * analysis/meteorNTF.m).  For callers that cannot call cudaMalloc while they
  * run -- a plugin inside a host that owns all device memory, a service that
  * reserves its memory at start-up and forbids allocation afterwards.  The
- * working memory is one fixed array of about 17 MB inside the library, held
- * on every GPU the process uses until it exits.  Limits: each face of the
- * Huygens box at most 2048 cells along either in-plane axis (larger grids:
- * mfdtd_sim_far_field).  All calls share that array, so calls whose GPU work
- * overlaps race and must be serialised by the caller.  The first call on a
- * device looks up the array's device address; make that first call before
- * any stream capture.
+ * working memory is one fixed array of about 17 MB inside the library.  It
+ * is created on a device when the library's far-field module is first used
+ * there (CUDA loads modules lazily), normally by the first call of this
+ * function, and held until the process exits: make one warm-up call per
+ * device at start-up, before the request path and before any stream
+ * capture.  Every call looks the array's device address up again (with the
+ * device current), so a context reset in between is safe.  Limits: each face
+ * of the Huygens box at most 2048 cells along either in-plane axis (larger
+ * grids: mfdtd_sim_far_field); ntfb >= 0.  All calls share that array and see
+ * what the last call left in it, so calls whose GPU work overlaps race and
+ * must be serialised by the caller.
  * ntf_dev: the 24 face arrays on the current device, output_NTF.dat order and
  * layout ([a][b][2*nntf] doubles).  fntf[nntf], srcdft (Eydft[2n] then
  * Ezdft[2n]), theta/phi[ndir] and out[nntf*ndir*3] are host arrays; out has the
@@ -259,9 +263,11 @@ int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t Nx, int32_t 
 /* Per-kernel-class device time of the last mfdtd_sim_advance when the
  * simulation was created with opts.profile set: for class `which` (0, 1, ...)
  * its name, mean duration of one launch in ms, and launch count.  A class
- * may time consecutive launches together: the FP32 form's class 0
- * ("k_fp32_step") is the pass with the two CPML band kernels that complete
- * it.  Returns MFDTD_EINVAL when `which` is past the last class. */
+ * may time consecutive launches together: the FP32 form's class 0 is the
+ * pass with the two CPML band kernels that complete it, named after the pass
+ * kernel(s) that ran in that advance: "k_fp32_step_fast" (every tile and plane
+ * interior, no record step), "k_fp32_step" (the general pass), or both joined
+ * by '+'.  Returns MFDTD_EINVAL when `which` is past the last class. */
 int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t name_len,
                            double *avg_ms, int64_t *launches);
 

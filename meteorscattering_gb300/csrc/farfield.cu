@@ -26,7 +26,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -487,8 +486,13 @@ void far_field_fp64(const Problem &P, double *const ntf[24], const double *srcdf
 // that must not call into the CUDA allocator at all.  This variant keeps its
 // working memory in one file-scope device array instead, so it only needs the
 // inputs and outputs the caller already holds.  Its limits, and the reasons:
-//   * the array is allocated when the library is loaded, on every GPU the
-//     process uses, and is held until the process exits -- so it is small;
+//   * the array belongs to this file's CUDA module.  With lazy module loading
+//     (the CUDA default since 12.2) the module, and with it the array, is
+//     created on each device the first time the process uses a kernel or
+//     symbol of this file there -- typically the first call of this entry
+//     point -- and held until the process exits.  A caller whose request path
+//     must not allocate makes one warm-up call per device at start-up (also
+//     before any stream capture).  The array is small for that reason;
 //   * every call uses the same array, so calls whose GPU work overlaps (on two
 //     streams, or from two threads) race with each other; callers must
 //     serialise them;
@@ -499,11 +503,28 @@ namespace {
 
 constexpr int kStaticDirs = 256;      // directions per pass
 constexpr int kStaticFace = 2048;     // max in-plane face extent (cells)
-constexpr size_t kStaticBytes =
-    (size_t)kStaticDirs * (2 * kStaticFace) * sizeof(double2)   // P and T
-    + (size_t)kStaticDirs * 6 * sizeof(double2)                 // L, N accumulators
-    + (size_t)kStaticDirs * 7 * sizeof(double)                  // theta, phi, r_hat, sigma staging
-    + (size_t)kStaticDirs * sizeof(int) + 4096;                 // identity map + alignment slack
+
+// The regions carve() takes from the array, in order, each rounded up to 256
+// bytes: P and T (one row of kStaticFace phasors per direction), the L and N
+// accumulators (6 complex values per direction), then per direction theta,
+// phi, the three components of r_hat, the three sigma values, and the
+// identity direction map.  The array's size is computed from the same list.
+constexpr size_t kStaticRegions[] = {
+    (size_t)kStaticDirs * kStaticFace * sizeof(double2),   // P
+    (size_t)kStaticDirs * kStaticFace * sizeof(double2),   // T
+    (size_t)kStaticDirs * 6 * sizeof(double2),             // L, N accumulators
+    kStaticDirs * sizeof(double), kStaticDirs * sizeof(double),  // theta, phi
+    kStaticDirs * sizeof(double), kStaticDirs * sizeof(double), kStaticDirs * sizeof(double),  // r_hat
+    (size_t)kStaticDirs * 3 * sizeof(double),              // sigma and its two terms
+    kStaticDirs * sizeof(int),                             // identity direction map
+};
+constexpr size_t round256(size_t b) { return (b + 255) / 256 * 256; }
+constexpr size_t static_bytes() {
+    size_t t = 0;
+    for (size_t b : kStaticRegions) t += round256(b);
+    return t;
+}
+constexpr size_t kStaticBytes = static_bytes();
 __device__ __align__(256) unsigned char g_ff_scratch[kStaticBytes];
 
 struct StaticScratch {
@@ -515,39 +536,33 @@ struct StaticScratch {
 StaticScratch carve(unsigned char *base) {
     StaticScratch sc;
     size_t off = 0;
-    auto take = [&](size_t bytes) {
+    int region = 0;
+    auto take = [&]() {
         unsigned char *p = base + off;
-        off += (bytes + 255) / 256 * 256;
+        off += round256(kStaticRegions[region++]);
         return p;
     };
-    sc.P = (double2 *)take((size_t)kStaticDirs * kStaticFace * sizeof(double2));
-    sc.T = (double2 *)take((size_t)kStaticDirs * kStaticFace * sizeof(double2));
-    sc.acc = (double2 *)take((size_t)kStaticDirs * 6 * sizeof(double2));
-    sc.th = (double *)take(kStaticDirs * sizeof(double));
-    sc.ph = (double *)take(kStaticDirs * sizeof(double));
-    for (int q = 0; q < 3; q++) sc.r[q] = (double *)take(kStaticDirs * sizeof(double));
-    sc.sig = (double *)take((size_t)kStaticDirs * 3 * sizeof(double));
-    sc.umap = (int *)take(kStaticDirs * sizeof(int));
+    sc.P = (double2 *)take();
+    sc.T = (double2 *)take();
+    sc.acc = (double2 *)take();
+    sc.th = (double *)take();
+    sc.ph = (double *)take();
+    for (int q = 0; q < 3; q++) sc.r[q] = (double *)take();
+    sc.sig = (double *)take();
+    sc.umap = (int *)take();
+    if (off != kStaticBytes || region != (int)(sizeof kStaticRegions / sizeof kStaticRegions[0]))
+        throw Error(MFDTD_EINVAL, "allocation-free far field: scratch layout mismatch");
     return sc;
 }
 
-// Device address of g_ff_scratch, looked up once per device with that device
-// current (the host-side symbol is only a stand-in, never a device address).
-constexpr int kMaxDevices = 64;
-std::atomic<unsigned char *> g_scratch_addr[kMaxDevices];
-
+// Device address of g_ff_scratch on the current device.  The host-side symbol
+// is only a stand-in, never a device address, so the address is looked up
+// with the device current -- on every call: a cached address would go stale
+// when the context is torn down (cudaDeviceReset) and the module reloaded.
 unsigned char *scratch_for_current_device() {
-    int dev = 0;
-    ck(cudaGetDevice(&dev), "cudaGetDevice");
-    if (dev < 0 || dev >= kMaxDevices) throw Error(MFDTD_EINVAL, "device ordinal out of range");
-    unsigned char *p = g_scratch_addr[dev].load(std::memory_order_acquire);
-    if (!p) {
-        void *addr = nullptr;
-        ck(cudaGetSymbolAddress(&addr, g_ff_scratch), "cudaGetSymbolAddress");
-        p = (unsigned char *)addr;
-        g_scratch_addr[dev].store(p, std::memory_order_release);
-    }
-    return p;
+    void *addr = nullptr;
+    ck(cudaGetSymbolAddress(&addr, g_ff_scratch), "cudaGetSymbolAddress");
+    return (unsigned char *)addr;
 }
 
 __global__ void k_ff_dirs(const double *th, const double *ph, int n, double *rx, double *ry, double *rz,
@@ -578,6 +593,7 @@ extern "C" int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t N
             throw Error(MFDTD_EINVAL, "NULL argument or empty direction/frequency list");
         for (int q = 0; q < 24; q++)
             if (!ntf_dev[q]) throw Error(MFDTD_EINVAL, "NULL face array");
+        if (ntfb < 0) throw Error(MFDTD_EINVAL, "ntfb < 0: the Huygens faces lie outside the grid");
         const int dims[3] = {Nx, Ny, Nz};
         for (int q = 0; q < 3; q++)
             if (dims[q] - 2 * ntfb + 1 > kStaticFace || dims[q] - 2 * ntfb < 1)

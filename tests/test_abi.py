@@ -115,3 +115,8 @@ def test_static_far_field_rejects_oversize_faces(built):
                                     dp(one), dp(one), dp(out), None)
     assert E.STATUS[rc] == "EINVAL"
     assert "2048" in E.last_error()
+    # a negative Huygens offset would place the faces before the arrays' start
+    rc = lib.mfdtd_far_field_static(fake, 64, 64, 64, -1, 1, dp(one), 0.2, 0.2, 0.2, dp(one), 1,
+                                    dp(one), dp(one), dp(out), None)
+    assert E.STATUS[rc] == "EINVAL"
+    assert "ntfb" in E.last_error()

@@ -7,8 +7,11 @@ path.  It keeps its working memory in one fixed array inside the library.
 This test feeds it DFT sums held in device buffers owned by the caller, calls
 it twice in a row (the second call sees the array as the first left it), and
 requires both results to equal the allocating mfdtd_sim_far_field within
-1e-9 relative.  It is collected last so that a run stopping at the first
-failure has already run every other test.
+1e-9 relative.  The first call may load the library's far-field module on
+the device (CUDA loads modules lazily), which creates the fixed array; the
+second call must leave the device's free memory exactly as it found it.  It
+is collected last so that a run stopping at the first failure has already run
+every other test.
 """
 import ctypes as C
 import math
@@ -54,7 +57,12 @@ def test_static_far_field_matches_allocating_far_field(built):
     dp = lambda x: x.ctypes.data_as(C.POINTER(C.c_double))
     for call in range(2):
         out = np.full((p.nntf, th.size, 3), np.nan)
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(0)[0]
         rc = lib.mfdtd_far_field_static(ptrs, p.Nx, p.Ny, p.Nz, 15, p.nntf, dp(fntf), p.dx, p.dx,
                                         p.dx, dp(srcdft), th.size, dp(th), dp(ph), dp(out), None)
         assert rc == 0, E.last_error()
+        free_after = torch.cuda.mem_get_info(0)[0]
         np.testing.assert_allclose(out, want, rtol=1e-9, atol=1e-300, err_msg=f"call {call}")
+        if call == 1:  # the module (and its array) exists now: nothing may be allocated
+            assert free_after == free_before, (free_before, free_after)
