@@ -53,21 +53,27 @@ FALLBACK_HBM_GBS = 6800.0
 # Workloads
 
 
+TRAIL_GRIDS = {"trail768": (768, 768, 1536), "trailprof": (128, 384, 1024),
+               "trail384": (384, 384, 768), "trail96": (96, 96, 192)}
+
+
 def workload(name: str, steps_total: int):
     """(RunParams, wp2 [Nx][Ny] C-order, nu2, B0, description, MATLAB-shaped wp,
     ExtParams or None, TrailParams or None)."""
     B0 = (5e-5 * math.cos(math.pi / 3), 0.0, -5e-5 * math.sin(math.pi / 3))  # 60 deg dip
     ext = trail = None
-    if name in ("trail768", "trailprof"):
+    if name in TRAIL_GRIDS:
         # Large single trail: 768 x 768 x 1536 cells (trailprof: 128 x 384 x 1024,
-        # the profiling-size case with the same physics), dx = 0.2 m (50 MHz
-        # radar, gridfactor 30), 12-cell CPML graded m = 3, kappa_max = 5,
-        # alpha_max = 0.05; trail axis tilted 30 degrees from z in the x-z plane,
-        # log10 n0 rising linearly from 13 to 16 along it, r0 = 0.8 m; nu = 3e4;
-        # B0 = 5e-5 T dipped 60 degrees; oblique TM plane wave along
-        # (theta, phi) = (70, 20) degrees; Lee-Kalluri current driven by E at the
-        # current's node (the reference's two-node average diverges here).
-        N = (768, 768, 1536) if name == "trail768" else (128, 384, 1024)
+        # the profiling-size case; trail384: 384 x 384 x 768, the precision
+        # check; trail96: 96 x 96 x 192, the parity test; all with the same
+        # physics), dx = 0.2 m (50 MHz radar, gridfactor 30), 12-cell CPML
+        # graded m = 3, kappa_max = 5, alpha_max = 0.05; trail axis tilted 30
+        # degrees from z in the x-z plane, log10 n0 rising linearly from 13 to
+        # 16 along it, r0 = 0.8 m; nu = 3e4; B0 = 5e-5 T dipped 60 degrees;
+        # oblique TM plane wave along (theta, phi) = (70, 20) degrees;
+        # Lee-Kalluri current driven by E at the current's node (the
+        # reference's two-node average diverges here).
+        N = TRAIL_GRIDS[name]
         f0, gf, nu = 50e6, 30.0, 3e4
         desc = (f"{N[0]}x{N[1]}x{N[2]} tilted magnetized trail, dx=0.2 m, 12-cell CPML "
                 "(m=3, kappa_max=5, alpha_max=0.05), trail axis 30 deg from z in x-z, "
@@ -182,7 +188,7 @@ def traffic_per_launch(form: str, workload: str, kernel: str, p: rd.RunParams, L
                        per_cell_map: bool):
     """DRAM traffic (read + write bytes) of one step's pass, or None when no
     ncu capture of this workload's kernels is recorded."""
-    if form == "fp32" and kernel == "k_fp32_step" and workload in TRAFFIC_WORKLOADS:
+    if form == "fp32" and kernel.startswith("k_fp32_step") and workload in TRAFFIC_WORKLOADS:
         own = marched_cells(p, L) * (48 + plasma * (24 + (4 if per_cell_map else 0)))
         return PASS_TRAFFIC_RATIO * own + BAND_BYTES_PER_CELL * band_cells(p, L)
     return None
@@ -556,6 +562,65 @@ def mie_bench(args, steps: int = 4000, courant: float = 0.5):
     print(json.dumps(line), flush=True)
 
 
+def precision_bench(args, steps: int = 4000):
+    """FP32 fused against FP64 plain on the large-trail physics at 384 x 384 x
+    768 cells (half the 768 x 768 x 1536 benchmark grid along each axis; the
+    full size in FP64 would take about 37 minutes), 4000 steps: relative L2 of
+    every field component after the last step and of the DFT sums, and the
+    bistatic RCS dB error on the 2-degree theta/phi grid (max and p99 over the
+    directions within 30 dB of the peak)."""
+    from meteorscattering_gb300 import build as B
+    B.build()
+    from meteorscattering_gb300 import engine as E
+    from meteorscattering_gb300 import sweep
+    steps = args.steps if args.steps > 100 else steps
+    p, wp2, nu2, B0, desc, _, ext, trail = workload("trail384", steps)
+    th, ph = sweep.direction_grid(2.0)
+    res, secs = {}, {}
+    for form in (E.FORM_FP32_FUSED, E.FORM_FP64_PLAIN):
+        sim = E.Simulation(make_problem(E, p, wp2, nu2, B0, ext, trail), form=form)
+        t0 = time.perf_counter()
+        sim.advance(steps)
+        sim.sync()
+        secs[form] = time.perf_counter() - t0
+        res[form] = {"rcs": sim.far_field(th, ph, method=0)[..., 0],
+                     "ntf": sim.read_ntf()[4 * p.nntf:]}
+        if form == E.FORM_FP32_FUSED:
+            res[form]["fields"] = [sim.read_field(c) for c in range(6)]
+        else:  # compared one component at a time (each is 0.9 GB in FP64)
+            res["field_rel_l2"] = {}
+            for c, n in enumerate(("Ex", "Ey", "Ez", "Hx", "Hy", "Hz")):
+                y = sim.read_field(c)
+                x = res[E.FORM_FP32_FUSED]["fields"][c]
+                res["field_rel_l2"][n] = float(np.linalg.norm((x - y).ravel()) / np.linalg.norm(y.ravel()))
+                res[E.FORM_FP32_FUSED]["fields"][c] = None
+        if form == E.FORM_FP32_FUSED:
+            res["tc"] = sim.far_field(th, ph, method=1)[..., 0]
+        sim.close()
+    a, b = res[E.FORM_FP32_FUSED], res[E.FORM_FP64_PLAIN]
+
+    def rel(x, y):
+        return float(np.linalg.norm((x - y).ravel()) / np.linalg.norm(y.ravel()))
+
+    mask = b["rcs"] > b["rcs"].max(axis=1, keepdims=True) * 1e-3
+    db = np.abs(10 * np.log10(a["rcs"][mask] / b["rcs"][mask]))
+    dbtc = np.abs(10 * np.log10(res["tc"][mask] / b["rcs"][mask]))
+    line = {"metric": "RCS error, FP32 fused vs FP64 plain", "value": float(db.max()),
+            "unit": "dB (max over the 2-degree directions within 30 dB of the peak)",
+            "higher_is_better": False, "n_gpus": 1, "steps": steps, "dtype": "f32 vs f64",
+            "data": "synthetic",
+            "config": {"workload": desc, "grid": [p.Nx, p.Ny, p.Nz], "directions": int(th.size)},
+            "rcs_db_max": float(db.max()), "rcs_db_p99": float(np.percentile(db, 99)),
+            "rcs_db_max_tensor_cores_vs_fp64_plain": float(dbtc.max()),
+            "directions_within_30db": int(mask.sum()),
+            "field_rel_l2": res["field_rel_l2"],
+            "dft_sums_rel_l2": rel(a["ntf"], b["ntf"]),
+            "seconds": {"fp32_fused": secs[E.FORM_FP32_FUSED], "fp64_plain": secs[E.FORM_FP64_PLAIN]},
+            "ms_per_step": {"fp32_fused": 1e3 * secs[E.FORM_FP32_FUSED] / steps,
+                            "fp64_plain": 1e3 * secs[E.FORM_FP64_PLAIN] / steps}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -576,6 +641,9 @@ def main():
         return
     if args.workload == "mie" and args.impl == "gb300":
         mie_bench(args)
+        return
+    if args.workload == "precision384" and args.impl == "gb300":
+        precision_bench(args)
         return
     K, W = args.steps, max(args.warmup, 0)
 
@@ -632,23 +700,31 @@ def main():
     peak, peak_kind = load_peaks()
     roof = None
     if dom:
-        # achieved: the per-cell-update figure of the hot-path table (76 B for the
-        # FP32 pass: E, H, J read and written, plus the plasma map) x cells;
-        # own: the bytes this pass must move, J and the map in plasma blocks only
-        alg = algorithmic_bytes(args.form, dom[0], p, L, per_cell)
+        # achieved / frac: the bytes this step must move (E and H read and
+        # written everywhere; J and the per-cell plasma map read and written in
+        # the (plane, tile) blocks holding plasma only, since J is identically
+        # zero elsewhere; every psi cell of both half-steps read and written)
+        # over the dominant launch's time.  per_cell_update: the same launch
+        # against the per-cell-update figure of the hot-path table (76 B for
+        # the FP32 pass with J and the map counted in every cell), which counts
+        # J traffic the pass does not have and so is not a DRAM efficiency.
+        alg76 = algorithmic_bytes(args.form, dom[0], p, L, per_cell)
         alg_own = algorithmic_bytes(args.form, dom[0], p, L, per_cell, plasma)
-        ach = alg / (dom[1] * 1e-3) / 1e9
+        secs = dom[1] * 1e-3
+        ach = alg_own / secs / 1e9
+        traffic = traffic_per_launch(args.form, args.workload, dom[0], p, L, plasma, per_cell)
         roof = {"kernel": dom[0], "bound": "hbm", "achieved": ach, "peak": peak,
                 "unit": "GB/s", "frac": ach / peak, "peak_source": peak_kind,
-                "algorithmic_bytes_per_launch": alg, "avg_launch_ms": dom[1],
-                "traffic": traffic_per_launch(args.form, args.workload, dom[0], p, L, plasma, per_cell),
-                "own_bytes": {"plasma_block_fraction": plasma, "bytes_per_launch": alg_own,
-                              "achieved": alg_own / (dom[1] * 1e-3) / 1e9,
-                              "frac": alg_own / (dom[1] * 1e-3) / 1e9 / peak},
+                "algorithmic_bytes_per_launch": alg_own, "avg_launch_ms": dom[1],
+                "plasma_block_fraction": plasma,
+                "traffic": traffic,
+                "traffic_over_algorithmic": traffic / alg_own if traffic else None,
+                "per_cell_update": {"bytes_per_launch": alg76, "achieved": alg76 / secs / 1e9,
+                                    "frac": alg76 / secs / 1e9 / peak},
                 "kernel_times_ms": {n: m for n, m, c in kstats},
                 # the same compulsory bytes over the whole step (every kernel of it)
-                "step_achieved": alg / (ms_step * 1e-3) / 1e9,
-                "step_frac": alg / (ms_step * 1e-3) / 1e9 / peak}
+                "step_achieved": alg_own / (ms_step * 1e-3) / 1e9,
+                "step_frac": alg_own / (ms_step * 1e-3) / 1e9 / peak}
 
     # end to end through the public API from host buffers
     e2e = None
@@ -685,8 +761,7 @@ def main():
                            "form": "fp32_fused" if args.form == "fp32" else "fp64_plain",
                            "parallelism": f"replicas x{world}",
                            "l2": "state larger than L2 (no flush needed)"},
-                "hbm_gbs": (algorithmic_bytes(args.form, dom[0], p, L, per_cell, plasma) / (dom[1] * 1e-3) / 1e9)
-                if dom else None,
+                "hbm_gbs": roof["achieved"] if roof else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
                 "gpu_launches": launches, "host_wall_s": wall}
         print(json.dumps(line), flush=True)

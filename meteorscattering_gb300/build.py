@@ -99,10 +99,10 @@ def build_oracle(with_reference: bool = True) -> None:
     if make is None:
         raise RuntimeError("make not found")
     subprocess.run([make, "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    refsrc = os.environ.get("MFDTD_REFSRC", "/root/reference/source")
-    if with_reference and os.path.isdir(refsrc):
-        subprocess.run([make, "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REFSRC={refsrc}"],
-                       check=True)
+    if with_reference:
+        # The recipe knows where the reference sources lie (REFSRC, or the
+        # MFDTD_REFSRC environment variable) and skips them when absent.
+        subprocess.run([make, "-s", "-C", os.path.join(ROOT, "oracle"), "ref-if-present"], check=True)
 
 
 if __name__ == "__main__":

@@ -16,6 +16,10 @@ public:
     // (may be null) receives kernel_classes()+1 boundary events.
     int step(int t, bool record, void *stream, void *const *ev);
     static int kernel_classes();
+    // Passes run so far by the fast kernel (k_fp32_step_fast: every tile and
+    // plane interior, no record step) and by the general one (k_fp32_step).
+    long long fast_passes() const;
+    long long general_passes() const;
     // Current-update kind of this simulation's kernel (0 Young DI, 1 uniform
     // Lee-Kalluri, 2 tabulated Lee-Kalluri); batches group by it.
     int current_update() const;

@@ -1863,6 +1863,7 @@ struct Fp32Sim::Impl {
     std::vector<int> tile_order;   // host copy: boundary tiles first
     int n_boundary = 0;            // how many of them are boundary tiles
     bool fast_ok = false;          // non-record passes may use k_fp32_step_fast
+    long long n_fast = 0, n_general = 0;  // passes run by each pass kernel
 
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
@@ -2182,6 +2183,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
 double Fp32Sim::plasma_fraction() const { return impl_->plasma_fraction; }
 
 int Fp32Sim::kernel_classes() { return 3; }
+long long Fp32Sim::fast_passes() const { return impl_->n_fast; }
+long long Fp32Sim::general_passes() const { return impl_->n_general; }
 int Fp32Sim::current_update() const { return impl_->jm; }
 const char *Fp32Sim::kernel_name(int which) {
     return which == 0 ? "k_fp32_step" : which == 1 ? "k_fp32_tfsf" : "k_fp32_ntf";
@@ -2196,6 +2199,7 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     auto go_fast = [&](auto kern) { kern<<<m.grid_fast, NTHREADS, SMEM_B, s>>>(m.maps, m.af, t); };
     // The pass reads the set holding the current state and writes the other.
     const bool fast = m.fast_ok && !record;
+    (fast ? m.n_fast : m.n_general) += 1;
     if (fast) {
         if (m_cur_ == 0) {
             if (m.jm == 0) go_fast(k_fp32_step_fast<0, 0>);

@@ -394,6 +394,7 @@ struct mfdtd_sim {
             }
         }
         mfdtd::ck(cudaEventRecord(ev0, stream), "cudaEventRecord");
+        const long long fast0 = f32 ? f32->fast_passes() : 0, gen0 = f32 ? f32->general_passes() : 0;
         const int t_begin = t, t_end = t + nsteps;
         for (; t < t_end; t++) {
             const bool rec = (t % P.record_period) == 0;
@@ -420,6 +421,12 @@ struct mfdtd_sim {
         mfdtd::ck(cudaEventRecord(ev1, stream), "cudaEventRecord");
         mfdtd::ck(cudaGetLastError(), "kernel launch");
         last_launches = launches;
+        if (prof_steps && f32) {
+            // Class 0 of the FP32 form is the pass with its band kernels; name
+            // the pass kernel(s) that ran in this advance.
+            const bool fast = f32->fast_passes() > fast0, gen = f32->general_passes() > gen0;
+            kname[0] = fast && gen ? "k_fp32_step_fast+k_fp32_step" : fast ? "k_fp32_step_fast" : "k_fp32_step";
+        }
         if (nsteps > 0) {
             wait();
             drain_records();

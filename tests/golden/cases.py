@@ -139,3 +139,44 @@ def write_trail_case(d, case):
     rd.write_rundir(d, p, wp, nu, B0)
     rd.write_ext(d, ext)
     rd.write_trail(d, tr)
+
+
+def plate_case(N=128, plate_wavelengths=3.0, steps=2000):
+    """The reference's far-field calibration run (doplate = 1,
+    analysis/meteorNTF.m:346-349) in reference-format inputs: a square PEC
+    plate of side `plate_wavelengths` wavelengths at f0 = 100 MHz, 24 cells
+    per wavelength, a Gaussian-modulated pulse along +x (E along z) of
+    bandwidth f0 / 4, DFT at 0.8, 0.9, 1.0, 1.1 and 1.2 f0."""
+    f0, gf = 100e6, 24.0
+    lam = rd.C0 / f0
+    dt = rd.stable_dt(lam / gf)
+    fntf = list(np.array([0.8, 0.9, 1.0, 1.1, 1.2]) * f0)
+    p = rd.RunParams(Nx=N, Ny=N, Nz=N, tsteps=steps, dt=dt, f0=f0,
+                     fsig=1 / (2 * math.pi * 0.25 * f0 * dt), gridfactor=gf, numfiles=1,
+                     savefields=0, fntf=fntf, doplate=1, platesize=plate_wavelengths * lam,
+                     metsize=(1e200, 1e200), doB0=0, probex=[], probey=[], probez=[])
+    return p, np.zeros((N, N)), np.zeros((N, N)), (0.0, 0.0, 0.0)
+
+
+def plate_physical_optics(p):
+    """sigma = 4 pi a^4 f^2 / vp^2, analysis/meteorNTF.m:347 (vp = 3e8 of the
+    analysis constants)."""
+    f = np.asarray(p.fntf, dtype=np.float64)
+    return 4 * math.pi * p.platesize ** 4 * f ** 2 / 3e8 ** 2
+
+
+def pec_sphere_case(N=128, radius=2.0, steps=2500):
+    """The reference's sphere calibration run (doplate = 2: a sigma = 1e7
+    conductor, source/meteor-2.1.cpp:200-206; compared with
+    analysis/sphereRCSvsFreq.m by analysis/meteorNTF.m:350-352 and
+    analysis/spherescattering.m) in reference-format inputs: radius 2 m at
+    dx = 0.1 m (20 cells), a Gaussian-modulated pulse centred at 30 MHz with a
+    10 MHz bandwidth, DFT at 20, 25, 30 and 35 MHz (ka from 0.84 to 1.47)."""
+    f0, dx = 30e6, 0.1
+    dt = rd.stable_dt(dx)
+    p = rd.RunParams(Nx=N, Ny=N, Nz=N, tsteps=steps, dt=dt, f0=f0,
+                     fsig=1 / (2 * math.pi * 10e6 * dt), gridfactor=(rd.C0 / f0) / dx, numfiles=1,
+                     savefields=0, fntf=[20e6, 25e6, 30e6, 35e6], doplate=2, platesize=radius,
+                     metsize=(1e200, 1e200), doB0=0, probex=[], probey=[], probez=[])
+    return p, np.zeros((N, N)), np.zeros((N, N)), (0.0, 0.0, 0.0)
+

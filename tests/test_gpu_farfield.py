@@ -52,10 +52,15 @@ def test_far_field_fp64_matches_oracle(built, name):
     ph = np.concatenate([[math.pi], rng.uniform(-math.pi, math.pi, 40)])
     got = sim.far_field(th, ph)
     want = NO.bistatic(_ntf_dict(sim, p), p.Nx, p.Ny, p.Nz, p.dx, th, ph)
+    # relative L2 over every direction and frequency (the FP64 tolerance on
+    # fields and RCS), and element-wise
+    assert H.rel_l2(got[..., 0], want["sig"]) < 1e-12
+    assert H.rel_l2(got[..., 1], want["sig_a"]) < 1e-12
     np.testing.assert_allclose(got[..., 0], want["sig"], rtol=1e-10)
     np.testing.assert_allclose(got[..., 1], want["sig_a"], rtol=1e-10, atol=1e-300)
     if p.Nx == p.Ny == p.Nz:  # the MATLAB itself assumes a cubic grid
         back = NO.meteorntf_backscatter(_ntf_dict(sim, p), p.Nx, p.dx)
+        assert H.rel_l2(got[:, 0, 0], back["sig"]) < 1e-12
         np.testing.assert_allclose(got[:, 0, 0], back["sig"], rtol=1e-10)
     sim.close()
 
