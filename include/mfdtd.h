@@ -264,10 +264,14 @@ int mfdtd_far_field_static(const double *const ntf_dev[24], int32_t Nx, int32_t 
  * simulation was created with opts.profile set: for class `which` (0, 1, ...)
  * its name, mean duration of one launch in ms, and launch count.  A class
  * may time consecutive launches together: the FP32 form's class 0 is the
- * pass with the two CPML band kernels that complete it, named after the pass
- * kernel(s) that ran in that advance: "k_fp32_step_fast" (every tile and plane
- * interior, no record step), "k_fp32_step" (the general pass), or both joined
- * by '+'.  Returns MFDTD_EINVAL when `which` is past the last class. */
+ * pass with the work that completes it, named after the kernels that ran in
+ * that advance: "k_fp32_step_wide+k_fp32_slab" (non-record steps: the interior
+ * pass with two cells per thread and, on a second stream, the march over the
+ * CPML slabs and domain edges), "k_fp32_step_fast" (non-record steps on grids
+ * too small for the wide pass, followed by the two CPML band kernels),
+ * "k_fp32_step" (record steps: the general pass and the band kernels), joined
+ * by '+' when several ran.  Returns MFDTD_EINVAL when `which` is past the last
+ * class. */
 int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t name_len,
                            double *avg_ms, int64_t *launches);
 

@@ -20,6 +20,10 @@ public:
     // plane interior, no record step) and by the general one (k_fp32_step).
     long long fast_passes() const;
     long long general_passes() const;
+    // Kernel name(s) of a fast pass: "k_fp32_step_wide+k_fp32_slab" (the
+    // interior pass with the slab march) or "k_fp32_step_fast" (followed by
+    // the band kernels).
+    const char *fast_pass_name() const;
     // Current-update kind of this simulation's kernel (0 Young DI, 1 uniform
     // Lee-Kalluri, 2 tabulated Lee-Kalluri); batches group by it.
     int current_update() const;

@@ -78,6 +78,10 @@ struct Tables {
     // auxiliary-line CPML (oblique incidence), A pre-divided by the line cell
     float Bh1[2 * kMaxPml], Ah1[2 * kMaxPml], Be1[2 * kMaxPml], Ae1[2 * kMaxPml];
 };
+// The slab march keeps a copy of the tables in shared memory, after the
+// barriers, poll flags and plasma flags.
+constexpr int SLAB_TB_OFF = NS * STAGE_B + 2 * align128(HN_B) + align128(NS * 8 + 16 + PF_CAP);
+constexpr int SMEM_BS = SLAB_TB_OFF + (int)sizeof(Tables) + 128;
 
 struct Args {
     int Nx, Ny, Nz, Nzp, L, xshift, yshift, zshift;
@@ -348,7 +352,10 @@ struct StageSrc {
 // loads overlap (a psi load placed after another component's psi store cannot
 // be moved above it: the two may alias); the band kernels use it, the pass
 // does not (the registers it holds made the pass spill).
-template <int PAR, bool CLEAN, bool HOIST = false, class Src>
+// LEAN (the CPML slab march): the TF/SF corrections are made after the pass
+// (oblique incidence) and there is no plate or sphere, so that code is not
+// compiled in.
+template <int PAR, bool CLEAN, bool HOIST = false, bool LEAN = false, class Src>
 __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, const Src &src, bool store_psi,
                                        bool want_y, bool want_z, bool tf_in, bool pml) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
@@ -383,7 +390,8 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, const
         const float dEy = src.ek(1) - ey;
         float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
         if (!CLEAN) {
-            if (!a.oblique) {
+            if (LEAN) {
+            } else if (!a.oblique) {
                 if (inbx && inbz) {
                     const float ezi = a.inc[PAR][1][i];
                     if (j == a.by1 - 1) h += a.chy * ezi;
@@ -422,7 +430,8 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, const
         const float dEx = src.ek(0) - ex;
         const float dEz = src.ei(2) - ez;
         float h = a.c1h * o.y - (a.chz * dEx - a.chx * dEz);
-        if (!a.oblique) {
+        if (LEAN) {
+        } else if (!a.oblique) {
             if (inby && inbz) {
                 if (i == a.bx1 - 1) h -= a.chx * a.inc[PAR][1][a.bx1];
                 if (i == a.bx2 - 1) h += a.chx * a.inc[PAR][1][a.bx2 - 1];
@@ -453,7 +462,8 @@ __device__ __forceinline__ HVal h_cell(const Args &a, int i, int j, int k, const
         const float dEy = src.ei(1) - ey;
         const float dEx = src.ej(0) - ex;
         float h = a.c1h * o.z - (a.chx * dEy - a.chy * dEx);
-        if (!a.oblique) {
+        if (LEAN) {
+        } else if (!a.oblique) {
             if (inby && inbz) {
                 if (i == a.bx1 - 1) h += a.chx * a.inc[PAR][0][a.bx1];
                 if (i == a.bx2 - 1) h -= a.chx * a.inc[PAR][0][a.bx2 - 1];
@@ -518,19 +528,19 @@ struct EVal {
 // E half-step of one cell (source/meteor-2.1.cpp:1020-1374 in FP32): the old
 // E (ex, ey, ez), the cell's new H (hv), the neighbours' new H through `hs`,
 // the current (jx, jy, jz).  `pml` as in h_cell.
-template <int PAR, bool CLEAN, bool HOIST = false, class HS>
+template <int PAR, bool CLEAN, bool HOIST = false, bool LEAN = false, class HS>
 __device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float ex, float ey, float ez, const HVal &hv,
                                        const HS &hs, float jx, float jy, float jz, bool tf_in, bool pml) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
     bool sphere = false;
-    if (!CLEAN && a.doplate == 2) {
+    if (!CLEAN && !LEAN && a.doplate == 2) {
         const double x = a.xc[i], y = a.yc[j], z = a.zc[k];
         sphere = sqrt(x * x + y * y + z * z) < a.platesize;
     }
     const float c1 = sphere ? a.c1s : a.c1e0, c2 = sphere ? a.c2s : a.c2e0;
     const float cx = sphere ? a.csx : a.cex, cy = sphere ? a.csy : a.cey,
                 cz = sphere ? a.csz : a.cez;
-    const bool plate_row = !CLEAN && a.doplate == 1 && i == a.ssx;
+    const bool plate_row = !CLEAN && !LEAN && a.doplate == 1 && i == a.ssx;
     const int sxe = pml ? eslab(i, Nx, L, a.xshift) : -1;
     const bool inby = CLEAN ? tf_in : (j >= a.by1 && j < a.by2);
     const bool inbz = CLEAN ? tf_in : (k >= a.bz1 && k < a.bz2);
@@ -557,7 +567,8 @@ __device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float
         const float dHy = hv.y - hs.hk(1);
         float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
         if (!CLEAN) {
-            if (a.oblique) {
+            if (LEAN) {
+            } else if (a.oblique) {
                 if (a.obl_inline && obl_shell(a, i, j, k)) e += obl_corr<PAR, true, 0>(a, i, j, k);
             } else if (i >= a.bx1 && i < a.bx2 - 1) {
                 if (inby) {
@@ -595,7 +606,8 @@ __device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float
         const float dHx = hv.x - hs.hk(0);
         const float dHz = hv.z - hs.hzi();
         float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
-        if (!a.oblique) {
+        if (LEAN) {
+        } else if (!a.oblique) {
             if (inby && inbz) {
                 if (i == a.bx1) e += a.cex * hzinc_new<PAR>(a, a.bx1 - 1);
                 if (i == a.bx2 - 1) e -= a.cex * hzinc_new<PAR>(a, a.bx2 - 1);
@@ -638,7 +650,8 @@ __device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float
         const float dHy = hv.y - hs.hyi();
         const float dHx = hv.x - hs.hj(0);
         float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
-        if (!a.oblique) {
+        if (LEAN) {
+        } else if (!a.oblique) {
             if (inby && inbz) {
                 if (i == a.bx1) e -= a.cex * hyinc_new<PAR>(a, a.bx1 - 1);
                 if (i == a.bx2 - 1) e += a.cex * hyinc_new<PAR>(a, a.bx2 - 1);
@@ -674,6 +687,203 @@ __device__ __forceinline__ EVal e_cell(const Args &a, int i, int j, int k, float
         ez_slice = 0.f;
     }
     return EVal{ex, ey, ez, ez_slice};
+}
+
+// ---- the slab march's CPML cell updates ------------------------------------
+// h_cell / e_cell with the CPML corrections (pml), without the TF/SF, plate,
+// sphere, DFT and slice code (LEAN), in a form for the slab march: what does
+// not change along x is computed once per thread (SlabCell: slab indices,
+// domain-edge flags, 32-bit psi offsets at plane 0), the CPML coefficient
+// tables are read from a shared-memory copy, and the cell's psi values are
+// loaded before its first update.  The expression trees are h_cell's and
+// e_cell's, so the results are the same.
+struct SlabCell {
+    int syh, szh, sye, sze;         // H and E slab indices along y and z (-1: none)
+    bool jn, kn, j1, k1;            // j < Ny-1, k < Nz-1, j >= 1, k >= 1
+    unsigned oyh, oye, ozh, oze;    // y- and z-normal psi offsets at plane 0
+    unsigned ox;                    // x-normal psi offset within a slab plane
+};
+__device__ __forceinline__ SlabCell slab_cell(const Args &a, int j, int k) {
+    SlabCell c;
+    const int L = a.L;
+    c.syh = hslab(j, a.Ny, L, a.yshift);
+    c.szh = hslab(k, a.Nz, L, a.zshift);
+    c.sye = eslab(j, a.Ny, L, a.yshift);
+    c.sze = eslab(k, a.Nz, L, a.zshift);
+    c.jn = j < a.Ny - 1;
+    c.kn = k < a.Nz - 1;
+    c.j1 = j >= 1;
+    c.k1 = k >= 1;
+    c.oyh = (unsigned)max(c.syh, 0) * a.Nz + k;
+    c.oye = (unsigned)max(c.sye, 0) * a.Nz + k;
+    c.ozh = (unsigned)j * (2 * L) + max(c.szh, 0);
+    c.oze = (unsigned)j * (2 * L) + max(c.sze, 0);
+    c.ox = (unsigned)j * a.Nz + k;
+    return c;
+}
+
+template <int PAR, class Src>
+__device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, int sxh, const Src &src,
+                                       const SlabCell &sc, bool store_psi, bool want_y, bool want_z) {
+    HVal o;
+    o.x = src.h(0);
+    o.y = src.h(1);
+    o.z = src.h(2);
+    const float ex = src.e(0), ey = src.e(1), ez = src.e(2);
+    const bool xin = i < a.Nx - 1;
+    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const bool ux = sc.jn && sc.kn, uy = want_y && xin && sc.kn, uz = want_z && xin && sc.jn;
+    const unsigned oy = sc.oyh + (unsigned)i * PY, oz = sc.ozh + (unsigned)i * PZ,
+                   ox = (unsigned)max(sxh, 0) * PX + sc.ox;
+    float *const *R = a.Ph[PAR];
+    float *const *W = a.Ph[PAR ^ 1];
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f;
+    if (ux && sc.syh >= 0) p0 = R[0][oy];
+    if (ux && sc.szh >= 0) p1 = R[1][oz];
+    if (uy && sxh >= 0) p2 = R[2][ox];
+    if (uy && sc.szh >= 0) p3 = R[3][oz];
+    if (uz && sxh >= 0) p4 = R[4][ox];
+    if (uz && sc.syh >= 0) p5 = R[5][oy];
+    if (ux) {
+        const float dEz = src.ej(2) - ez;
+        const float dEy = src.ek(1) - ey;
+        float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
+        if (sc.syh >= 0) {
+            const float p = T.Bh[sc.syh] * p0 + T.Ahy[sc.syh] * dEz;
+            if (store_psi) W[0][oy] = p;
+            h -= a.c2h * p;
+            if (a.kappa_on) h -= a.c2h * (T.Khy[sc.syh] * dEz);
+        }
+        if (sc.szh >= 0) {
+            const float p = T.Bh[sc.szh] * p1 + T.Ahz[sc.szh] * dEy;
+            if (store_psi) W[1][oz] = p;
+            h += a.c2h * p;
+            if (a.kappa_on) h += a.c2h * (T.Khz[sc.szh] * dEy);
+        }
+        o.x = h;
+    }
+    if (uy) {
+        const float dEx = src.ek(0) - ex;
+        const float dEz = src.ei(2) - ez;
+        float h = a.c1h * o.y - (a.chz * dEx - a.chx * dEz);
+        if (sxh >= 0) {
+            const float p = T.Bh[sxh] * p2 + T.Ahx[sxh] * dEz;
+            if (store_psi) W[2][ox] = p;
+            h += a.c2h * p;
+            if (a.kappa_on) h += a.c2h * (T.Khx[sxh] * dEz);
+        }
+        if (sc.szh >= 0) {
+            const float p = T.Bh[sc.szh] * p3 + T.Ahz[sc.szh] * dEx;
+            if (store_psi) W[3][oz] = p;
+            h -= a.c2h * p;
+            if (a.kappa_on) h -= a.c2h * (T.Khz[sc.szh] * dEx);
+        }
+        o.y = h;
+    }
+    if (uz) {
+        const float dEy = src.ei(1) - ey;
+        const float dEx = src.ej(0) - ex;
+        float h = a.c1h * o.z - (a.chx * dEy - a.chy * dEx);
+        if (sxh >= 0) {
+            const float p = T.Bh[sxh] * p4 + T.Ahx[sxh] * dEy;
+            if (store_psi) W[4][ox] = p;
+            h -= a.c2h * p;
+            if (a.kappa_on) h -= a.c2h * (T.Khx[sxh] * dEy);
+        }
+        if (sc.syh >= 0) {
+            const float p = T.Bh[sc.syh] * p5 + T.Ahy[sc.syh] * dEx;
+            if (store_psi) W[5][oy] = p;
+            h += a.c2h * p;
+            if (a.kappa_on) h += a.c2h * (T.Khy[sc.syh] * dEx);
+        }
+        o.z = h;
+    }
+    return o;
+}
+
+template <int PAR, class HS>
+__device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, int sxe, float ex, float ey, float ez,
+                                       const HVal &hv, const HS &hs, float jx, float jy, float jz,
+                                       const SlabCell &sc) {
+    const float c1 = a.c1e0, c2 = a.c2e0, cx = a.cex, cy = a.cey, cz = a.cez;
+    const bool iy = i >= 1 && i < a.Nx - 1;
+    const bool ux = i < a.Nx - 1 && sc.j1 && sc.jn && sc.k1 && sc.kn, uy = iy && sc.k1, uz = iy && sc.j1;
+    const bool xp = sxe >= 0 && sc.jn && sc.kn;
+    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const unsigned oy = sc.oye + (unsigned)i * PY, oz = sc.oze + (unsigned)i * PZ,
+                   ox = (unsigned)max(sxe, 0) * PX + sc.ox;
+    float *const *Pe = a.Pe;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f;
+    if (ux && sc.sye >= 0) p0 = Pe[0][oy];
+    if (ux && sc.sze >= 0) p1 = Pe[1][oz];
+    if (uy && xp) p2 = Pe[2][ox];
+    if (uy && sc.sze >= 0 && sc.jn) p3 = Pe[3][oz];
+    if (uz && xp) p4 = Pe[4][ox];
+    if (uz && sc.sye >= 0 && sc.kn) p5 = Pe[5][oy];
+    if (ux) {
+        const float dHz = hv.z - hs.hj(2);
+        const float dHy = hv.y - hs.hk(1);
+        float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
+        if (sc.sye >= 0) {
+            const float p = T.Be[sc.sye] * p0 + T.Aey[sc.sye] * dHz;
+            Pe[0][oy] = p;
+            e += a.c2e0 * p;
+            if (a.kappa_on) e += a.c2e0 * (T.Key[sc.sye] * dHz);
+        }
+        if (sc.sze >= 0) {
+            const float p = T.Be[sc.sze] * p1 + T.Aez[sc.sze] * dHy;
+            Pe[1][oz] = p;
+            e -= a.c2e0 * p;
+            if (a.kappa_on) e -= a.c2e0 * (T.Kez[sc.sze] * dHy);
+        }
+        ex = e;
+    }
+    if (uy) {
+        const float dHx = hv.x - hs.hk(0);
+        const float dHz = hv.z - hs.hzi();
+        float e = c1 * ey + (cz * dHx - cx * dHz) - c2 * jy;
+        if (sxe >= 0) {
+            float p = 0.f;
+            if (sc.jn && sc.kn) {
+                p = T.Be[sxe] * p2 + T.Aex[sxe] * dHz;
+                Pe[2][ox] = p;
+            }
+            e -= a.c2e0 * p;
+            if (a.kappa_on) e -= a.c2e0 * (T.Kex[sxe] * dHz);
+        }
+        if (sc.sze >= 0) {
+            float p = 0.f;
+            if (sc.jn) {
+                p = T.Be[sc.sze] * p3 + T.Aez[sc.sze] * dHx;
+                Pe[3][oz] = p;
+            }
+            e += a.c2e0 * p;
+            if (a.kappa_on) e += a.c2e0 * (T.Kez[sc.sze] * dHx);
+        }
+        ey = e;
+    }
+    if (uz) {
+        const float dHy = hv.y - hs.hyi();
+        const float dHx = hv.x - hs.hj(0);
+        float e = c1 * ez + (cx * dHy - cy * dHx) - c2 * jz;
+        if (sxe >= 0) {
+            float p = 0.f;
+            if (sc.jn && sc.kn) {
+                p = T.Be[sxe] * p4 + T.Aex[sxe] * dHy;
+                Pe[4][ox] = p;
+            }
+            e += a.c2e0 * p;
+            if (a.kappa_on) e += a.c2e0 * (T.Kex[sxe] * dHy);
+        }
+        if (sc.sye >= 0 && sc.kn) {
+            const float p = T.Be[sc.sye] * p5 + T.Aey[sc.sye] * dHx;
+            Pe[5][oy] = p;
+            e -= a.c2e0 * p;
+            if (a.kappa_on) e -= a.c2e0 * (T.Key[sc.sye] * dHx);
+        }
+        ez = e;
+    }
+    return EVal{ex, ey, ez, ez};
 }
 
 // The whole 1-D incident line for this step, written to set PAR^1 (one CTA).
@@ -799,6 +1009,7 @@ struct MarchCtx {
     bool role_ok, in_grid, valid;
     int issued;
     int tile_id;
+    const Tables *tbs;  // MARCH_SLAB: the CPML tables, copied to shared memory
 };
 
 // Shared-memory layout after the stages and new-H planes: NS stage barriers,
@@ -859,14 +1070,23 @@ __device__ __forceinline__ void j_advance(const Args &a, const float *m, float c
     }
 }
 
+// How a CTA marches its planes (template parameter of march and run_item):
+//   MARCH_GENERAL: per tile and plane, the fast path where it applies, else
+//     the general path (CPML, domain edges, TF/SF, DFT, slices as Args says);
+//   MARCH_FAST: a clean tile whose every plane is an interior one (oblique
+//     TF/SF corrections after the pass, no record step, the CPML slabs and
+//     domain edges left to other work): the warm-up plane also takes the fast
+//     path (its H only), and the general path is not compiled in;
+//   MARCH_SLAB: the CPML slabs and domain edges (k_fp32_slab): every cell
+//     takes the CPML path of h_slab / e_slab.
+enum : int { MARCH_GENERAL = 0, MARCH_FAST = 1, MARCH_SLAB = 2 };
+
 // The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
-// or -1.  FASTONLY (a clean tile whose every plane is an interior one, as
-// with the band kernels, oblique TF/SF corrections after the pass and no
-// record step): the warm-up plane also takes the fast path (its H only), and
-// the general path is not compiled in.
-template <int PAR, int JM, bool CLEAN, bool FASTONLY = false>
+// or -1.
+template <int PAR, int JM, bool CLEAN, int MODE = MARCH_GENERAL>
 __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &c, int t, int record,
                                      bool tf_in) {
+    constexpr bool FASTONLY = MODE == MARCH_FAST, SLAB = MODE == MARCH_SLAB;
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
     const size_t plane = (size_t)Ny * a.Nzp;
     const int dj = c.dj, dk = c.dk, j = c.j, k = c.k, warp = c.warp;
@@ -933,6 +1153,8 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     };
 
     float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
+    SlabCell sc{};
+    if constexpr (SLAB) sc = slab_cell(a, j, k);
     // The stage slot of plane q and the cell offset advance with q (no
     // modulo or 64-bit multiply per plane).
     int slot = 0;
@@ -961,7 +1183,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         const bool x_tfsf = (!a.oblique || a.obl_inline) && tf_in &&
                             (i == a.bx1 - 1 || i == a.bx1 || i == a.bx2 - 1);
         const bool x_ntf = a.ntf_inline && (i == a.ntfb || i == Nx - a.ntfb);
-        const bool fast = FASTONLY || (CLEAN && real && i >= xlo && i <= xhi && !x_ntf &&
+        const bool fast = FASTONLY || (!SLAB && CLEAN && real && i >= xlo && i <= xhi && !x_ntf &&
                                         !(record && i == a.ssx) && !x_tfsf);
         if (fast) {
             // With the band kernels a clean tile may reach past the grid
@@ -1040,7 +1262,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             jx = a.J[0][cg];
             jy = a.J[1][cg];
             jz = a.J[2][cg];
-            const bool jdom = (CLEAN && !a.band)
+            const bool jdom = (CLEAN && !a.band && !SLAB)
                                   ? (i >= 1 && i < Nx - 1)
                                   : (i >= 1 && i < Nx - 1 && j >= 1 && j < Ny - 1 && k >= 1 && k < Nz - 1);
             if (t > 0 && jdom) {
@@ -1078,9 +1300,15 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
         // ---- H of this plane: tile (all comps), halo row (Hx, Hz), halo column (Hx, Hy)
         HVal hv = {0.f, 0.f, 0.f};
-        if (in_grid)
-            hv = h_cell<PAR, CLEAN>(a, i, j, k, StageSrc{s, s1, dj, dk}, tile && real, warp != TJ,
-                                    warp != TJ + 1, tf_in, a.dopml && !a.band);
+        if constexpr (SLAB) {
+            if (in_grid)
+                hv = h_slab<PAR>(a, *c.tbs, i, hslab(i, Nx, L, a.xshift), StageSrc{s, s1, dj, dk}, sc, tile && real,
+                                 warp != TJ, warp != TJ + 1);
+        } else {
+            if (in_grid)
+                hv = h_cell<PAR, CLEAN>(a, i, j, k, StageSrc{s, s1, dj, dk}, tile && real, warp != TJ,
+                                        warp != TJ + 1, tf_in, a.dopml && !a.band);
+        }
         if (c.role_ok) {
             HN(0, dj, dk) = hv.x;
             if (warp != TJ) HN(1, dj, dk) = hv.y;
@@ -1096,9 +1324,14 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         // ---- E of this plane (tile), source/meteor-2.1.cpp:1020-1374
         if (valid && real) {
             const float ex_old = s.e[0][EIDX(dj, dk)];
-            const EVal ev = e_cell<PAR, CLEAN>(a, i, j, k, ex_old, s.e[1][EIDX(dj, dk)], s.e[2][EIDX(dj, dk)], hv,
-                                               StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, tf_in,
-                                               a.dopml && !a.band);
+            EVal ev;
+            if constexpr (SLAB)
+                ev = e_slab<PAR>(a, *c.tbs, i, eslab(i, Nx, L, a.xshift), ex_old, s.e[1][EIDX(dj, dk)],
+                                 s.e[2][EIDX(dj, dk)], hv, StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, sc);
+            else
+                ev = e_cell<PAR, CLEAN>(a, i, j, k, ex_old, s.e[1][EIDX(dj, dk)], s.e[2][EIDX(dj, dk)], hv,
+                                        StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, tf_in,
+                                        a.dopml && !a.band);
             const float ex = ev.x, ey = ev.y, ez = ev.z, ez_slice = ev.z_slice;
             a.E[PAR ^ 1][0][cg] = ex;
             a.E[PAR ^ 1][1][cg] = ey;
@@ -1114,7 +1347,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             const bool fr = i == nb, bk = i == Nx - nb;
             const bool tp = !CLEAN && j == Ny - nb, bt = !CLEAN && j == nb;
             const bool lf = !CLEAN && k == nb, rt = !CLEAN && k == Nz - nb;
-            if (a.ntf_inline && (fr || bk || tp || bt || lf || rt)) {
+            if (!SLAB && a.ntf_inline && (fr || bk || tp || bt || lf || rt)) {
                 const size_t n2 = 2 * (size_t)nf;
                 if (fr || bk) {
                     const size_t base = ((size_t)j * Nz + k) * n2;
@@ -1139,7 +1372,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             }
 
             // ---- slices on record steps
-            if (record) {
+            if (!SLAB && record) {
                 const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
                 if (!CLEAN && k == a.ssz) {
                     a.slE[oz + (size_t)i * Ny + j] = ey;
@@ -1176,15 +1409,36 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     return -1;
 }
 
+// Probes of the previous step from the read set (source/meteor-2.1.cpp:1443-1455),
+// by lanes 8.. of warp 9 of the item that advances the incident line.
+template <int PAR>
+__device__ __forceinline__ void record_probes(const Args &a, int t) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp != 9 || lane < 8 || lane - 8 >= a.nprobes) return;
+    const int pidx = lane - 8;
+    const int ix = a.probe_ijk[3 * pidx], iy = a.probe_ijk[3 * pidx + 1], iz = a.probe_ijk[3 * pidx + 2];
+    const size_t sI = (size_t)a.Ny * a.Nzp, sJ = a.Nzp;
+    const size_t cc = ix * sI + iy * sJ + iz;
+    const float *E0 = a.E[PAR][0], *E1 = a.E[PAR][1], *E2 = a.E[PAR][2];
+    const float *H0 = a.H[PAR][0], *H1 = a.H[PAR][1], *H2 = a.H[PAR][2];
+    const size_t o = (size_t)(t - 1) * a.nprobes + pidx, T = (size_t)a.tsteps * a.nprobes;
+    a.probe[o] = 0.5 * ((double)E0[cc] + E0[cc - sI]);
+    a.probe[T + o] = 0.5 * ((double)E1[cc] + E1[cc - sJ]);
+    a.probe[2 * T + o] = 0.5 * ((double)E2[cc] + E2[cc - 1]);
+    a.probe[3 * T + o] = 0.25 * ((double)H0[cc] + H0[cc - sJ] + H0[cc - 1] + H0[cc - sJ - 1]);
+    a.probe[4 * T + o] = 0.25 * ((double)H1[cc] + H1[cc - sI] + H1[cc - 1] + H1[cc - sI - 1]);
+    a.probe[5 * T + o] = 0.25 * ((double)H2[cc] + H2[cc - sJ] + H2[cc - sI] + H2[cc - sI - sJ]);
+}
+
 // ---------------------------------------------------------------------------
-// One work item: tile `tile_id` of simulation `a` over x-chunk `chunk` (planes
-// chunk*a.chunk .. +a.chunk).  The item with `first` set also advances the
-// incident line and records the probes of the previous step.  `inited` says
-// whether the CTA's stage mbarriers hold an earlier item's objects (they are
-// invalidated and re-initialised).  Returns false when a bounded wait ran out
-// (the simulation's error flag is then set).
-template <int PAR, int JM, bool FASTONLY = false>
-__device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int tile_id, int chunk,
+// One work item: tile `tile_id` of simulation `a` over the planes
+// [i_begin, i_end).  The item with `first` set also advances the incident line
+// and records the probes of the previous step.  `inited` says whether the
+// CTA's stage mbarriers hold an earlier item's objects (they are invalidated
+// and re-initialised).  Returns false when a bounded wait ran out (the
+// simulation's error flag is then set).
+template <int PAR, int JM, int MODE = MARCH_GENERAL>
+__device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int tile_id, int i_begin, int i_end,
                                          bool first, int t, int record, unsigned char *smem_raw,
                                          bool inited) {
     MarchCtx c;
@@ -1200,31 +1454,15 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     c.tile_id = tile_id;
     c.k0 = (tile_id % a.ntk) * TK;
     c.j0 = (tile_id / a.ntk) * TJ;
-    c.i_begin = a.xbeg + chunk * a.chunk;
-    c.i_end = min(a.xend, c.i_begin + a.chunk);
-    if (c.i_begin >= a.xend) return true;
+    c.i_begin = i_begin;
+    c.i_end = i_end;
+    if (c.i_begin >= c.i_end) return true;
     c.p0 = max(c.i_begin - 1, 0);
     c.q_last = min(c.i_end, Nx - 1);  // last plane loaded
-    const size_t plane = (size_t)Ny * a.Nzp;
 
     if (first) line_update<PAR>(a, t);
 
-    // Probes of the previous step from the read set (source/meteor-2.1.cpp:1443-1455).
-    if (first && t > 0 && c.warp == 9 && c.lane >= 8 && c.lane - 8 < a.nprobes) {
-        const int pidx = c.lane - 8;
-        const int ix = a.probe_ijk[3 * pidx], iy = a.probe_ijk[3 * pidx + 1], iz = a.probe_ijk[3 * pidx + 2];
-        const size_t sI = plane, sJ = a.Nzp;
-        const size_t cc = ix * sI + iy * sJ + iz;
-        const float *E0 = a.E[PAR][0], *E1 = a.E[PAR][1], *E2 = a.E[PAR][2];
-        const float *H0 = a.H[PAR][0], *H1 = a.H[PAR][1], *H2 = a.H[PAR][2];
-        const size_t o = (size_t)(t - 1) * a.nprobes + pidx, T = (size_t)a.tsteps * a.nprobes;
-        a.probe[o] = 0.5 * ((double)E0[cc] + E0[cc - sI]);
-        a.probe[T + o] = 0.5 * ((double)E1[cc] + E1[cc - sJ]);
-        a.probe[2 * T + o] = 0.5 * ((double)E2[cc] + E2[cc - 1]);
-        a.probe[3 * T + o] = 0.25 * ((double)H0[cc] + H0[cc - sJ] + H0[cc - 1] + H0[cc - sJ - 1]);
-        a.probe[4 * T + o] = 0.25 * ((double)H1[cc] + H1[cc - sI] + H1[cc - 1] + H1[cc - sI - 1]);
-        a.probe[5 * T + o] = 0.25 * ((double)H2[cc] + H2[cc - sJ] + H2[cc - sI] + H2[cc - sI - sJ]);
-    }
+    if (first && t > 0) record_probes<PAR>(a, t);
 
     if (c.tid == PROD) {
         // An earlier item's barriers have no pending operation (every stage it
@@ -1238,6 +1476,12 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     // Plasma flags of the item's planes, read through plasma_at after the barrier.
     if (a.plasma && c.tid < PF_CAP && c.tid < c.i_end - c.p0)
         pflags(c)[c.tid] = a.plasma[(size_t)(c.p0 + c.tid) * a.ntiles + tile_id];
+    if constexpr (MODE == MARCH_SLAB) {  // the CPML tables, read per cell by the slab march
+        float *dst = (float *)(c.smem + SLAB_TB_OFF);
+        const float *src = (const float *)a.tb;
+        for (int q = c.tid; q < (int)(sizeof(Tables) / 4); q += NTHREADS) dst[q] = src[q];
+        c.tbs = (const Tables *)dst;
+    }
     __syncthreads();
     c.issued = c.p0 - 1;
     if (c.tid == PROD) {
@@ -1258,13 +1502,17 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
     c.in_grid = c.role_ok && c.j >= 0 && c.j < Ny && c.k >= 0 && c.k < Nz;
     c.valid = tile && c.in_grid;
 
-    const TileInfo ti = classify(a, c.j0, c.k0, record);
     int fail_q;
-    if constexpr (FASTONLY)
-        fail_q = march<PAR, JM, true, true>(maps, a, c, t, 0, ti.tf_in);
-    else
-        fail_q = ti.clean ? march<PAR, JM, true>(maps, a, c, t, record, ti.tf_in)
-                          : march<PAR, JM, false>(maps, a, c, t, record, false);
+    if constexpr (MODE == MARCH_SLAB) {
+        fail_q = march<PAR, JM, false, MARCH_SLAB>(maps, a, c, t, 0, false);
+    } else {
+        const TileInfo ti = classify(a, c.j0, c.k0, record);
+        if constexpr (MODE == MARCH_FAST)
+            fail_q = march<PAR, JM, true, MARCH_FAST>(maps, a, c, t, 0, ti.tf_in);
+        else
+            fail_q = ti.clean ? march<PAR, JM, true>(maps, a, c, t, record, ti.tf_in)
+                              : march<PAR, JM, false>(maps, a, c, t, record, false);
+    }
     if (fail_q >= 0 && c.tid == PROD) {
         atomicOr(a.err, 1u);
         // Let the copies already issued land (bounded) before the CTA exits.
@@ -1290,7 +1538,9 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
     k_fp32_step(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t, int record) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const bool first = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
-    run_item<PAR, JM>(maps, a, a.tile_order[blockIdx.x], blockIdx.z, first, t, record, smem_raw, false);
+    const int ib = a.xbeg + (int)blockIdx.z * a.chunk;
+    run_item<PAR, JM>(maps, a, a.tile_order[blockIdx.x], ib, min(a.xend, ib + a.chunk), first, t, record, smem_raw,
+                      false);
 }
 
 // The same pass when every tile and plane takes the fast path (Args::band,
@@ -1302,7 +1552,266 @@ __global__ void __launch_bounds__(NTHREADS, 4)
     k_fp32_step_fast(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const bool first = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
-    run_item<PAR, JM, true>(maps, a, a.tile_order[blockIdx.x], blockIdx.z, first, t, 0, smem_raw, false);
+    const int ib = a.xbeg + (int)blockIdx.z * a.chunk;
+    run_item<PAR, JM, MARCH_FAST>(maps, a, a.tile_order[blockIdx.x], ib, min(a.xend, ib + a.chunk), first, t, 0,
+                                  smem_raw, false);
+}
+
+// The CPML slabs and domain edges of a non-record step, as marches of their
+// own (MARCH_SLAB), run on a second stream alongside k_fp32_step_wide, which
+// then marches only the tiles and planes whose every cell is interior.  A work
+// item is (tile, first plane, end plane): every tile over the x-slab planes
+// [0, w) and [Nx - w, Nx), and the tiles that reach into the y or z slabs (or
+// past the grid) over all planes, in x-chunks (w = L + 1 with the CPML, else
+// 1).  The two kernels write disjoint cells of the new state and read the old
+// one, so they need no ordering; each CTA recomputes the halo H its E update
+// needs, as in the pass.  The CPML corrections are those of the general path
+// (h_cell, e_cell), so the results are the pass-plus-band-kernels ones.
+template <int PAR, int JM>
+__global__ void __launch_bounds__(NTHREADS, 3)
+    k_fp32_slab(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t,
+                const int4 *__restrict__ items) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int4 w = items[blockIdx.x];
+    run_item<PAR, JM, MARCH_SLAB>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
+}
+
+// ---------------------------------------------------------------------------
+// The interior pass with two cells per thread (k_fp32_step_wide), run with the
+// slab march: tiles of TJ x TKW = 8 x 64 (j, k) columns -- two neighbouring
+// 8 x 32 tiles -- whose every cell is interior in j and k, over the interior
+// planes [w, Nx - w).  Each tile thread owns the cells k0 + 2 lane and
+// k0 + 2 lane + 1 of its row: stage reads, new-H plane writes and global
+// stores move both cells as one 8-byte access (ld.shared.v2, st.shared.v2,
+// st.global.v2: a warp stores 256 contiguous bytes per instruction), and the
+// per-plane work that does not depend on the cell (loop, plasma flag, stage
+// addresses, the barrier) is shared by the two.  The -k neighbour of the
+// second cell is the first cell, in registers.  Warp 8 recomputes H on the
+// halo row j0 - 1 (two cells per lane), warp 9 on the halo column k0 - 1
+// (lanes 0-7).  The arithmetic is the fast path's, cell by cell.
+constexpr int TKW = 2 * TK;                   // tile columns
+constexpr int EKW = TKW + 8;                  // box columns k0-4 .. k0+TKW+3
+constexpr int C_BW = EJ * EKW * 4;            // one component's box
+constexpr int STAGE_BW = align128(6 * C_BW);
+constexpr int STAGE_TXW = 6 * C_BW;
+constexpr int HNW_COLS = TKW + 2;             // new-H plane columns k0-2 .. k0+TKW-1
+constexpr int HNW_B = 3 * HJ * HNW_COLS * 4;
+constexpr int SMEM_BW = NS * STAGE_BW + 2 * align128(HNW_B) + NS * 8 + 16 + PF_CAP + 128;
+#define EW(dj, dk) (((dj) + 1) * EKW + (dk) + 4)
+#define HNW(c, dj, dk) (((c) * HJ + (dj) + 1) * HNW_COLS + (dk) + 2)
+
+__device__ __forceinline__ float2 lds2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ void sts2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+__device__ __forceinline__ float2 ldg2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
+__device__ __forceinline__ void stg2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
+
+template <int PAR, int JM>
+__device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int tile_id, int i_begin, int i_end,
+                                          bool first, int t, unsigned char *smem_raw) {
+    unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+    float *hnb = (float *)(smem + NS * STAGE_BW);
+    uint64_t *bar = (uint64_t *)(smem + NS * STAGE_BW + 2 * align128(HNW_B));
+    volatile int *okflag = (volatile int *)(bar + NS);
+    unsigned char *pf = (unsigned char *)(bar + NS) + 16;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int Nx = a.Nx, Ny = a.Ny;
+    const int k0 = (tile_id % a.ntk) * TK, j0 = (tile_id / a.ntk) * TJ;
+    if (i_begin >= i_end) return;
+    const int p0 = max(i_begin - 1, 0), q_last = min(i_end, Nx - 1);
+    const size_t plane = (size_t)Ny * a.Nzp;
+
+    if (first) line_update<PAR>(a, t);
+    if (first && t > 0) record_probes<PAR>(a, t);
+    if (tid == PROD) {
+        for (int q = 0; q < NS; q++) mbar_init(&bar[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // plasma flags of the item's planes: the block of either 8 x 32 half
+    if (a.plasma && tid < PF_CAP && tid < i_end - p0) {
+        const size_t r = (size_t)(p0 + tid) * a.ntiles + tile_id;
+        pf[tid] = a.plasma[r] | a.plasma[r + 1];
+    }
+    __syncthreads();
+    int issued = p0 - 1;
+    auto issue = [&](int q) {
+        const int slot = (q - p0) % NS;
+        mbar_arm(&bar[slot], STAGE_TXW);
+        tma4(smem + slot * STAGE_BW, &maps.F[PAR], k0 - 4, j0 - 1, q, 0, &bar[slot]);
+    };
+    if (tid == PROD) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int q = p0; q <= q_last && q < p0 + NS; q++) {
+            issue(q);
+            issued = q;
+        }
+    }
+    auto plasma_q = [&](int q) {
+        if (!a.plasma) return true;
+        const int r = q - p0;
+        return r < PF_CAP ? pf[r] != 0
+                          : (a.plasma[(size_t)q * a.ntiles + tile_id] | a.plasma[(size_t)q * a.ntiles + tile_id + 1]) != 0;
+    };
+    auto stage_ready = [&](int qq) {
+        return qq > q_last || mbar_wait(&bar[(qq - p0) % NS], ((qq - p0) / NS) & 1);
+    };
+
+    // roles
+    const bool tile = warp < TJ, row_halo = warp == TJ, col_halo = warp == TJ + 1 && lane < TJ;
+    const int dj = tile ? warp : row_halo ? -1 : lane;
+    const int dk = (tile || row_halo) ? 2 * lane : -1;
+    const int j = j0 + dj, k = k0 + dk;
+    const size_t col = tile ? (size_t)j * a.Nzp + k : 0;
+    float2 Gk = make_float2(0.f, 0.f), G2k = Gk;
+    if (tile) {
+        Gk = make_float2(a.G[k], a.G[k + 1]);
+        G2k = make_float2(a.G2[k], a.G2[k + 1]);
+    }
+    // plasma weight (and collision frequency) of the thread's cells, one plane ahead
+    auto pf_load = [&](int qq, float2 &wq, float2 &nu) {
+        if (!tile || qq >= Nx) return;
+        const size_t ij = (size_t)qq * Ny + j;
+        if (a.wq3) wq = ldg2(a.wq3 + (size_t)qq * plane + col);
+        else wq.x = wq.y = a.wq2[ij];
+        if (JM == 0) {
+            if (a.nu3) nu = ldg2(a.nu3 + (size_t)qq * plane + col);
+            else nu.x = nu.y = a.nu2[ij];
+        }
+    };
+    float2 nwq = make_float2(0.f, 0.f), nnu = nwq;
+    bool npl = plasma_q(p0);
+    if (npl) pf_load(p0, nwq, nnu);
+
+    if (tid == PROD) okflag[2] = (stage_ready(p0) && stage_ready(p0 + 1)) ? 1 : 0;
+    __syncthreads();
+    int fail_q = -1;
+    if (!okflag[2]) fail_q = p0;
+
+    float2 hyp = make_float2(0.f, 0.f), hzp = hyp, exp2v = hyp;  // previous plane's Hy, Hz, old Ex
+    int slot = 0;
+    size_t cg = (size_t)p0 * plane + col;
+    const float c1h = a.c1h, chx = a.chx, chy = a.chy, chz = a.chz;
+    for (int q = p0; fail_q < 0 && q < i_end; q++, cg += plane) {
+        const float2 cwq = nwq, cnu = nnu;
+        const bool pl = npl;
+        npl = q + 1 < i_end && plasma_q(q + 1);
+        if (npl) pf_load(q + 1, nwq, nnu);
+        const int slot1 = slot == NS - 1 ? 0 : slot + 1;
+        float *hn = hnb + (q & 1) * (align128(HNW_B) / 4);
+        const float *sb = (const float *)(smem + slot * STAGE_BW);
+        const float *sb1 = (const float *)(smem + slot1 * STAGE_BW);
+        slot = slot1;
+        const bool real = q >= i_begin;
+        // component c of the stage: sb + c * (C_BW / 4)
+        constexpr int CB = C_BW / 4;
+        float2 e0 = make_float2(0.f, 0.f), e1 = e0, e2 = e0, hx = e0, hy = e0, hz = e0;
+        float2 jx = e0, jy = e0, jz = e0;
+        if (tile || row_halo) {
+            e0 = lds2(sb + 0 * CB + EW(dj, dk));
+            e1 = lds2(sb + 1 * CB + EW(dj, dk));
+            e2 = lds2(sb + 2 * CB + EW(dj, dk));
+            const float2 h0 = lds2(sb + 3 * CB + EW(dj, dk)), h2 = lds2(sb + 5 * CB + EW(dj, dk));
+            const float2 e2j = lds2(sb + 2 * CB + EW(dj + 1, dk)), e0j = lds2(sb + 0 * CB + EW(dj + 1, dk));
+            const float e1k = sb[1 * CB + EW(dj, dk + 2)];
+            const float2 e1i = lds2(sb1 + 1 * CB + EW(dj, dk));
+            hx.x = c1h * h0.x - (chy * (e2j.x - e2.x) - chz * (e1.y - e1.x));
+            hx.y = c1h * h0.y - (chy * (e2j.y - e2.y) - chz * (e1k - e1.y));
+            hz.x = c1h * h2.x - (chx * (e1i.x - e1.x) - chy * (e0j.x - e0.x));
+            hz.y = c1h * h2.y - (chx * (e1i.y - e1.y) - chy * (e0j.y - e0.y));
+            sts2(hn + HNW(0, dj, dk), hx);
+            sts2(hn + HNW(2, dj, dk), hz);
+            if (tile) {
+                const float2 h1 = lds2(sb + 4 * CB + EW(dj, dk));
+                const float e0k = sb[0 * CB + EW(dj, dk + 2)];
+                const float2 e2i = lds2(sb1 + 2 * CB + EW(dj, dk));
+                hy.x = c1h * h1.x - (chz * (e0.y - e0.x) - chx * (e2i.x - e2.x));
+                hy.y = c1h * h1.y - (chz * (e0k - e0.y) - chx * (e2i.y - e2.y));
+                sts2(hn + HNW(1, dj, dk), hy);
+                if (real) {
+                    stg2(a.H[PAR ^ 1][0] + cg, hx);
+                    stg2(a.H[PAR ^ 1][1] + cg, hy);
+                    stg2(a.H[PAR ^ 1][2] + cg, hz);
+                    if (pl) {  // J of the previous step, lagged (source/meteor-fork.cpp:1539-1595)
+                        jx = ldg2(a.J[0] + cg);
+                        jy = ldg2(a.J[1] + cg);
+                        jz = ldg2(a.J[2] + cg);
+                        if (t > 0) {
+                            const float2 eyjm = lds2(sb + 1 * CB + EW(dj - 1, dk));
+                            const float ezkm = sb[2 * CB + EW(dj, dk - 1)];
+                            j_advance<JM>(a, a.lku, cwq.x, cnu.x, Gk.x, G2k.x, e0.x, e1.x, e2.x, exp2v.x, eyjm.x,
+                                          ezkm, jx.x, jy.x, jz.x);
+                            j_advance<JM>(a, a.lku, cwq.y, cnu.y, Gk.y, G2k.y, e0.y, e1.y, e2.y, exp2v.y, eyjm.y,
+                                          e2.x, jx.y, jy.y, jz.y);
+                        }
+                    }
+                }
+            }
+        } else if (col_halo) {  // H on the halo column k0 - 1: Hx and Hy
+            const float ex = sb[0 * CB + EW(dj, -1)], ey = sb[1 * CB + EW(dj, -1)], ez = sb[2 * CB + EW(dj, -1)];
+            const float h0 = sb[3 * CB + EW(dj, -1)], h1 = sb[4 * CB + EW(dj, -1)];
+            hx.x = c1h * h0 - (chy * (sb[2 * CB + EW(dj + 1, -1)] - ez) - chz * (sb[1 * CB + EW(dj, 0)] - ey));
+            hy.x = c1h * h1 - (chz * (sb[0 * CB + EW(dj, 0)] - ex) - chx * (sb1[2 * CB + EW(dj, -1)] - ez));
+            hn[HNW(0, dj, -1)] = hx.x;
+            hn[HNW(1, dj, -1)] = hy.x;
+        }
+        // one CTA barrier per plane: the new-H plane is complete; the stage of
+        // plane q+2 has landed; the producer refills plane q-1's slot
+        if (tid == PROD) okflag[q & 1] = stage_ready(q + 2) ? 1 : 0;
+        __syncthreads();
+        if (!okflag[q & 1]) {
+            fail_q = q + 2;
+            break;
+        }
+        if (tid == PROD && q > p0 && q - 1 + NS <= q_last) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(q - 1 + NS);
+            issued = q - 1 + NS;
+        }
+        if (tile) {
+            if (real) {
+                const float c1 = a.c1e0, c2 = a.c2e0, cex = a.cex, cey = a.cey, cez = a.cez;
+                const float2 hzj = lds2(hn + HNW(2, dj - 1, dk)), hxj = lds2(hn + HNW(0, dj - 1, dk));
+                const float hykm = hn[HNW(1, dj, dk - 1)], hxkm = hn[HNW(0, dj, dk - 1)];
+                float2 ex, ey, ez;
+                ex.x = c1 * e0.x + (cey * (hz.x - hzj.x) - cez * (hy.x - hykm)) - c2 * jx.x;
+                ex.y = c1 * e0.y + (cey * (hz.y - hzj.y) - cez * (hy.y - hy.x)) - c2 * jx.y;
+                ey.x = c1 * e1.x + (cez * (hx.x - hxkm) - cex * (hz.x - hzp.x)) - c2 * jy.x;
+                ey.y = c1 * e1.y + (cez * (hx.y - hx.x) - cex * (hz.y - hzp.y)) - c2 * jy.y;
+                ez.x = c1 * e2.x + (cex * (hy.x - hyp.x) - cey * (hx.x - hxj.x)) - c2 * jz.x;
+                ez.y = c1 * e2.y + (cex * (hy.y - hyp.y) - cey * (hx.y - hxj.y)) - c2 * jz.y;
+                stg2(a.E[PAR ^ 1][0] + cg, ex);
+                stg2(a.E[PAR ^ 1][1] + cg, ey);
+                stg2(a.E[PAR ^ 1][2] + cg, ez);
+                if (pl) {
+                    stg2(a.J[0] + cg, jx);
+                    stg2(a.J[1] + cg, jy);
+                    stg2(a.J[2] + cg, jz);
+                }
+            }
+            exp2v = e0;
+            hyp = hy;
+            hzp = hz;
+        }
+    }
+    if (fail_q >= 0 && tid == PROD) {
+        atomicOr(a.err, 1u);
+        // Let the copies already issued land (bounded) before the CTA exits.
+        for (int qq = fail_q; qq <= issued; qq++) {
+            const int sl = (qq - p0) % NS;
+            const unsigned pp = ((qq - p0) / NS) & 1;
+            const uint64_t t0 = globaltimer();
+            while (!mbar_test(&bar[sl], pp) && globaltimer() - t0 < 200000000ull) {
+            }
+        }
+    }
+}
+
+template <int PAR, int JM>
+__global__ void __launch_bounds__(NTHREADS, 2)
+    k_fp32_step_wide(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const bool first = blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0;
+    const int ib = a.xbeg + (int)blockIdx.z * a.chunk;
+    wide_item<PAR, JM>(maps, a, a.tile_order[blockIdx.x], ib, min(a.xend, ib + a.chunk), first, t, smem_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -1338,7 +1847,9 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
         const BatchItem w = items[it];
         const int t = job_t[w.job];
         if (t >= job_end[w.job]) continue;
-        if (!run_item<PAR, JM>(maps[w.job], c_jobs[w.job], w.tile, w.chunk, w.first != 0, t, 0, smem_raw,
+        const Args &a = c_jobs[w.job];
+        const int ib = a.xbeg + w.chunk * a.chunk;
+        if (!run_item<PAR, JM>(maps[w.job], a, w.tile, ib, min(a.xend, ib + a.chunk), w.first != 0, t, 0, smem_raw,
                                inited))
             break;
         inited = true;
@@ -1849,6 +2360,7 @@ struct Fp32Sim::Impl {
     Args af;        // the fast pass's Args: the same, over the planes [L + 1, Nx - L - 1)
     dim3 grid_fast;
     Maps maps;
+    Maps mapsw;     // boxes of the wide interior pass (8 x 64 tiles)
     std::vector<void *> allocs;
     int64_t bytes = 0;
     int Nx = 0, Ny = 0, Nz = 0, Nzp = 0, tsteps = 0, nntf = 0, nprobes = 0;
@@ -1864,6 +2376,14 @@ struct Fp32Sim::Impl {
     int n_boundary = 0;            // how many of them are boundary tiles
     bool fast_ok = false;          // non-record passes may use k_fp32_step_fast
     long long n_fast = 0, n_general = 0;  // passes run by each pass kernel
+    // Non-record passes as k_fp32_step_wide over the interior tiles and planes
+    // plus k_fp32_slab over the rest, on a second stream (see k_fp32_slab);
+    // else k_fp32_step_fast followed by the band kernels.
+    bool slab_ok = false;
+    const int4 *slab_items = nullptr;
+    int n_slab_items = 0;
+    cudaStream_t aux = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
@@ -1881,6 +2401,12 @@ struct Fp32Sim::Impl {
         return d;
     }
     ~Impl() {
+        if (aux) {
+            cudaStreamSynchronize(aux);
+            cudaStreamDestroy(aux);
+        }
+        if (ev_fork) cudaEventDestroy(ev_fork);
+        if (ev_join) cudaEventDestroy(ev_join);
         for (void *p : allocs) cudaFree(p);
     }
 };
@@ -1896,16 +2422,18 @@ int64_t Fp32Sim::footprint(const Problem &P) {
     // band kernels' unit table (an upper bound) and the plasma-block table
     const int64_t w = P.dopml ? P.L + 1 : 1, nseg = (P.Nz + 31) / 32, nsegz = (2 * w + 31) / 32;
     const int64_t band = 8 * (2 * w * P.Ny * nseg + (int64_t)P.Nx * 2 * w * nseg + (int64_t)P.Nx * P.Ny * nsegz);
-    const int64_t ptab = (int64_t)P.Nx * (Nzp / TK) * ((P.Ny + TJ - 1) / TJ);
+    const int64_t ntiles = (Nzp / TK) * ((P.Ny + TJ - 1) / TJ);
+    const int64_t ptab = (int64_t)P.Nx * ntiles;
+    const int64_t slab = 16 * ntiles * ((P.Nx + 95) / 96 + 2);  // slab-march items (an upper bound)
+    // Lee-Kalluri table: a matrix pair per cell (padded layout) when nu varies
+    // along all three axes
+    const int64_t lkt = (P.doB0 && P.lk_mode == LK_PER_CELL) ? cells * 4 * kLkStride : 4 * (int64_t)P.lk.size();
     return cells * 4 * 15 + maps + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2) + band +
-           ptab;
+           ptab + slab + lkt;
 }
 
 void Fp32Sim::init(const Problem &P, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
-    if (P.doB0 && P.lk_mode == LK_PER_CELL)
-        throw Error(MFDTD_EINVAL, "FP32 form: collision frequency varying along all three axes "
-                                  "is not supported (use the FP64 plain form)");
     if (P.L > kMaxPml) throw Error(MFDTD_EINVAL, "CPML too thick");
     impl_ = new Impl();
     Impl &m = *impl_;
@@ -2045,7 +2573,20 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         }
         a.nu3 = n3 ? m.upload(per_cell(P.nu3, false), s) : nullptr;
         a.wq2 = m.upload(wq2, s); a.nu2 = m.upload(nu2, s); a.G = m.upload(G, s); a.G2 = m.upload(G2, s);
-        std::vector<float> lk(P.lk.begin(), P.lk.end());
+        // Lee-Kalluri matrices (18 per entry): per k, per (i,j), or per cell.
+        // A per-cell table is stored in the padded field layout, so the
+        // kernels index it by the cell's offset (source/meteor-fork.cpp:1546-1573
+        // builds one matrix pair per cell when nu varies along all three axes).
+        std::vector<float> lk;
+        if (P.lk_mode == LK_PER_CELL && !P.lk.empty()) {
+            lk.assign((size_t)P.Nx * P.Ny * m.Nzp * kLkStride, 0.f);
+            for (size_t ij = 0; ij < (size_t)P.Nx * P.Ny; ij++)
+                for (int k = 0; k < P.Nz; k++)
+                    for (int u = 0; u < kLkStride; u++)
+                        lk[(ij * m.Nzp + k) * kLkStride + u] = (float)P.lk[(ij * P.Nz + k) * kLkStride + u];
+        } else {
+            lk.assign(P.lk.begin(), P.lk.end());
+        }
         a.lk = m.upload(lk, s);
         std::vector<float> src(P.src.begin(), P.src.end());
         a.src = m.upload(src, s);
@@ -2067,7 +2608,10 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     m.dtmp_len = std::max(m.slice_len, (size_t)1);
     m.dtmp = m.alloc<double>(m.dtmp_len, s);
 
-    for (int b = 0; b < 2; b++) make_map(&m.maps.F[b], a.E[b][0], P.Nx, P.Ny, P.Nz, m.Nzp, EK, EJ);
+    for (int b = 0; b < 2; b++) {
+        make_map(&m.maps.F[b], a.E[b][0], P.Nx, P.Ny, P.Nz, m.Nzp, EK, EJ);
+        make_map(&m.mapsw.F[b], a.E[b][0], P.Nx, P.Ny, P.Nz, m.Nzp, EKW, EJ);
+    }
 
     {
         auto attr = [](const void *f) {
@@ -2084,6 +2628,14 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         };
         attr4((const void *)k_fp32_step_fast<0, 0>); attr4((const void *)k_fp32_step_fast<1, 0>);
         attr4((const void *)k_fp32_step_fast<0, 1>); attr4((const void *)k_fp32_step_fast<1, 1>);
+        auto attrs = [&](const void *f, int bytes) {
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes), "attr");
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100), "attr");
+        };
+        attrs((const void *)k_fp32_slab<0, 0>, SMEM_BS); attrs((const void *)k_fp32_slab<1, 0>, SMEM_BS);
+        attrs((const void *)k_fp32_slab<0, 1>, SMEM_BS); attrs((const void *)k_fp32_slab<1, 1>, SMEM_BS);
+        attrs((const void *)k_fp32_step_wide<0, 0>, SMEM_BW); attrs((const void *)k_fp32_step_wide<1, 0>, SMEM_BW);
+        attrs((const void *)k_fp32_step_wide<0, 1>, SMEM_BW); attrs((const void *)k_fp32_step_wide<1, 1>, SMEM_BW);
     }
     m.jm = 0;
     if (P.doB0) {
@@ -2158,24 +2710,75 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         a.plasma = d;
     }
     if (m.fast_ok) {
-        // The fast pass leaves the band's x planes, and the tile rows lying
-        // wholly in the band's y rows, to the band kernels.
+        // With the slab march: the wide interior pass marches pairs of tiles
+        // whose cells are all interior in j and k, over the planes
+        // [w, Nx - w); k_fp32_slab the rest.  Without it: the fast pass leaves
+        // the band's x planes, and the tile rows lying wholly in the band's y
+        // rows, to the band kernels.
         const int w = P.dopml ? P.L + 1 : 1, len = P.Nx - 2 * w;
+        auto interior = [&](int tl) {
+            const int j0 = (tl / a.ntk) * TJ, k0 = (tl % a.ntk) * TK;
+            return j0 >= w && j0 + TJ <= P.Ny - w && k0 >= w && k0 + TK <= P.Nz - w;
+        };
+        std::vector<int> inner, edge;
+        for (int tl : m.tile_order) (interior(tl) ? inner : edge).push_back(tl);
+        // Pairs of neighbouring interior tiles (8 x 64 columns); a tile left
+        // without a partner joins the slab march.
+        std::vector<int> pairs;
+        {
+            std::vector<char> is_in((size_t)a.ntiles, 0);
+            for (int tl : inner) is_in[tl] = 1;
+            std::vector<int> rest;
+            for (int ty = 0; ty * TJ < P.Ny; ty++)
+                for (int tk = 0; tk < a.ntk; tk++) {
+                    const int tl = ty * a.ntk + tk;
+                    if (!is_in[tl]) continue;
+                    if (tk + 1 < a.ntk && is_in[tl + 1]) {
+                        pairs.push_back(tl);
+                        tk++;
+                    } else {
+                        rest.push_back(tl);
+                    }
+                }
+            for (int tl : rest) edge.push_back(tl);
+            inner.clear();
+            for (int tl : pairs) { inner.push_back(tl); inner.push_back(tl + 1); }
+        }
+        m.slab_ok = !pairs.empty() && len > 0;
+        if (m.slab_ok) {
+            std::vector<int4> items;
+            // Tiles reaching into the y/z slabs: every plane, in x-chunks of
+            // about 96 planes (long marches first).
+            const int ce = std::max(1, (P.Nx + 95) / 96), cl = (P.Nx + ce - 1) / ce;
+            for (int tl : edge)
+                for (int ib = 0; ib < P.Nx; ib += cl) items.push_back(make_int4(tl, ib, std::min(P.Nx, ib + cl), 0));
+            for (int tl : inner) {
+                items.push_back(make_int4(tl, 0, w, 0));
+                items.push_back(make_int4(tl, P.Nx - w, P.Nx, 0));
+            }
+            m.slab_items = m.upload(items, s);
+            m.n_slab_items = (int)items.size();
+            ck(cudaStreamCreateWithFlags(&m.aux, cudaStreamNonBlocking), "cudaStreamCreate");
+            ck(cudaEventCreateWithFlags(&m.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+            ck(cudaEventCreateWithFlags(&m.ev_join, cudaEventDisableTiming), "cudaEventCreate");
+        } else {
+            inner.clear();
+            for (int tl : m.tile_order) {
+                const int j0 = (tl / a.ntk) * TJ;
+                if (!(j0 + TJ <= w || j0 >= P.Ny - w)) inner.push_back(tl);
+            }
+        }
         m.af = a;
         m.af.xbeg = w;
         m.af.xend = P.Nx - w;
-        std::vector<int> inner;
-        for (int tl : m.tile_order) {
-            const int j0 = (tl / a.ntk) * TJ;
-            if (!(j0 + TJ <= w || j0 >= P.Ny - w)) inner.push_back(tl);
-        }
-        m.af.tile_order = m.upload(inner, s);
-        const int tf = std::max(1, (int)inner.size());
+        const std::vector<int> &fast_tiles = m.slab_ok ? pairs : inner;
+        m.af.tile_order = m.upload(fast_tiles, s);
+        const int tf = std::max(1, (int)fast_tiles.size());
         int cf = std::max(1, std::min(len / 16 > 0 ? len / 16 : 1, (want + tf - 1) / tf));
         cf = std::max(cf, (len + 159) / 160);
         m.af.chunk = (len + cf - 1) / cf;
         cf = (len + m.af.chunk - 1) / m.af.chunk;
-        m.grid_fast = dim3((unsigned)inner.size(), 1, cf);
+        m.grid_fast = dim3((unsigned)fast_tiles.size(), 1, cf);
     }
     bytes_ = m.bytes;
 }
@@ -2185,6 +2788,9 @@ double Fp32Sim::plasma_fraction() const { return impl_->plasma_fraction; }
 int Fp32Sim::kernel_classes() { return 3; }
 long long Fp32Sim::fast_passes() const { return impl_->n_fast; }
 long long Fp32Sim::general_passes() const { return impl_->n_general; }
+const char *Fp32Sim::fast_pass_name() const {
+    return impl_->slab_ok ? "k_fp32_step_wide+k_fp32_slab" : "k_fp32_step_fast";
+}
 int Fp32Sim::current_update() const { return impl_->jm; }
 const char *Fp32Sim::kernel_name(int which) {
     return which == 0 ? "k_fp32_step" : which == 1 ? "k_fp32_tfsf" : "k_fp32_ntf";
@@ -2200,7 +2806,31 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     // The pass reads the set holding the current state and writes the other.
     const bool fast = m.fast_ok && !record;
     (fast ? m.n_fast : m.n_general) += 1;
-    if (fast) {
+    int launches = 1;
+    if (fast && m.slab_ok) {
+        // the slab march on the second stream, concurrently with the pass
+        ck(cudaEventRecord(m.ev_fork, s), "cudaEventRecord");
+        ck(cudaStreamWaitEvent(m.aux, m.ev_fork, 0), "cudaStreamWaitEvent");
+        const dim3 g((unsigned)m.n_slab_items);
+        if (m_cur_ == 0) {
+            if (m.jm == 0) k_fp32_slab<0, 0><<<g, NTHREADS, SMEM_BS, m.aux>>>(m.maps, m.a, t, m.slab_items);
+            else k_fp32_slab<0, 1><<<g, NTHREADS, SMEM_BS, m.aux>>>(m.maps, m.a, t, m.slab_items);
+        } else {
+            if (m.jm == 0) k_fp32_slab<1, 0><<<g, NTHREADS, SMEM_BS, m.aux>>>(m.maps, m.a, t, m.slab_items);
+            else k_fp32_slab<1, 1><<<g, NTHREADS, SMEM_BS, m.aux>>>(m.maps, m.a, t, m.slab_items);
+        }
+        launches++;
+    }
+    auto go_wide = [&](auto kern) { kern<<<m.grid_fast, NTHREADS, SMEM_BW, s>>>(m.mapsw, m.af, t); };
+    if (fast && m.slab_ok) {
+        if (m_cur_ == 0) {
+            if (m.jm == 0) go_wide(k_fp32_step_wide<0, 0>);
+            else go_wide(k_fp32_step_wide<0, 1>);
+        } else {
+            if (m.jm == 0) go_wide(k_fp32_step_wide<1, 0>);
+            else go_wide(k_fp32_step_wide<1, 1>);
+        }
+    } else if (fast) {
         if (m_cur_ == 0) {
             if (m.jm == 0) go_fast(k_fp32_step_fast<0, 0>);
             else go_fast(k_fp32_step_fast<0, 1>);
@@ -2217,8 +2847,10 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
         else if (m.jm == 1) go(k_fp32_step<1, 1>);
         else go(k_fp32_step<1, 2>);
     }
-    int launches = 1;
-    if (m.a.band) {
+    if (fast && m.slab_ok) {
+        ck(cudaEventRecord(m.ev_join, m.aux), "cudaEventRecord");
+        ck(cudaStreamWaitEvent(s, m.ev_join, 0), "cudaStreamWaitEvent");
+    } else if (m.a.band) {
         const int g = m.sms * 8, xs = fast ? 1 : 0;
         auto band_e = [&](auto kern) { kern<<<g, 256, 0, s>>>(m.a, rec, t, xs); };
         if (m_cur_ == 0) {

@@ -425,7 +425,8 @@ struct mfdtd_sim {
             // Class 0 of the FP32 form is the pass with its band kernels; name
             // the pass kernel(s) that ran in this advance.
             const bool fast = f32->fast_passes() > fast0, gen = f32->general_passes() > gen0;
-            kname[0] = fast && gen ? "k_fp32_step_fast+k_fp32_step" : fast ? "k_fp32_step_fast" : "k_fp32_step";
+            const std::string fname = f32->fast_pass_name();
+            kname[0] = fast && gen ? fname + "+k_fp32_step" : fast ? fname : std::string("k_fp32_step");
         }
         if (nsteps > 0) {
             wait();

@@ -50,7 +50,7 @@ def _faces(flat, p):
     return flat[4 * p.nntf:]
 
 
-@pytest.mark.parametrize("name", sorted(n for n in EXT if n != "ext_lk_cell"))
+@pytest.mark.parametrize("name", sorted(EXT))
 def test_fp32_ext_close_to_plain(built, tmp_path, name):
     case = EXT[name]
     p = case[0]
@@ -67,14 +67,6 @@ def test_fp32_ext_close_to_plain(built, tmp_path, name):
     mask = r64 > r64.max(axis=1, keepdims=True) * 1e-3
     err = np.abs(10 * np.log10(r32[mask] / r64[mask]))
     assert err.max() < 0.1, err.max()
-
-
-def test_fp32_rejects_lee_kalluri_per_cell(built, tmp_path):
-    d = os.path.join(str(tmp_path), "r")
-    golden_cases.write_ext_case(d, EXT["ext_lk_cell"])
-    with pytest.raises(E.MfdtdError) as ei:
-        E.Simulation(E.Problem.from_rundir(d), form=E.FORM_FP32_FUSED)
-    assert E.STATUS[ei.value.code] == "EINVAL"
 
 
 def mie_sphere_case(N=72, dx=0.15, radius=1.0, n_e=1e13, nu=1e5, steps=2500,

@@ -76,7 +76,7 @@ def compare_fp32(da, db, p):
     np.testing.assert_allclose(la[big], lb[big], rtol=1e-3)
 
 
-FP32_CASES = sorted(n for n in CASES if n != "lk_general")
+FP32_CASES = sorted(CASES)  # lk_general: one Lee-Kalluri matrix pair per cell
 
 
 @pytest.mark.parametrize("name", FP32_CASES)
@@ -100,14 +100,6 @@ def test_fp32_uniform_lee_kalluri(built, tmp_path):
     E.run_rundir(da, form=E.FORM_FP32_FUSED)
     H.run_oracle(db)
     compare_fp32(da, db, p)
-
-
-def test_fp32_rejects_per_cell_collision_tables(built, tmp_path):
-    case = CASES["lk_general"]
-    d = H.fresh_dir(tmp_path, "g", case)
-    with pytest.raises(E.MfdtdError) as ei:
-        E.run_rundir(d, form=E.FORM_FP32_FUSED)
-    assert E.STATUS[ei.value.code] == "EINVAL"
 
 
 def test_fp32_chunked_grid_and_long_run(built, tmp_path):
