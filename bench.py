@@ -15,6 +15,16 @@ than the 129 MB L2, so no flush is needed between steps.
 creation from host arrays, device allocation and upload, K steps, and the
 device-to-host read of the near-to-far-field sums, timed by the host clock.
 
+Beside the headline, the default line carries (one GPU only; ``--no-plain``,
+``--no-sweep`` skip them):
+
+* ``plain_fp64``: the FP64 plain form on the same workload (device time of 3
+  steps after a warm-up step) and the FP32/FP64 speed ratio;
+* ``sweep``: the batched sweep of 128 random trails from one seed (2500 steps
+  each, bistatic RCS on a 5-degree grid) through the serving loop: solves/hour,
+  latency p50/p99, and two sequential baselines of the same jobs, FP64 plain
+  and single-simulation FP32 (``run_population``).
+
 ``--impl reference`` times the reference's CPU implementation of the path on
 this host's cores (the reference binary built from its sources when present,
 else the C restatement of it in oracle/) on a bounded slab of the same
@@ -356,25 +366,29 @@ def load_peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def population_bench(args):
+def run_population(kind: str, n: int = 0):
     """Batched sweep ("sweep": 128 random trails submitted together) or serving
     stream ("serve": Poisson arrivals, 90 % sweep-distribution trails and 10 %
     384 x 384 x 768 trails, offered at about 80 % of the measured capacity):
     every trail runs its full 2500 steps through the native serving loop and
-    returns its bistatic RCS on a 5-degree grid.  Reports solves/hour, the
-    latency distribution, Gcell-updates/s, and sequential FP64 plain solves of
-    the same jobs (device time per cell measured on a sample, scaled to every
-    job) as the comparison."""
+    returns its bistatic RCS on a 5-degree grid.  Returns solves/hour, the
+    latency distribution, Gcell-updates/s, and two sequential baselines of the
+    same jobs: FP64 plain solves (device time per cell-update measured on the
+    smallest and largest job, scaled to every job) and single-simulation FP32
+    solves (the whole solve -- set-up, 2500 steps, far field -- timed on the
+    smallest and largest job, interpolated in cell count), the latter being
+    what batching and serving gain over running the same fused kernels one
+    job at a time."""
     from meteorscattering_gb300 import build as B
     B.build()
     from meteorscattering_gb300 import engine as E
     from meteorscattering_gb300 import sweep
     steps = 2500
-    if args.workload == "sweep":
-        n = args.jobs or 128
+    if kind == "sweep":
+        n = n or 128
         jobs = sweep.population(n, seed=4, steps=steps)
     else:
-        n = args.jobs or 32
+        n = n or 32
         jobs = sweep.population(n, seed=5, steps=steps, big_fraction=0.1)
     th, ph = sweep.direction_grid(5.0)
     cells = np.array([j.cells for j in jobs], dtype=np.float64)
@@ -385,7 +399,7 @@ def population_bench(args):
     rng = np.random.default_rng(11)
     lat, adm, pending = [], [], {}
     t0 = time.perf_counter()
-    if args.workload == "sweep":
+    if kind == "sweep":
         for j in jobs:
             pending[srv.submit(j.problem(E), th, ph)] = j
     else:
@@ -397,7 +411,7 @@ def population_bench(args):
     submitted = 0
     while len(lat) < n:
         now = time.perf_counter() - t0
-        if args.workload == "serve":
+        if kind == "serve":
             while submitted < n and arrivals[submitted] <= now:
                 pending[srv.submit(jobs[submitted].problem(E), th, ph)] = jobs[submitted]
                 submitted += 1
@@ -411,10 +425,9 @@ def population_bench(args):
     wall = time.perf_counter() - t0
     clocks = clk.stop()
     srv.close()
-    # sequential FP64 plain solves of the same jobs: device time per cell-update
-    # measured on the smallest and the largest job, interpolated in cell count
-    sample = sorted(range(n), key=lambda q: cells[q])
-    sample = [sample[0], sample[-1]]
+    order = sorted(range(n), key=lambda q: cells[q])
+    sample = [order[0], order[-1]]
+    # sequential FP64 plain solves: device time per cell-update, interpolated in cell count
     rate = []
     for q in sample:
         s = E.Simulation(jobs[q].problem(E), form=E.FORM_FP64_PLAIN)
@@ -426,33 +439,68 @@ def population_bench(args):
     (c0, r0), (c1, r1) = rate
     per_cell = np.interp(cells, [c0, c1], [1 / r0, 1 / r1]) if c1 > c0 else np.full_like(cells, 1 / r0)
     plain_s = float((cells * steps * per_cell).sum())
+    # sequential single-simulation FP32 solves: the whole solve, timed
+    solve = []
+    for q in sample:
+        ts = time.perf_counter()
+        s = E.Simulation(jobs[q].problem(E), form=E.FORM_FP32_FUSED)
+        s.advance(steps)
+        s.far_field(th, ph, method=1)
+        s.close()
+        solve.append((cells[q], time.perf_counter() - ts))
+    (c0, t0s), (c1, t1s) = solve
+    single_s = float(np.interp(cells, [c0, c1], [t0s, t1s]).sum()) if c1 > c0 else t0s * n
     lat = np.array(lat)
-    line = {"metric": "RCS solves/hour", "value": n / wall * 3600, "unit": "solves/hour",
-            "n_gpus": 1, "steps": steps, "warmup": 0, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": (f"{n} random trails submitted together (batched sweep)"
-                                    if args.workload == "sweep" else
-                                    f"{n}-job Poisson stream at ~80% load, 10% 384x384x768 trails"),
-                       "jobs": n, "steps_per_job": steps, "rcs_grid_deg": 5,
-                       "hbm_cap_gb": 150, "steps_per_round": 100,
-                       "l2": "inputs far larger than L2 on the large jobs; small jobs are "
-                             "L2-resident between steps (reported as is)"},
+    return {"kind": kind, "jobs": n, "steps_per_job": steps, "wall_s": wall,
+            "solves_per_hour": n / wall * 3600,
             "gcell_updates_per_s": work / wall / 1e9,
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
             "admission_wait_s": {"p50": float(np.percentile(adm, 50)),
                                  "p99": float(np.percentile(adm, 99))},
-            "plain_fp64_sequential": {"solves_per_hour": n / plain_s * 3600,
-                                      "seconds": plain_s,
+            "plain_fp64_sequential": {"solves_per_hour": n / plain_s * 3600, "seconds": plain_s,
                                       "method": "device time per cell-update of FP64 plain measured "
                                                 "on the smallest and largest job, scaled to every job"},
+            "fp32_single_sequential": {"solves_per_hour": n / single_s * 3600, "seconds": single_s,
+                                       "method": "whole FP32 solve (set-up, all steps, far field) timed "
+                                                 "on the smallest and largest job, interpolated in cell "
+                                                 "count over every job"},
             "speedup_vs_plain_sequential": plain_s / wall,
-            "e2e": {"value": n / wall * 3600, "unit": "solves/hour", "h2d_bytes_per_step": 0,
+            "speedup_vs_fp32_single_sequential": single_s / wall,
+            "clocks": clocks}
+
+
+def population_bench(args):
+    r = run_population(args.workload, args.jobs)
+    n = r["jobs"]
+    line = {"metric": "RCS solves/hour", "value": r["solves_per_hour"], "unit": "solves/hour",
+            "n_gpus": 1, "steps": r["steps_per_job"], "warmup": 0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": (f"{n} random trails submitted together (batched sweep)"
+                                    if args.workload == "sweep" else
+                                    f"{n}-job Poisson stream at ~80% load, 10% 384x384x768 trails"),
+                       "jobs": n, "steps_per_job": r["steps_per_job"], "rcs_grid_deg": 5,
+                       "hbm_cap_gb": 150, "steps_per_round": 100,
+                       "l2": "inputs far larger than L2 on the large jobs; small jobs are "
+                             "L2-resident between steps (reported as is)"},
+            "e2e": {"value": r["solves_per_hour"], "unit": "solves/hour", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0,
                     "includes": "problem set-up from host parameters, admission, all steps, "
-                                "far field on the device, D2H of the cross sections"},
-            "clocks": clocks, "wall_s": wall}
+                                "far field on the device, D2H of the cross sections"}}
+    line.update({k: v for k, v in r.items() if k not in ("kind", "jobs", "steps_per_job")})
     print(json.dumps(line), flush=True)
+
+
+def plain_fp64_rate(p, wp2, nu2, B0, ext, trail, steps: int = 3):
+    """Device time per step of the FP64 plain form on the same workload (one
+    warm-up step, then `steps` timed with CUDA events)."""
+    from meteorscattering_gb300 import engine as E
+    sim = E.Simulation(make_problem(E, p, wp2, nu2, B0, ext, trail), form=E.FORM_FP64_PLAIN)
+    sim.advance(1)
+    sim.advance(steps)
+    ms, _ = sim.last_timing()
+    sim.close()
+    return ms
 
 
 def farfield_bench(args):
@@ -631,6 +679,8 @@ def main():
     ap.add_argument("--workload", default="trail768")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain comparison")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the 128-trail batched sweep")
     ap.add_argument("--jobs", type=int, default=0, help="sweep/serve: number of trails")
     args = ap.parse_args()
     if args.workload in ("sweep", "serve") and args.impl == "gb300":
@@ -745,6 +795,19 @@ def main():
                "includes": "problem set-up from host arrays, device allocation + upload, "
                            "K steps, D2H of the near-to-far-field sums"}
 
+    # The FP64 plain form on the same workload (the FP32 form's comparison
+    # target), and the batched sweep of 128 random trails, on one GPU.
+    plain = None
+    if rank == 0 and world == 1 and args.form == "fp32" and not args.no_plain:
+        pm = plain_fp64_rate(p, wp2, nu2, B0, ext, trail, steps=min(3, K))
+        plain = {"ms_per_step": pm, "gcell_updates_per_s": cells / (pm * 1e-3) / 1e9,
+                 "fp32_over_fp64": pm / ms_step, "steps": min(3, K),
+                 "how": "same workload and API, FP64 plain form, one warm-up step then CUDA-event "
+                        "device time of the timed steps"}
+    sweep_summary = None
+    if rank == 0 and world == 1 and args.form == "fp32" and not args.no_sweep:
+        sweep_summary = run_population("sweep")
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -763,7 +826,8 @@ def main():
                            "l2": "state larger than L2 (no flush needed)"},
                 "hbm_gbs": roof["achieved"] if roof else None,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-                "gpu_launches": launches, "host_wall_s": wall}
+                "gpu_launches": launches, "host_wall_s": wall,
+                "plain_fp64": plain, "sweep": sweep_summary}
         print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
