@@ -64,7 +64,8 @@ FALLBACK_HBM_GBS = 6800.0
 
 
 TRAIL_GRIDS = {"trail768": (768, 768, 1536), "trailprof": (128, 384, 1024),
-               "trail384": (384, 384, 768), "trail96": (96, 96, 192)}
+               "trail384": (384, 384, 768), "trail96": (96, 96, 192),
+               "trail768_nodeavg": (768, 768, 1536)}
 
 
 def workload(name: str, steps_total: int):
@@ -82,15 +83,19 @@ def workload(name: str, steps_total: int):
         # 16 along it, r0 = 0.8 m; nu = 3e4; B0 = 5e-5 T dipped 60 degrees;
         # oblique TM plane wave along (theta, phi) = (70, 20) degrees;
         # Lee-Kalluri current driven by E at the current's node (the
-        # reference's two-node average diverges here).
+        # reference's two-node average diverges here; trail768_nodeavg runs
+        # it anyway, for its speed over a few steps).
         N = TRAIL_GRIDS[name]
         f0, gf, nu = 50e6, 30.0, 3e4
         desc = (f"{N[0]}x{N[1]}x{N[2]} tilted magnetized trail, dx=0.2 m, 12-cell CPML "
                 "(m=3, kappa_max=5, alpha_max=0.05), trail axis 30 deg from z in x-z, "
                 "log10 n0 13..16 along the axis, r0=0.8 m, nu=3e4, B0=5e-5 T at 60 deg dip, "
                 "oblique TM plane wave theta=70 phi=20 deg, Lee-Kalluri J (E at the J node)")
+        nodeavg = name.endswith("_nodeavg")
+        if nodeavg:
+            desc = desc.replace("Lee-Kalluri J (E at the J node)", "Lee-Kalluri J (E averaged over two nodes)")
         ext = rd.ExtParams(pmllen=12, pml_m=3.0, kappa_max=5.0, alpha_max=0.05, oblique=1,
-                           exact_coords=1, lk_colocated=1, inc_theta=math.radians(70),
+                           exact_coords=1, lk_colocated=0 if nodeavg else 1, inc_theta=math.radians(70),
                            inc_phi=math.radians(20), inc_psi=0.0)
         dx = rd.C0 / f0 / gf
         trail = rd.TrailParams.tilted(30.0, 0.8, 13.0, 16.0, 0.5 * (N[2] - 1) * dx)
@@ -164,43 +169,62 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
     raise KeyError(kernel)
 
 
-# DRAM traffic of one FP32 step (the pass and the two CPML band kernels),
-# measured by ncu on the 128 x 384 x 1024 profiling case of the large-trail
-# workload (profiles/k_fp32_step_trailprof_full.md); the full-size grid is too
-# large for a multi-pass capture.  The pass moves a fixed multiple of its own
-# bytes over the cells it marches (E and H, plus J and the plasma map in
-# plasma blocks: the tile boxes' halo rows and columns are the excess), a
-# property of the tile shape; the band kernels move a fixed number of bytes
-# per band cell.  A full launch's traffic is both scaled to its grid.
-TILE_J = 8            # tile rows of the pass
-PASS_TRAFFIC_RATIO = (1.060137e9 + 0.903979e9) / (102 * 368 * 1024 * (48 + 0.0368245 * 28))
-BAND_BYTES_PER_CELL = (0.791891e9 + 0.796273e9) / (26 * 384 * 1024 + 102 * 26 * 1024 + 102 * 358 * 26)
+# DRAM traffic of one FP32 step's pass (the wide interior pass and the CPML
+# slab march), measured by ncu on the 128 x 384 x 1024 profiling case of the
+# large-trail workload (profiles/k_fp32_step_wide_trailprof_full.md,
+# profiles/k_fp32_slab_trailprof_full.md); the full-size grid is too large for
+# a multi-pass capture.  The wide pass moves a fixed multiple of its own bytes
+# over the cells it marches (E and H, plus J and the plasma map in plasma
+# blocks; the excess is the tile boxes' halo rows and columns, a property of
+# the tile shape); the slab march moves a fixed number of bytes per cell it
+# marches.  A full launch's traffic is both scaled to its grid.
+TILE_J, TILE_K = 8, 32     # rows and columns of an 8 x 32 tile (the wide pass pairs two)
+PROFILE_PLASMA = 0.0368245  # share of plasma blocks in the profiling case
+WIDE_TRAFFIC_RATIO = (1.011269e9 + 0.809244e9) / (660 * 512 * 102 * (48 + PROFILE_PLASMA * 28))
+SLAB_BYTES_PER_CELL = (0.724610e9 + 0.561876e9) / (216 * 256 * 128 + 1320 * 256 * 26)
 TRAFFIC_WORKLOADS = ("trail768", "trailprof")
 
 
-def band_cells(p: rd.RunParams, L: int) -> int:
-    """Cells the band kernels recompute: a coordinate in the first or last
-    L + 1 indices of an axis."""
+def pass_cells(p: rd.RunParams, L: int):
+    """(cells of the wide interior pass, cells of the slab march) of a
+    non-record step, with the host's tile classification: 8 x 32 tiles whose
+    cells are all interior in j and k (w = L + 1 from every face) pair up
+    along k into 8 x 64 tiles marched over the planes [w, Nx - w); every
+    other tile, over every plane, and the paired tiles over the 2 w x-slab
+    planes, go to the slab march."""
     w = L + 1
-    return (2 * w * p.Ny * p.Nz + (p.Nx - 2 * w) * 2 * w * p.Nz + (p.Nx - 2 * w) * (p.Ny - 2 * w) * 2 * w)
-
-
-def marched_cells(p: rd.RunParams, L: int) -> int:
-    """Cells the fast pass marches: the planes between the band's x planes,
-    without the tile rows lying wholly in the band's y rows."""
-    w = L + 1
-    lo = TILE_J * (w // TILE_J)
-    hi = p.Ny - TILE_J * (-(-(p.Ny - w) // TILE_J))
-    return (p.Nx - 2 * w) * (p.Ny - lo - max(hi, 0)) * p.Nz
+    nzp = -(-p.Nz // TILE_K) * TILE_K
+    ntk, nty = nzp // TILE_K, -(-p.Ny // TILE_J)
+    pairs = 0
+    for ty in range(nty):
+        j0 = ty * TILE_J
+        if not (j0 >= w and j0 + TILE_J <= p.Ny - w):
+            continue
+        run = 0
+        for tk in range(ntk):
+            k0 = tk * TILE_K
+            if k0 >= w and k0 + TILE_K <= p.Nz - w:
+                run += 1
+            else:
+                pairs += run // 2
+                run = 0
+        pairs += run // 2
+    paired = 2 * pairs
+    tiles = ntk * nty
+    cells_tile = TILE_J * TILE_K
+    wide = pairs * 2 * cells_tile * (p.Nx - 2 * w)
+    slab = ((tiles - paired) * p.Nx + paired * 2 * w) * cells_tile
+    return wide, slab
 
 
 def traffic_per_launch(form: str, workload: str, kernel: str, p: rd.RunParams, L: int, plasma: float,
                        per_cell_map: bool):
     """DRAM traffic (read + write bytes) of one step's pass, or None when no
     ncu capture of this workload's kernels is recorded."""
-    if form == "fp32" and kernel.startswith("k_fp32_step") and workload in TRAFFIC_WORKLOADS:
-        own = marched_cells(p, L) * (48 + plasma * (24 + (4 if per_cell_map else 0)))
-        return PASS_TRAFFIC_RATIO * own + BAND_BYTES_PER_CELL * band_cells(p, L)
+    if form == "fp32" and kernel.startswith("k_fp32_step_wide") and workload in TRAFFIC_WORKLOADS:
+        wide, slab = pass_cells(p, L)
+        own = wide * (48 + plasma * (24 + (4 if per_cell_map else 0)))
+        return WIDE_TRAFFIC_RATIO * own + SLAB_BYTES_PER_CELL * slab
     return None
 
 

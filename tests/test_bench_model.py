@@ -2,9 +2,9 @@
 
 The compulsory bytes follow the per-cell-update figures of the step (E, H and
 J read and written, plus the plasma map where the plasma is 3-D), and the
-DRAM traffic estimate scales the ncu capture of the 128 x 384 x 1024
-profiling case to other grids: the pass's bytes per own byte of the cells it
-marches, and the CPML band kernels' bytes per band cell.  On the captured
+DRAM traffic estimate scales the ncu captures of the 128 x 384 x 1024
+profiling case to other grids: the wide interior pass's bytes per own byte of
+the cells it marches, and the slab march's bytes per cell.  On the captured
 grid the estimate must give back the captured bytes.
 """
 import os
@@ -16,35 +16,39 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
-# The profiling capture: the pass read + written, the H and E band kernels.
-CAPTURED_PASS = 1.060137e9 + 0.903979e9
-CAPTURED_BAND = 0.791891e9 + 0.796273e9
+# The profiling captures: the wide pass and the slab march, read + written.
+CAPTURED_WIDE = 1.011269e9 + 0.809244e9
+CAPTURED_SLAB = 0.724610e9 + 0.561876e9
 CAPTURED_PLASMA = 0.0368245
 
 
-def test_band_and_marched_cells():
+def test_pass_cells():
     p, *_ = bench.workload("trailprof", 10)
     w = 13  # 12-cell CPML + 1
-    assert bench.band_cells(p, 12) == p.Nx * p.Ny * p.Nz - (p.Nx - 2 * w) * (p.Ny - 2 * w) * (p.Nz - 2 * w)
-    # planes 13..114; rows 8..375 (tile rows 0-7 and 376-383 lie in the band)
-    assert bench.marched_cells(p, 12) == (p.Nx - 2 * w) * (p.Ny - 16) * p.Nz
+    wide, slab = bench.pass_cells(p, 12)
+    # tiles interior in j: rows 16..363 (44 tile rows); in k: 32..991 (30 tiles, 15 pairs)
+    assert wide == 44 * 15 * 512 * (p.Nx - 2 * w)
+    assert wide + slab == p.Nx * p.Ny * p.Nz  # every cell exactly once (Ny, Nz tile-aligned)
     q, *_ = bench.workload("trail768", 10)
-    assert bench.marched_cells(q, 12) == (768 - 26) * (768 - 16) * 1536
+    wide, slab = bench.pass_cells(q, 12)
+    assert wide == 92 * 23 * 512 * (768 - 26)
+    assert wide + slab == 768 * 768 * 1536
 
 
 def test_traffic_reproduces_the_capture():
     p, *_ = bench.workload("trailprof", 10)
-    t = bench.traffic_per_launch("fp32", "trailprof", "k_fp32_step", p, 12, CAPTURED_PLASMA, True)
-    assert t == pytest.approx(CAPTURED_PASS + CAPTURED_BAND, rel=1e-4)
+    t = bench.traffic_per_launch("fp32", "trailprof", "k_fp32_step_wide+k_fp32_slab", p, 12, CAPTURED_PLASMA,
+                                 True)
+    assert t == pytest.approx(CAPTURED_WIDE + CAPTURED_SLAB, rel=1e-4)
 
 
 def test_traffic_at_full_size_is_near_the_compulsory_bytes():
     p, *_ = bench.workload("trail768", 10)
-    own = bench.algorithmic_bytes("fp32", "k_fp32_step", p, 12, True, 0.0118)
-    t = bench.traffic_per_launch("fp32", "trail768", "k_fp32_step", p, 12, 0.0118, True)
-    # halo re-reads and the band recomputation: a little above the compulsory bytes
+    own = bench.algorithmic_bytes("fp32", "k_fp32_step_wide", p, 12, True, 0.0118)
+    t = bench.traffic_per_launch("fp32", "trail768", "k_fp32_step_wide+k_fp32_slab", p, 12, 0.0118, True)
+    # halo re-reads and the slab march's psi: a little above the compulsory bytes
     assert 1.0 < t / own < 1.25
-    assert bench.traffic_per_launch("fp32", "cfg1", "k_fp32_step", p, 12, 0.0118, True) is None
+    assert bench.traffic_per_launch("fp32", "cfg1", "k_fp32_step_wide", p, 12, 0.0118, True) is None
 
 
 def test_per_cell_update_figure():
