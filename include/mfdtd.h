@@ -278,7 +278,8 @@ int mfdtd_sim_kernel_stats(const mfdtd_sim *s, int32_t which, char *name, size_t
 /* ---- batches (chosen form: many trails in one persistent kernel) ----------
  * No counterpart in the reference, which runs one trail per process and fans
  * trails out as separate PBS jobs (setup/meteorbatch.m, setup/writepbsfile.m).
- * A batch advances up to mfdtd_batch_capacity() FP32 simulations together:
+ * A batch advances up to mfdtd_batch_capacity() FP32 simulations together
+ * (a capacity shared by every batch on the same device):
  * each time step is one launch of a persistent kernel whose CTAs pull
  * (simulation, tile, x-slab) work items from a device queue, boundary tiles
  * first; two steps are replayed as one CUDA graph.  Members keep their fields

@@ -16,6 +16,12 @@ public:
     // (may be null) receives kernel_classes()+1 boundary events.
     int step(int t, bool record, void *stream, void *const *ev);
     static int kernel_classes();
+    // Batch class of a problem's FP32 simulation: 1 when batches march it
+    // with the fast path and the CPML slab march (CPML band on every axis,
+    // oblique incidence without a plate or sphere, no Lee-Kalluri table, an
+    // 8 x 32 tile interior in j and k), else 0 (general path).  A batch holds
+    // simulations of one class.
+    static int batch_class(const Problem &P);
     // Passes run so far by the fast kernel (k_fp32_step_fast: every tile and
     // plane interior, no record step) and by the general one (k_fp32_step).
     long long fast_passes() const;
@@ -69,6 +75,9 @@ public:
     explicit Fp32Batch(int device);
     ~Fp32Batch();
     static int capacity();
+    // Member slots still free on `device`: the capacity is shared by every
+    // batch on a device.
+    static int free_slots(int device);
     // Join at step 0; returns the slot.  Throws when full or when the current
     // update differs from the batch's.
     int add(Fp32Sim *sim, int t0);

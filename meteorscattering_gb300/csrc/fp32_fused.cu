@@ -28,6 +28,8 @@
 
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "fp32.hpp"
@@ -1825,11 +1827,20 @@ __global__ void __launch_bounds__(NTHREADS, 2)
 constexpr int kMaxBatch = 56;  // 56 x 1080-byte Args in the 64 KB constant bank
 __constant__ Args c_jobs[kMaxBatch];
 
+// A work item of the batch: simulation slot `job`, tile `tile` over the planes
+// [ib, ie), marched as `mode` (MARCH_GENERAL, MARCH_FAST or MARCH_SLAB);
+// `first` advances the simulation's incident line and records its probes.
 struct BatchItem {
-    int job, tile, chunk, first;
+    int job, tile;
+    unsigned short ib, ie;
+    unsigned char mode, first, pad[2];
 };
 
-template <int PAR, int JM>
+// SLABK: a batch whose members all qualify for the slab march
+// (Fp32Sim::batch_class): its items take the fast path or the slab march.
+// Otherwise every item takes the general path.  (One kernel holding all three
+// paths spills.)
+template <int PAR, int JM, bool SLABK>
 __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
     k_fp32_batch(const BatchItem *__restrict__ items, const int *__restrict__ n_items, int *next,
                  const Maps *__restrict__ maps, const int *__restrict__ job_t,
@@ -1848,10 +1859,18 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
         const int t = job_t[w.job];
         if (t >= job_end[w.job]) continue;
         const Args &a = c_jobs[w.job];
-        const int ib = a.xbeg + w.chunk * a.chunk;
-        if (!run_item<PAR, JM>(maps[w.job], a, w.tile, ib, min(a.xend, ib + a.chunk), w.first != 0, t, 0, smem_raw,
-                               inited))
-            break;
+        bool ok;
+        if constexpr (SLABK) {
+            if (w.mode == MARCH_FAST)
+                ok = run_item<PAR, JM, MARCH_FAST>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw,
+                                                   inited);
+            else
+                ok = run_item<PAR, JM, MARCH_SLAB>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw,
+                                                   inited);
+        } else {
+            ok = run_item<PAR, JM>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw, inited);
+        }
+        if (!ok) break;
         inited = true;
     }
 }
@@ -2384,6 +2403,13 @@ struct Fp32Sim::Impl {
     int n_slab_items = 0;
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // In a batch of class 1 (Fp32Sim::batch_class): the tiles whose cells are
+    // all interior in j and k (fast path over the interior planes, slab march
+    // over the x-slab planes) and the rest (slab march over every plane);
+    // w = L + 1 with the CPML, else 1.
+    bool slab_eligible = false;
+    int wband = 1;
+    std::vector<int> inner32, edge32;
 
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
@@ -2709,6 +2735,19 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         m.plasma_fraction = nb ? (double)np / (double)nb : 0.0;
         a.plasma = d;
     }
+    {
+        const int w = P.dopml ? P.L + 1 : 1;
+        m.wband = w;
+        m.slab_eligible = batch_class(P) == 1;
+        if (m.slab_eligible) {
+            for (int tl : m.tile_order) {
+                const int j0 = (tl / a.ntk) * TJ, k0 = (tl % a.ntk) * TK;
+                const bool in = j0 >= w && j0 + TJ <= P.Ny - w && k0 >= w && k0 + TK <= P.Nz - w;
+                (in ? m.inner32 : m.edge32).push_back(tl);
+            }
+            if (m.inner32.empty()) m.slab_eligible = false;
+        }
+    }
     if (m.fast_ok) {
         // With the slab march: the wide interior pass marches pairs of tiles
         // whose cells are all interior in j and k, over the planes
@@ -2784,6 +2823,24 @@ void Fp32Sim::init(const Problem &P, void *stream) {
 }
 
 double Fp32Sim::plasma_fraction() const { return impl_->plasma_fraction; }
+
+int Fp32Sim::batch_class(const Problem &P) {
+    const int w = P.dopml ? P.L + 1 : 1;
+    const bool band = P.Nx > 2 * w && P.Ny > 2 * w && P.Nz > 2 * w && P.Nx < 65536 && P.Ny < 65536 && P.Nz < 65536;
+    int jm = 0;
+    if (P.doB0) {
+        bool uniform = !P.lk.empty();
+        for (size_t q = 18; q < P.lk.size() && uniform; q++) uniform = P.lk[q] == P.lk[q % 18];
+        jm = uniform ? 1 : 2;
+    }
+    // the oblique TF/SF corrections run after the pass exactly when there is
+    // no plate or sphere (see init)
+    if (!(band && P.oblique && P.doplate == 0 && jm != 2)) return 0;
+    bool jin = false, kin = false;  // some 8 x 32 tile interior in j and in k
+    for (int j0 = 0; j0 < P.Ny && !jin; j0 += TJ) jin = j0 >= w && j0 + TJ <= P.Ny - w;
+    for (int k0 = 0; k0 < P.Nz && !kin; k0 += TK) kin = k0 >= w && k0 + TK <= P.Nz - w;
+    return jin && kin ? 1 : 0;
+}
 
 int Fp32Sim::kernel_classes() { return 3; }
 long long Fp32Sim::fast_passes() const { return impl_->n_fast; }
@@ -3005,6 +3062,7 @@ struct Fp32Batch::Impl {
     bool dirty = true;
     int chunk = 0;                  // planes per item (0: per-simulation default)
     int ctas_per_sm = 3;
+    int slabk = -1;                 // batch class of the members (Fp32Sim::batch_class); -1: empty
     cudaGraphExec_t graph = nullptr;
     int graph_ctas = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -3021,6 +3079,42 @@ struct Fp32Batch::Impl {
 };
 
 int Fp32Batch::capacity() { return kMaxBatch; }
+
+// The kMaxBatch slots of c_jobs belong to a device's copy of this module, so
+// every batch on a device draws its members' slots from one pool: two
+// batches running at the same time (a server with several batch keys) must
+// not write the same slot.  A batch's own per-slot arrays (step, end step,
+// maps) are indexed by the same slot numbers and hold zeros elsewhere, so its
+// kernels skip the slots of other batches.
+namespace {
+std::mutex g_slot_mu;
+std::map<int, std::vector<char>> g_slot_used;  // device -> slot in use
+int take_slot(int device) {
+    std::lock_guard<std::mutex> lk(g_slot_mu);
+    std::vector<char> &u = g_slot_used[device];
+    if (u.empty()) u.assign(kMaxBatch, 0);
+    for (int q = 0; q < kMaxBatch; q++)
+        if (!u[q]) {
+            u[q] = 1;
+            return q;
+        }
+    return -1;
+}
+void release_slot(int device, int q) {
+    std::lock_guard<std::mutex> lk(g_slot_mu);
+    std::vector<char> &u = g_slot_used[device];
+    if (q >= 0 && q < (int)u.size()) u[q] = 0;
+}
+}  // namespace
+
+int Fp32Batch::free_slots(int device) {
+    std::lock_guard<std::mutex> lk(g_slot_mu);
+    auto it = g_slot_used.find(device);
+    if (it == g_slot_used.end()) return kMaxBatch;
+    int n = 0;
+    for (char c : it->second) n += c ? 0 : 1;
+    return n;
+}
 
 Fp32Batch::Fp32Batch(int device) : impl_(new Impl()) {
     Impl &b = *impl_;
@@ -3039,18 +3133,24 @@ Fp32Batch::Fp32Batch(int device) : impl_(new Impl()) {
     ck(cudaMemsetAsync(b.d_end, 0, 4 * kMaxBatch, b.stream), "memset");
     ck(cudaEventCreate(&b.e0), "event");
     ck(cudaEventCreate(&b.e1), "event");
-    for (int jm = 0; jm < 3; jm++) {
-        auto attr = [](const void *f) {
-            ck(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_B), "attr");
+    {
+        auto attr = [](const void *f, int bytes) {
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes), "attr");
         };
-        if (jm == 0) { attr((const void *)k_fp32_batch<0, 0>); attr((const void *)k_fp32_batch<1, 0>); }
-        if (jm == 1) { attr((const void *)k_fp32_batch<0, 1>); attr((const void *)k_fp32_batch<1, 1>); }
-        if (jm == 2) { attr((const void *)k_fp32_batch<0, 2>); attr((const void *)k_fp32_batch<1, 2>); }
+        attr((const void *)k_fp32_batch<0, 0, false>, SMEM_B); attr((const void *)k_fp32_batch<1, 0, false>, SMEM_B);
+        attr((const void *)k_fp32_batch<0, 1, false>, SMEM_B); attr((const void *)k_fp32_batch<1, 1, false>, SMEM_B);
+        attr((const void *)k_fp32_batch<0, 2, false>, SMEM_B); attr((const void *)k_fp32_batch<1, 2, false>, SMEM_B);
+        attr((const void *)k_fp32_batch<0, 0, true>, SMEM_BS); attr((const void *)k_fp32_batch<1, 0, true>, SMEM_BS);
+        attr((const void *)k_fp32_batch<0, 1, true>, SMEM_BS); attr((const void *)k_fp32_batch<1, 1, true>, SMEM_BS);
     }
     ck(cudaStreamSynchronize(b.stream), "batch set-up");
 }
 
-Fp32Batch::~Fp32Batch() { delete impl_; }
+Fp32Batch::~Fp32Batch() {
+    for (int q = 0; q < kMaxBatch; q++)
+        if (impl_->slot[q]) release_slot(impl_->device, q);
+    delete impl_;
+}
 
 void *Fp32Batch::stream() const { return impl_->stream; }
 
@@ -3061,11 +3161,20 @@ int Fp32Batch::add(Fp32Sim *sim, int t0) {
     if (b.jm >= 0 && m.jm != b.jm)
         throw Error(MFDTD_EINVAL, "batch: every simulation of a batch uses the same current update "
                                   "(Young DI, uniform Lee-Kalluri, or tabulated Lee-Kalluri)");
-    int s = -1;
-    for (int q = 0; q < kMaxBatch; q++)
-        if (!b.slot[q]) { s = q; break; }
-    if (s < 0) throw Error(MFDTD_ENOMEM, "batch: all " + std::to_string(kMaxBatch) + " slots in use");
-    ck(cudaStreamSynchronize(b.stream), "batch");
+    const int cls = m.slab_eligible ? 1 : 0;
+    if (b.slabk >= 0 && cls != b.slabk)
+        throw Error(MFDTD_EINVAL, "batch: every simulation of a batch is of the same batch class (the fast "
+                                  "path with the CPML slab march, or the general path)");
+    const int s = take_slot(b.device);
+    if (s < 0)
+        throw Error(MFDTD_ENOMEM, "batch: all " + std::to_string(kMaxBatch) +
+                                      " member slots of this device are in use (shared by every batch on it)");
+    try {
+        ck(cudaStreamSynchronize(b.stream), "batch");
+    } catch (...) {
+        release_slot(b.device, s);
+        throw;
+    }
     // The state is all zeros in both sets, so the simulation can take the
     // parity of the current tick.
     sim->m_cur_ = (int)(b.tick & 1);
@@ -3081,6 +3190,10 @@ int Fp32Batch::add(Fp32Sim *sim, int t0) {
     b.tsteps[s] = m.tsteps;
     b.host_t[s] = 0;
     b.jm = m.jm;
+    if (b.slabk != cls) {
+        b.slabk = cls;
+        if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
+    }
     b.dirty = true;
     return s;
 }
@@ -3093,11 +3206,15 @@ void Fp32Batch::remove(Fp32Sim *sim) {
             int zero = 0;
             ck(cudaMemcpy(b.d_end + q, &zero, 4, cudaMemcpyHostToDevice), "H2D");
             b.slot[q] = nullptr;
+            release_slot(b.device, q);
             b.dirty = true;
         }
     bool any = false;
     for (int q = 0; q < kMaxBatch; q++) any |= b.slot[q] != nullptr;
-    if (!any) b.jm = -1;
+    if (!any) {
+        b.jm = -1;
+        b.slabk = -1;
+    }
 }
 
 int Fp32Batch::steps_done(const Fp32Sim *sim) const {
@@ -3106,33 +3223,63 @@ int Fp32Batch::steps_done(const Fp32Sim *sim) const {
     return -1;
 }
 
-// Work items of every simulation still short of its step count: boundary
-// tiles of all simulations first (their general path is the slow one), then
-// interior tiles, each split into x-chunks (the slab depth).
+// Work items of every simulation still short of its step count, each tile
+// split into x-chunks (the slab depth).  In a batch of class 1 every member is
+// marched like a single simulation: its interior tiles on the fast path over
+// the interior planes and by the slab march over the x-slab planes, its other
+// tiles by the slab march over every plane.  In a batch of class 0 every item
+// takes the general path (boundary tiles first).  Order: slab marches of whole
+// tile columns and general boundary tiles (the slow items), then fast and
+// general interior items, then the short x-slab items.
 static void build_items(Fp32Batch::Impl &b) {
-    std::vector<BatchItem> first, rest;
+    std::vector<BatchItem> slow, mid, tail;
     for (int q = 0; q < kMaxBatch; q++) {
         Fp32Sim *sim = b.slot[q];
         if (!sim || b.host_t[q] >= b.tsteps[q]) continue;
         Fp32Sim::Impl &m = *sim->impl();
         const int chunk = b.chunk > 0 ? b.chunk : m.a.chunk;
-        const int nch = (m.Nx + chunk - 1) / chunk;
-        for (size_t ti = 0; ti < m.tile_order.size(); ti++)
-            for (int c = 0; c < nch; c++) {
-                BatchItem w{q, m.tile_order[ti], c, ti == 0 && c == 0};
-                ((int)ti < m.n_boundary ? first : rest).push_back(w);
+        const int Nx = m.Nx;
+        bool first = true;
+        auto add = [&](std::vector<BatchItem> &v, int tile, int ib, int ie, int mode) {
+            for (int c0 = ib; c0 < ie; c0 += chunk) {
+                BatchItem w{};
+                w.job = q;
+                w.tile = tile;
+                w.ib = (unsigned short)c0;
+                w.ie = (unsigned short)std::min(ie, c0 + chunk);
+                w.mode = (unsigned char)mode;
+                w.first = first ? 1 : 0;
+                first = false;
+                v.push_back(w);
             }
+        };
+        if (b.slabk == 1) {
+            const int w = m.wband;
+            for (int tl : m.edge32) add(slow, tl, 0, Nx, MARCH_SLAB);
+            for (int tl : m.inner32) add(mid, tl, w, Nx - w, MARCH_FAST);
+            for (int tl : m.inner32) {
+                add(tail, tl, 0, w, MARCH_SLAB);
+                add(tail, tl, Nx - w, Nx, MARCH_SLAB);
+            }
+        } else {
+            for (size_t ti = 0; ti < m.tile_order.size(); ti++)
+                add((int)ti < m.n_boundary ? slow : mid, m.tile_order[ti], 0, Nx, MARCH_GENERAL);
+        }
     }
-    first.insert(first.end(), rest.begin(), rest.end());
-    if ((int)first.size() > b.item_cap) {
+    std::vector<BatchItem> all;
+    all.reserve(slow.size() + mid.size() + tail.size());
+    all.insert(all.end(), slow.begin(), slow.end());
+    all.insert(all.end(), mid.begin(), mid.end());
+    all.insert(all.end(), tail.begin(), tail.end());
+    if ((int)all.size() > b.item_cap) {
         cudaFree(b.items);
-        b.item_cap = (int)first.size() * 2 + 1024;
+        b.item_cap = (int)all.size() * 2 + 1024;
         ck(cudaMalloc(&b.items, sizeof(BatchItem) * b.item_cap), "cudaMalloc");
         if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
     }
-    b.n_items = (int)first.size();
+    b.n_items = (int)all.size();
     if (b.n_items)
-        ck(cudaMemcpyAsync(b.items, first.data(), sizeof(BatchItem) * b.n_items, cudaMemcpyHostToDevice,
+        ck(cudaMemcpyAsync(b.items, all.data(), sizeof(BatchItem) * b.n_items, cudaMemcpyHostToDevice,
                            b.stream), "H2D");
     ck(cudaMemcpyAsync(b.d_n, &b.n_items, 4, cudaMemcpyHostToDevice, b.stream), "H2D");
     b.dirty = false;
@@ -3151,17 +3298,19 @@ static void apply_chunk(Fp32Batch::Impl &b) {
 
 static void launch_tick(Fp32Batch::Impl &b, int par) {
     const dim3 grid(b.sms * b.ctas_per_sm);
+    const int smem = b.slabk == 1 ? SMEM_BS : SMEM_B;
     auto go = [&](auto kern) {
-        kern<<<grid, NTHREADS, SMEM_B, b.stream>>>(b.items, b.d_n, b.d_next, b.d_maps, b.d_t, b.d_end);
+        kern<<<grid, NTHREADS, smem, b.stream>>>(b.items, b.d_n, b.d_next, b.d_maps, b.d_t, b.d_end);
     };
+    const bool sk = b.slabk == 1;
     if (par == 0) {
-        if (b.jm == 0) go(k_fp32_batch<0, 0>);
-        else if (b.jm == 1) go(k_fp32_batch<0, 1>);
-        else go(k_fp32_batch<0, 2>);
+        if (b.jm == 0) sk ? go(k_fp32_batch<0, 0, true>) : go(k_fp32_batch<0, 0, false>);
+        else if (b.jm == 1) sk ? go(k_fp32_batch<0, 1, true>) : go(k_fp32_batch<0, 1, false>);
+        else go(k_fp32_batch<0, 2, false>);
     } else {
-        if (b.jm == 0) go(k_fp32_batch<1, 0>);
-        else if (b.jm == 1) go(k_fp32_batch<1, 1>);
-        else go(k_fp32_batch<1, 2>);
+        if (b.jm == 0) sk ? go(k_fp32_batch<1, 0, true>) : go(k_fp32_batch<1, 0, false>);
+        else if (b.jm == 1) sk ? go(k_fp32_batch<1, 1, true>) : go(k_fp32_batch<1, 1, false>);
+        else go(k_fp32_batch<1, 2, false>);
     }
     const dim3 pgrid(b.sms, kMaxBatch);
     if (par == 0) k_batch_post<0><<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);

@@ -970,7 +970,7 @@ struct ServerJob {
     std::vector<double> theta, phi;
     std::unique_ptr<mfdtd_sim> sim;
     int64_t bytes = 0;
-    int kind = -1;                 // current-update kind (batch key)
+    int kind = -1;                 // batch key: current-update kind + 3 x batch class
     double t_submit = 0, t_admit = 0, t_done = 0;
     int state = 0;                 // 0 queued, 1 running, 2 retired, 3 failed
     bool cancel = false;           // leave at the end of the current round
@@ -1006,15 +1006,15 @@ struct mfdtd_server {
                     cv_work.wait_for(lk, std::chrono::milliseconds(20));
                 if (stop) break;
                 int64_t free_bytes = cap - used;
-                std::map<int, int> members;
-                for (auto &kv : batches) members[kv.first] = (int)kv.second->members.size();
+                // member slots are shared by every batch on the device
+                int slots = mfdtd::Fp32Batch::free_slots(device);
                 while (!queued.empty()) {
                     ServerJob *j = queued.front();
                     if (j->bytes > free_bytes) break;  // arrival order: no overtaking
-                    if (members[j->kind] >= mfdtd::Fp32Batch::capacity()) break;
+                    if (slots <= 0) break;
                     queued.pop_front();
                     free_bytes -= j->bytes;
-                    members[j->kind]++;
+                    slots--;
                     used += j->bytes;
                     admit.push_back(j);
                 }
@@ -1180,7 +1180,7 @@ int mfdtd_server_submit(mfdtd_server *s, const mfdtd_problem *pb, int32_t ndir, 
             for (size_t q = 18; q < P.lk.size() && uniform; q++) uniform = P.lk[q] == P.lk[q % 18];
             kind = uniform ? 1 : 2;
         }
-        j->kind = kind;
+        j->kind = kind + 3 * mfdtd::Fp32Sim::batch_class(P);  // and the batch class
         j->t_submit = mfdtd::wall_s();
         std::lock_guard<std::mutex> lk(s->mu);
         j->id = s->next_id++;

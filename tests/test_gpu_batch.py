@@ -129,3 +129,40 @@ def test_batch_membership_rules(built):
     s.advance(15)                # on its own again
     assert s.step_index == 20
     b.close()
+
+
+def test_two_batches_on_one_device_keep_their_members_apart(built):
+    """Batches of different current updates (Lee-Kalluri, Young DI) run side by
+    side on one device, as a server with several batch keys runs them.  The
+    members' kernel arguments live in constant-memory slots that every batch
+    on the device draws from, so each member must still get its stand-alone
+    result, and the slots must come back when the batches close."""
+    cases = [_long("lk_trail", 60), _long("di_sine_ey", 60)]
+    pbs = [_problem(c) for c in cases]
+    want = [_alone(pb) for pb in pbs]
+    cap = E.Batch.capacity()
+    batches, sims = [], []
+    for pb in pbs:
+        b = E.Batch()
+        s = E.Simulation(pb, form=E.FORM_FP32_FUSED)
+        b.add(s)
+        batches.append(b)
+        sims.append(s)
+    for b in batches:
+        b.run(60)               # both enqueued before either is synchronised
+    for b in batches:
+        b.sync()
+    for s, (ntf, prb) in zip(sims, want):
+        assert np.abs(ntf).max() > 0
+        assert H.rel_l2(s.read_ntf(), ntf) < TOL
+        assert H.rel_l2(s.read_probes(), prb) < TOL_PROBE
+    for b in batches:
+        b.close()
+    # every slot is free again: a batch can take the whole capacity
+    b = E.Batch()
+    full = [E.Simulation(pbs[0], form=E.FORM_FP32_FUSED) for _ in range(cap)]
+    for s in full:
+        b.add(s)
+    b.close()
+    for s in full:
+        s.close()
