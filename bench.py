@@ -173,25 +173,32 @@ def algorithmic_bytes(form: str, kernel: str, p: rd.RunParams, L: int = 10,
 # slab march), measured by ncu on the 128 x 384 x 1024 profiling case of the
 # large-trail workload (profiles/k_fp32_step_wide_trailprof_full.md,
 # profiles/k_fp32_slab_trailprof_full.md); the full-size grid is too large for
-# a multi-pass capture.  The wide pass moves a fixed multiple of its own bytes
-# over the cells it marches (E and H, plus J and the plasma map in plasma
-# blocks; the excess is the tile boxes' halo rows and columns, a property of
-# the tile shape); the slab march moves a fixed number of bytes per cell it
-# marches.  A full launch's traffic is both scaled to its grid.
+# a multi-pass capture.  Three parts scale to a full launch:
+#   * the wide pass over the interior planes moves a fixed multiple of its own
+#     bytes (E and H, plus J and the plasma map in plasma blocks; the excess
+#     is the tile boxes' halo rows and columns, a property of the tile shape):
+#     1.077, from a capture of the pass over the interior planes only;
+#   * its cells on the x-slab planes move a fixed number of bytes each (the
+#     same capture of the pass over every plane, less the first part);
+#   * the slab march moves a fixed number of bytes per cell it marches.
 TILE_J, TILE_K = 8, 32     # rows and columns of an 8 x 32 tile (the wide pass pairs two)
 PROFILE_PLASMA = 0.0368245  # share of plasma blocks in the profiling case
-WIDE_TRAFFIC_RATIO = (1.011269e9 + 0.809244e9) / (660 * 512 * 102 * (48 + PROFILE_PLASMA * 28))
-SLAB_BYTES_PER_CELL = (0.724610e9 + 0.561876e9) / (216 * 256 * 128 + 1320 * 256 * 26)
+PROFILE_OWN = 48 + PROFILE_PLASMA * 28
+WIDE_TRAFFIC_RATIO = (1.011269e9 + 0.809244e9) / (660 * 512 * 102 * PROFILE_OWN)
+WIDE_XSLAB_BYTES_PER_CELL = ((1.372194e9 + 1.150718e9) - WIDE_TRAFFIC_RATIO * 660 * 512 * 102 * PROFILE_OWN) / (
+    660 * 512 * 26)
+SLAB_BYTES_PER_CELL = (0.340058e9 + 0.213999e9) / (216 * 256 * 128)
 TRAFFIC_WORKLOADS = ("trail768", "trailprof")
 
 
 def pass_cells(p: rd.RunParams, L: int):
-    """(cells of the wide interior pass, cells of the slab march) of a
-    non-record step, with the host's tile classification: 8 x 32 tiles whose
-    cells are all interior in j and k (w = L + 1 from every face) pair up
-    along k into 8 x 64 tiles marched over the planes [w, Nx - w); every
-    other tile, over every plane, and the paired tiles over the 2 w x-slab
-    planes, go to the slab march."""
+    """(cells of the wide pass over the interior planes, its cells on the
+    x-slab planes, cells of the slab march) of a non-record step, with the
+    host's tile classification: 8 x 32 tiles whose cells are all interior in
+    j and k (w = L + 1 from every face) pair up along k into 8 x 64 tiles that
+    the wide pass marches over every plane (the 2 w x-slab planes with their
+    x-normal CPML terms); every other tile goes to the slab march, over every
+    plane."""
     w = L + 1
     nzp = -(-p.Nz // TILE_K) * TILE_K
     ntk, nty = nzp // TILE_K, -(-p.Ny // TILE_J)
@@ -209,12 +216,11 @@ def pass_cells(p: rd.RunParams, L: int):
                 pairs += run // 2
                 run = 0
         pairs += run // 2
-    paired = 2 * pairs
-    tiles = ntk * nty
     cells_tile = TILE_J * TILE_K
-    wide = pairs * 2 * cells_tile * (p.Nx - 2 * w)
-    slab = ((tiles - paired) * p.Nx + paired * 2 * w) * cells_tile
-    return wide, slab
+    wide_inner = pairs * 2 * cells_tile * (p.Nx - 2 * w)
+    wide_xslab = pairs * 2 * cells_tile * 2 * w
+    slab = (ntk * nty - 2 * pairs) * p.Nx * cells_tile
+    return wide_inner, wide_xslab, slab
 
 
 def traffic_per_launch(form: str, workload: str, kernel: str, p: rd.RunParams, L: int, plasma: float,
@@ -222,9 +228,9 @@ def traffic_per_launch(form: str, workload: str, kernel: str, p: rd.RunParams, L
     """DRAM traffic (read + write bytes) of one step's pass, or None when no
     ncu capture of this workload's kernels is recorded."""
     if form == "fp32" and kernel.startswith("k_fp32_step_wide") and workload in TRAFFIC_WORKLOADS:
-        wide, slab = pass_cells(p, L)
-        own = wide * (48 + plasma * (24 + (4 if per_cell_map else 0)))
-        return WIDE_TRAFFIC_RATIO * own + SLAB_BYTES_PER_CELL * slab
+        inner, xslab, slab = pass_cells(p, L)
+        own = inner * (48 + plasma * (24 + (4 if per_cell_map else 0)))
+        return WIDE_TRAFFIC_RATIO * own + WIDE_XSLAB_BYTES_PER_CELL * xslab + SLAB_BYTES_PER_CELL * slab
     return None
 
 
@@ -344,6 +350,11 @@ def cpu_baseline(name: str, steps: int, budget_s: float = 20.0):
         cells = p.Nx * p.Ny * nz
         return {"value": cells * n / t_run / 1e9, "unit": "Gcell-updates/s", "cores": threads,
                 "kind": "reference" if use_ref else "port",
+                "note": None if use_ref else
+                ("the C restatement; on an 8-thread x86 host, on the 768x768x67 slab of the "
+                 "reference-format workload, it runs at 0.68x the reference binary built from source "
+                 "(0.0298 against 0.0436 Gcell/s), so ratios against it overstate the reference-relative "
+                 "speed-up by up to 1.46x"),
                 "sample": f"{p.Nx}x{p.Ny}x{nz} slab of the workload, {n} steps, "
                           f"{'reference binary (source/meteor-fork.cpp)' if use_ref else 'oracle/fdtd_oracle.c'} "
                           f"with {threads} OpenMP threads; time-loop seconds"}

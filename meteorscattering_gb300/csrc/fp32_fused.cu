@@ -1707,6 +1707,14 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
         constexpr int CB = C_BW / 4;
         float2 e0 = make_float2(0.f, 0.f), e1 = e0, e2 = e0, hx = e0, hy = e0, hz = e0;
         float2 jx = e0, jy = e0, jz = e0;
+        // The x-slab planes and the domain's x faces (uniform over the CTA):
+        // the x-normal CPML terms of Hy, Hz, Ey, Ez (h_cell / e_cell in their
+        // clean-tile form, same expression order), and the components the
+        // faces do not update keep their old values.
+        const int sxh = hslab(q, Nx, a.L, a.xshift);
+        const bool xin = q < Nx - 1;
+        const bool hpsi = a.dopml && sxh >= 0 && xin;
+        const unsigned oxh = (unsigned)(max(sxh, 0) * Ny + j) * a.Nz + k;  // x-normal psi of (j, k)
         if (tile || row_halo) {
             e0 = lds2(sb + 0 * CB + EW(dj, dk));
             e1 = lds2(sb + 1 * CB + EW(dj, dk));
@@ -1719,6 +1727,23 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
             hx.y = c1h * h0.y - (chy * (e2j.y - e2.y) - chz * (e1k - e1.y));
             hz.x = c1h * h2.x - (chx * (e1i.x - e1.x) - chy * (e0j.x - e0.x));
             hz.y = c1h * h2.y - (chx * (e1i.y - e1.y) - chy * (e0j.y - e0.y));
+            if (!xin) {
+                hz = h2;
+            } else if (hpsi) {  // zx psi: Hz -= c2h p
+                const float B = a.tb->Bh[sxh], A = a.tb->Ahx[sxh], K = a.tb->Khx[sxh];
+                const float dEy0 = e1i.x - e1.x, dEy1 = e1i.y - e1.y;
+                const float p0 = B * a.Ph[PAR][4][oxh] + A * dEy0, p1 = B * a.Ph[PAR][4][oxh + 1] + A * dEy1;
+                if (tile && real) {
+                    a.Ph[PAR ^ 1][4][oxh] = p0;
+                    a.Ph[PAR ^ 1][4][oxh + 1] = p1;
+                }
+                hz.x -= a.c2h * p0;
+                hz.y -= a.c2h * p1;
+                if (a.kappa_on) {
+                    hz.x -= a.c2h * (K * dEy0);
+                    hz.y -= a.c2h * (K * dEy1);
+                }
+            }
             sts2(hn + HNW(0, dj, dk), hx);
             sts2(hn + HNW(2, dj, dk), hz);
             if (tile) {
@@ -1727,6 +1752,23 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
                 const float2 e2i = lds2(sb1 + 2 * CB + EW(dj, dk));
                 hy.x = c1h * h1.x - (chz * (e0.y - e0.x) - chx * (e2i.x - e2.x));
                 hy.y = c1h * h1.y - (chz * (e0k - e0.y) - chx * (e2i.y - e2.y));
+                if (!xin) {
+                    hy = h1;
+                } else if (hpsi) {  // yx psi: Hy += c2h p
+                    const float B = a.tb->Bh[sxh], A = a.tb->Ahx[sxh], K = a.tb->Khx[sxh];
+                    const float dEz0 = e2i.x - e2.x, dEz1 = e2i.y - e2.y;
+                    const float p0 = B * a.Ph[PAR][2][oxh] + A * dEz0, p1 = B * a.Ph[PAR][2][oxh + 1] + A * dEz1;
+                    if (real) {
+                        a.Ph[PAR ^ 1][2][oxh] = p0;
+                        a.Ph[PAR ^ 1][2][oxh + 1] = p1;
+                    }
+                    hy.x += a.c2h * p0;
+                    hy.y += a.c2h * p1;
+                    if (a.kappa_on) {
+                        hy.x += a.c2h * (K * dEz0);
+                        hy.y += a.c2h * (K * dEz1);
+                    }
+                }
                 sts2(hn + HNW(1, dj, dk), hy);
                 if (real) {
                     stg2(a.H[PAR ^ 1][0] + cg, hx);
@@ -1736,7 +1778,7 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
                         jx = ldg2(a.J[0] + cg);
                         jy = ldg2(a.J[1] + cg);
                         jz = ldg2(a.J[2] + cg);
-                        if (t > 0) {
+                        if (t > 0 && q >= 1 && xin) {
                             const float2 eyjm = lds2(sb + 1 * CB + EW(dj - 1, dk));
                             const float ezkm = sb[2 * CB + EW(dj, dk - 1)];
                             j_advance<JM>(a, a.lku, cwq.x, cnu.x, Gk.x, G2k.x, e0.x, e1.x, e2.x, exp2v.x, eyjm.x,
@@ -1751,7 +1793,15 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
             const float ex = sb[0 * CB + EW(dj, -1)], ey = sb[1 * CB + EW(dj, -1)], ez = sb[2 * CB + EW(dj, -1)];
             const float h0 = sb[3 * CB + EW(dj, -1)], h1 = sb[4 * CB + EW(dj, -1)];
             hx.x = c1h * h0 - (chy * (sb[2 * CB + EW(dj + 1, -1)] - ez) - chz * (sb[1 * CB + EW(dj, 0)] - ey));
-            hy.x = c1h * h1 - (chz * (sb[0 * CB + EW(dj, 0)] - ex) - chx * (sb1[2 * CB + EW(dj, -1)] - ez));
+            const float dEz = sb1[2 * CB + EW(dj, -1)] - ez;
+            hy.x = c1h * h1 - (chz * (sb[0 * CB + EW(dj, 0)] - ex) - chx * dEz);
+            if (!xin) {
+                hy.x = h1;
+            } else if (hpsi) {
+                const float p = a.tb->Bh[sxh] * a.Ph[PAR][2][oxh] + a.tb->Ahx[sxh] * dEz;
+                hy.x += a.c2h * p;
+                if (a.kappa_on) hy.x += a.c2h * (a.tb->Khx[sxh] * dEz);
+            }
             hn[HNW(0, dj, -1)] = hx.x;
             hn[HNW(1, dj, -1)] = hy.x;
         }
@@ -1780,6 +1830,35 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
                 ey.y = c1 * e1.y + (cez * (hx.y - hx.x) - cex * (hz.y - hzp.y)) - c2 * jy.y;
                 ez.x = c1 * e2.x + (cex * (hy.x - hyp.x) - cey * (hx.x - hxj.x)) - c2 * jz.x;
                 ez.y = c1 * e2.y + (cex * (hy.y - hyp.y) - cey * (hx.y - hxj.y)) - c2 * jz.y;
+                if (q < 1 || !xin) {  // x faces: Ey, Ez not updated; Ex not at Nx - 1
+                    ey = e1;
+                    ez = e2;
+                    if (!xin) ex = e0;
+                } else {
+                    const int sxe = a.dopml ? eslab(q, Nx, a.L, a.xshift) : -1;
+                    if (sxe >= 0) {  // yx and zx psi: Ey -= c2 p, Ez += c2 p
+                        const float B = a.tb->Be[sxe], A = a.tb->Aex[sxe], K = a.tb->Kex[sxe];
+                        const unsigned oxe = (unsigned)(sxe * Ny + j) * a.Nz + k;
+                        const float dHz0 = hz.x - hzp.x, dHz1 = hz.y - hzp.y;
+                        const float dHy0 = hy.x - hyp.x, dHy1 = hy.y - hyp.y;
+                        const float py0 = B * a.Pe[2][oxe] + A * dHz0, py1 = B * a.Pe[2][oxe + 1] + A * dHz1;
+                        const float pz0 = B * a.Pe[4][oxe] + A * dHy0, pz1 = B * a.Pe[4][oxe + 1] + A * dHy1;
+                        a.Pe[2][oxe] = py0;
+                        a.Pe[2][oxe + 1] = py1;
+                        a.Pe[4][oxe] = pz0;
+                        a.Pe[4][oxe + 1] = pz1;
+                        ey.x -= a.c2e0 * py0;
+                        ey.y -= a.c2e0 * py1;
+                        ez.x += a.c2e0 * pz0;
+                        ez.y += a.c2e0 * pz1;
+                        if (a.kappa_on) {
+                            ey.x -= a.c2e0 * (K * dHz0);
+                            ey.y -= a.c2e0 * (K * dHz1);
+                            ez.x += a.c2e0 * (K * dHy0);
+                            ez.y += a.c2e0 * (K * dHy1);
+                        }
+                    }
+                }
                 stg2(a.E[PAR ^ 1][0] + cg, ex);
                 stg2(a.E[PAR ^ 1][1] + cg, ey);
                 stg2(a.E[PAR ^ 1][2] + cg, ez);
@@ -2433,6 +2512,7 @@ struct Fp32Sim::Impl {
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
+
         for (void *p : allocs) cudaFree(p);
     }
 };
@@ -2791,15 +2871,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
             const int ce = std::max(1, (P.Nx + 95) / 96), cl = (P.Nx + ce - 1) / ce;
             for (int tl : edge)
                 for (int ib = 0; ib < P.Nx; ib += cl) items.push_back(make_int4(tl, ib, std::min(P.Nx, ib + cl), 0));
-            for (int tl : inner) {
-                items.push_back(make_int4(tl, 0, w, 0));
-                items.push_back(make_int4(tl, P.Nx - w, P.Nx, 0));
-            }
             m.slab_items = m.upload(items, s);
             m.n_slab_items = (int)items.size();
-            ck(cudaStreamCreateWithFlags(&m.aux, cudaStreamNonBlocking), "cudaStreamCreate");
-            ck(cudaEventCreateWithFlags(&m.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
-            ck(cudaEventCreateWithFlags(&m.ev_join, cudaEventDisableTiming), "cudaEventCreate");
         } else {
             inner.clear();
             for (int tl : m.tile_order) {
@@ -2807,17 +2880,29 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                 if (!(j0 + TJ <= w || j0 >= P.Ny - w)) inner.push_back(tl);
             }
         }
+        // The wide pass marches its tile pairs over every plane (the x-slab
+        // planes with their x-normal CPML terms); the fast pass the planes
+        // [w, Nx - w).
+        const int xb = m.slab_ok ? 0 : w, xl = m.slab_ok ? P.Nx : len;
         m.af = a;
-        m.af.xbeg = w;
-        m.af.xend = P.Nx - w;
+        m.af.xbeg = xb;
+        m.af.xend = xb + xl;
         const std::vector<int> &fast_tiles = m.slab_ok ? pairs : inner;
         m.af.tile_order = m.upload(fast_tiles, s);
         const int tf = std::max(1, (int)fast_tiles.size());
-        int cf = std::max(1, std::min(len / 16 > 0 ? len / 16 : 1, (want + tf - 1) / tf));
-        cf = std::max(cf, (len + 159) / 160);
-        m.af.chunk = (len + cf - 1) / cf;
-        cf = (len + m.af.chunk - 1) / m.af.chunk;
+        int cf = std::max(1, std::min(xl / 16 > 0 ? xl / 16 : 1, (want + tf - 1) / tf));
+        cf = std::max(cf, (xl + 159) / 160);
+        m.af.chunk = (xl + cf - 1) / cf;
+        cf = (xl + m.af.chunk - 1) / m.af.chunk;
         m.grid_fast = dim3((unsigned)fast_tiles.size(), 1, cf);
+    }
+    // The second stream, for the slab march.  (Running the DFT there, beside
+    // the next step's pass, which only reads the state the DFT reads, was
+    // measured: no gain, both are bound by DRAM bandwidth.)
+    if (m.slab_ok) {
+        ck(cudaStreamCreateWithFlags(&m.aux, cudaStreamNonBlocking), "cudaStreamCreate");
+        ck(cudaEventCreateWithFlags(&m.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&m.ev_join, cudaEventDisableTiming), "cudaEventCreate");
     }
     bytes_ = m.bytes;
 }

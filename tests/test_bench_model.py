@@ -16,23 +16,25 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 sys.path.insert(0, ROOT)
 import bench  # noqa: E402
 
-# The profiling captures: the wide pass and the slab march, read + written.
-CAPTURED_WIDE = 1.011269e9 + 0.809244e9
-CAPTURED_SLAB = 0.724610e9 + 0.561876e9
+# The profiling captures: the wide pass over every plane, the slab march,
+# read + written.
+CAPTURED_WIDE = 1.372194e9 + 1.150718e9
+CAPTURED_SLAB = 0.340058e9 + 0.213999e9
 CAPTURED_PLASMA = 0.0368245
 
 
 def test_pass_cells():
     p, *_ = bench.workload("trailprof", 10)
     w = 13  # 12-cell CPML + 1
-    wide, slab = bench.pass_cells(p, 12)
+    inner, xslab, slab = bench.pass_cells(p, 12)
     # tiles interior in j: rows 16..363 (44 tile rows); in k: 32..991 (30 tiles, 15 pairs)
-    assert wide == 44 * 15 * 512 * (p.Nx - 2 * w)
-    assert wide + slab == p.Nx * p.Ny * p.Nz  # every cell exactly once (Ny, Nz tile-aligned)
+    assert inner == 44 * 15 * 512 * (p.Nx - 2 * w)
+    assert xslab == 44 * 15 * 512 * 2 * w
+    assert inner + xslab + slab == p.Nx * p.Ny * p.Nz  # every cell once (Ny, Nz tile-aligned)
     q, *_ = bench.workload("trail768", 10)
-    wide, slab = bench.pass_cells(q, 12)
-    assert wide == 92 * 23 * 512 * (768 - 26)
-    assert wide + slab == 768 * 768 * 1536
+    inner, xslab, slab = bench.pass_cells(q, 12)
+    assert inner + xslab == 92 * 23 * 512 * 768
+    assert inner + xslab + slab == 768 * 768 * 1536
 
 
 def test_traffic_reproduces_the_capture():
