@@ -401,10 +401,11 @@ def load_peaks():
         return FALLBACK_HBM_GBS, "fallback"
 
 
-def run_population(kind: str, n: int = 0):
+def run_population(kind: str, n: int = 0, capacity_gcells: float = 44.0):
     """Batched sweep ("sweep": 128 random trails submitted together) or serving
     stream ("serve": Poisson arrivals, 90 % sweep-distribution trails and 10 %
-    384 x 384 x 768 trails, offered at about 80 % of the measured capacity):
+    384 x 384 x 768 trails, offered at 80 % of `capacity_gcells`, the
+    Gcell-updates/s the batched sweep measures):
     every trail runs its full 2500 steps through the native serving loop and
     returns its bistatic RCS on a 5-degree grid.  Returns solves/hour, the
     latency distribution, Gcell-updates/s, and two sequential baselines of the
@@ -439,7 +440,7 @@ def run_population(kind: str, n: int = 0):
             pending[srv.submit(j.problem(E), th, ph)] = j
     else:
         # offered load: 80 % of the capacity measured by the batched sweep
-        rate_cells = 30e9 * 0.8
+        rate_cells = capacity_gcells * 1e9 * 0.8
         mean_job = float(cells.mean()) * steps / rate_cells
         arrivals = np.cumsum(rng.exponential(mean_job, size=n))
         arrivals -= arrivals[0]
@@ -506,7 +507,7 @@ def run_population(kind: str, n: int = 0):
 
 
 def population_bench(args):
-    r = run_population(args.workload, args.jobs)
+    r = run_population(args.workload, args.jobs, args.capacity)
     n = r["jobs"]
     line = {"metric": "RCS solves/hour", "value": r["solves_per_hour"], "unit": "solves/hour",
             "n_gpus": 1, "steps": r["steps_per_job"], "warmup": 0, "higher_is_better": True,
@@ -516,6 +517,7 @@ def population_bench(args):
                                     f"{n}-job Poisson stream at ~80% load, 10% 384x384x768 trails"),
                        "jobs": n, "steps_per_job": r["steps_per_job"], "rcs_grid_deg": 5,
                        "hbm_cap_gb": 150, "steps_per_round": 100,
+                       "offered_gcell_updates_per_s": (0.8 * args.capacity if args.workload == "serve" else None),
                        "l2": "inputs far larger than L2 on the large jobs; small jobs are "
                              "L2-resident between steps (reported as is)"},
             "e2e": {"value": r["solves_per_hour"], "unit": "solves/hour", "h2d_bytes_per_step": 0,
@@ -717,6 +719,8 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the FP64 plain comparison")
     ap.add_argument("--no-sweep", action="store_true", help="skip the 128-trail batched sweep")
     ap.add_argument("--jobs", type=int, default=0, help="sweep/serve: number of trails")
+    ap.add_argument("--capacity", type=float, default=44.0,
+                    help="serve: Gcell-updates/s the batched sweep measured; the stream offers 80 %% of it")
     args = ap.parse_args()
     if args.workload in ("sweep", "serve") and args.impl == "gb300":
         population_bench(args)

@@ -298,11 +298,19 @@ int mfdtd_batch_remove(mfdtd_batch *b, mfdtd_sim *s);
 int mfdtd_batch_run(mfdtd_batch *b, int32_t nsteps);
 /* Wait for the batch; updates every member's step index. */
 int mfdtd_batch_sync(mfdtd_batch *b);
-/* Autotuner: time every (slab depth, CTAs per SM) pair on the live members
- * (they advance while being timed) and keep the fastest; best_* may be NULL. */
+/* Autotuner: time every (tile shape, slab depth, CTAs per SM) on the live
+ * members (they advance while being timed) and keep the fastest; best_* may
+ * be NULL.  Tile shapes: 8 x 32 (j, k) tiles everywhere; and, when the
+ * members qualify for the CPML slab march (oblique incidence without a plate
+ * or sphere, no Lee-Kalluri table), their interior tiles paired into 8 x 64
+ * tiles with two cells per thread (at most two CTAs per SM).  A CTA count a
+ * shape cannot run is skipped for that shape. */
 int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depths,
                      const int32_t *ctas_per_sm, int32_t n_ctas, int32_t *best_depth,
                      int32_t *best_ctas);
+/* The (j, k) tile shape the batch runs its interior tiles with: 8 x 32 or
+ * 8 x 64 (see mfdtd_batch_tune). */
+int mfdtd_batch_tile_shape(const mfdtd_batch *b, int32_t *rows, int32_t *cols);
 
 /* ---- serving loop (chosen form) ---------------------------------------------
  * No counterpart in the reference (its sweep driver is MATLAB + PBS,

@@ -87,11 +87,16 @@ public:
     int run(int nticks);
     void sync();
     int steps_done(const Fp32Sim *sim) const;
-    // Try every (slab depth, CTAs per SM) pair on the live batch and keep the
-    // fastest; returns the steps spent.
+    // Try every (tile shape, slab depth, CTAs per SM) on the live batch and
+    // keep the fastest; returns the steps spent.  Tile shapes: 8 x 32 tiles
+    // everywhere, or, for a batch of the slab class, interior tiles paired into
+    // 8 x 64 tiles on the wide path (at most two CTAs per SM).
     int tune(const int *chunks, int nchunks, const int *ctas, int nctas);
     int tuned_chunk() const;
     int tuned_ctas() const;
+    // Columns of the interior tiles: 32 (the fast path), or 64 (pairs on the
+    // wide path; batches of the slab class only).
+    int tuned_tile_cols() const;
     long long tick() const;
     void *stream() const;
     int impl_device() const;

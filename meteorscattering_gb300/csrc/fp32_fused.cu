@@ -1599,6 +1599,7 @@ constexpr int STAGE_TXW = 6 * C_BW;
 constexpr int HNW_COLS = TKW + 2;             // new-H plane columns k0-2 .. k0+TKW-1
 constexpr int HNW_B = 3 * HJ * HNW_COLS * 4;
 constexpr int SMEM_BW = NS * STAGE_BW + 2 * align128(HNW_B) + NS * 8 + 16 + PF_CAP + 128;
+constexpr int SMEM_BATCHW = SMEM_BW > SMEM_BS ? SMEM_BW : SMEM_BS;  // a batch CTA runs either layout
 #define EW(dj, dk) (((dj) + 1) * EKW + (dk) + 4)
 #define HNW(c, dj, dk) (((c) * HJ + (dj) + 1) * HNW_COLS + (dk) + 2)
 
@@ -1607,8 +1608,10 @@ __device__ __forceinline__ void sts2(float *p, float2 v) { *reinterpret_cast<flo
 __device__ __forceinline__ float2 ldg2(const float *p) { return *reinterpret_cast<const float2 *>(p); }
 __device__ __forceinline__ void stg2(float *p, float2 v) { *reinterpret_cast<float2 *>(p) = v; }
 
+// Returns false when a bounded wait ran out (the error flag is then set); the
+// same value in every thread of the CTA.
 template <int PAR, int JM>
-__device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int tile_id, int i_begin, int i_end,
+__device__ __forceinline__ bool wide_item(const Maps &maps, const Args &a, int tile_id, int i_begin, int i_end,
                                           bool first, int t, unsigned char *smem_raw) {
     unsigned char *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
     float *hnb = (float *)(smem + NS * STAGE_BW);
@@ -1618,7 +1621,7 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int Nx = a.Nx, Ny = a.Ny;
     const int k0 = (tile_id % a.ntk) * TK, j0 = (tile_id / a.ntk) * TJ;
-    if (i_begin >= i_end) return;
+    if (i_begin >= i_end) return true;
     const int p0 = max(i_begin - 1, 0), q_last = min(i_end, Nx - 1);
     const size_t plane = (size_t)Ny * a.Nzp;
 
@@ -1884,6 +1887,7 @@ __device__ __forceinline__ void wide_item(const Maps &maps, const Args &a, int t
             }
         }
     }
+    return fail_q < 0;
 }
 
 template <int PAR, int JM>
@@ -1915,18 +1919,25 @@ struct BatchItem {
     unsigned char mode, first, pad[2];
 };
 
-// SLABK: a batch whose members all qualify for the slab march
-// (Fp32Sim::batch_class): its items take the fast path or the slab march.
-// Otherwise every item takes the general path.  (One kernel holding all three
-// paths spills.)
-template <int PAR, int JM, bool SLABK>
-__global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
+// KIND: 0, every item takes the general path; 1, a batch whose members all
+// qualify for the slab march (Fp32Sim::batch_class), items on the fast path
+// (8 x 32 tiles) or the slab march; 2, the same members with their interior
+// tiles paired into 8 x 64 tiles on the wide path (two cells per thread).
+// (One kernel holding every path spills.)  A CTA that moves from one
+// shared-memory layout to the other first invalidates the mbarriers of the
+// layout it leaves: the next item's stages overwrite that memory.
+enum : int { MARCH_WIDE = 3 };
+template <int PAR, int JM, int KIND>
+__global__ void __launch_bounds__(NTHREADS, (JM == 2 || KIND == 2) ? 2 : 3)
     k_fp32_batch(const BatchItem *__restrict__ items, const int *__restrict__ n_items, int *next,
-                 const Maps *__restrict__ maps, const int *__restrict__ job_t,
+                 const Maps *__restrict__ maps, const Maps *__restrict__ mapsw, const int *__restrict__ job_t,
                  const int *__restrict__ job_end) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     __shared__ int s_item;
-    bool inited = false;
+    unsigned char *sm = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+    uint64_t *bar_n = (uint64_t *)(sm + NS * STAGE_B + 2 * align128(HN_B));     // run_item's layout
+    uint64_t *bar_w = (uint64_t *)(sm + NS * STAGE_BW + 2 * align128(HNW_B));   // wide_item's layout
+    int last = 0;  // layout of the previous item: 0 none, 1 run_item, 2 wide_item
     const int n = *n_items;
     for (;;) {
         __syncthreads();  // everyone has read s_item of the previous round
@@ -1938,19 +1949,34 @@ __global__ void __launch_bounds__(NTHREADS, JM == 2 ? 2 : 3)
         const int t = job_t[w.job];
         if (t >= job_end[w.job]) continue;
         const Args &a = c_jobs[w.job];
-        bool ok;
-        if constexpr (SLABK) {
+        if (threadIdx.x == PROD && last != 0) {
+            uint64_t *b = last == 1 ? bar_n : bar_w;
+            for (int q = 0; q < NS; q++)
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&b[q])) : "memory");
+        }
+        bool ok = true;
+        if constexpr (KIND == 2) {
+            if (w.mode == MARCH_WIDE) {
+                ok = wide_item<PAR, JM>(mapsw[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, smem_raw);
+                last = 2;
+            } else {
+                ok = run_item<PAR, JM, MARCH_SLAB>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0,
+                                                   smem_raw, false);
+                last = 1;
+            }
+        } else if constexpr (KIND == 1) {
             if (w.mode == MARCH_FAST)
                 ok = run_item<PAR, JM, MARCH_FAST>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw,
-                                                   inited);
+                                                   false);
             else
-                ok = run_item<PAR, JM, MARCH_SLAB>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw,
-                                                   inited);
+                ok = run_item<PAR, JM, MARCH_SLAB>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0,
+                                                   smem_raw, false);
+            last = 1;
         } else {
-            ok = run_item<PAR, JM>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw, inited);
+            ok = run_item<PAR, JM>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw, false);
+            last = 1;
         }
         if (!ok) break;
-        inited = true;
     }
 }
 
@@ -2489,6 +2515,10 @@ struct Fp32Sim::Impl {
     bool slab_eligible = false;
     int wband = 1;
     std::vector<int> inner32, edge32;
+    // The same members with 8 x 64 tiles: pairs of neighbouring interior
+    // tiles (left tile ids) on the wide path, every other tile on the slab
+    // march.
+    std::vector<int> pairs32, edgew;
 
 
     template <class T> T *alloc(size_t n, cudaStream_t s) {
@@ -2826,6 +2856,20 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                 (in ? m.inner32 : m.edge32).push_back(tl);
             }
             if (m.inner32.empty()) m.slab_eligible = false;
+            std::vector<char> is_in((size_t)a.ntiles, 0);
+            for (int tl : m.inner32) is_in[tl] = 1;
+            std::vector<char> paired((size_t)a.ntiles, 0);
+            for (int ty = 0; ty * TJ < P.Ny; ty++)
+                for (int tk = 0; tk + 1 < a.ntk; tk++) {
+                    const int tl = ty * a.ntk + tk;
+                    if (is_in[tl] && is_in[tl + 1]) {
+                        m.pairs32.push_back(tl);
+                        paired[tl] = paired[tl + 1] = 1;
+                        tk++;
+                    }
+                }
+            for (int tl : m.tile_order)
+                if (!paired[tl]) m.edgew.push_back(tl);
         }
     }
     if (m.fast_ok) {
@@ -3148,6 +3192,9 @@ struct Fp32Batch::Impl {
     int chunk = 0;                  // planes per item (0: per-simulation default)
     int ctas_per_sm = 3;
     int slabk = -1;                 // batch class of the members (Fp32Sim::batch_class); -1: empty
+    int tile_cols = 32;             // class 1: interior tiles 8 x 32 (fast path) or 8 x 64 (wide path)
+    int graph_cols = 0;
+    Maps *d_mapsw = nullptr;        // the members' maps with the wide path's boxes
     cudaGraphExec_t graph = nullptr;
     int graph_ctas = 0;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -3157,6 +3204,7 @@ struct Fp32Batch::Impl {
         if (stream) cudaStreamSynchronize(stream);
         if (graph) cudaGraphExecDestroy(graph);
         cudaFree(items); cudaFree(d_n); cudaFree(d_next); cudaFree(d_t); cudaFree(d_end); cudaFree(d_maps);
+        cudaFree(d_mapsw);
         if (e0) cudaEventDestroy(e0);
         if (e1) cudaEventDestroy(e1);
         if (stream) cudaStreamDestroy(stream);
@@ -3212,6 +3260,7 @@ Fp32Batch::Fp32Batch(int device) : impl_(new Impl()) {
     ck(cudaMalloc(&b.d_t, 4 * kMaxBatch), "cudaMalloc");
     ck(cudaMalloc(&b.d_end, 4 * kMaxBatch), "cudaMalloc");
     ck(cudaMalloc(&b.d_maps, sizeof(Maps) * kMaxBatch), "cudaMalloc");
+    ck(cudaMalloc(&b.d_mapsw, sizeof(Maps) * kMaxBatch), "cudaMalloc");
     ck(cudaMemsetAsync(b.d_n, 0, 4, b.stream), "memset");
     ck(cudaMemsetAsync(b.d_next, 0, 4, b.stream), "memset");
     ck(cudaMemsetAsync(b.d_t, 0, 4 * kMaxBatch, b.stream), "memset");
@@ -3222,11 +3271,17 @@ Fp32Batch::Fp32Batch(int device) : impl_(new Impl()) {
         auto attr = [](const void *f, int bytes) {
             ck(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes), "attr");
         };
-        attr((const void *)k_fp32_batch<0, 0, false>, SMEM_B); attr((const void *)k_fp32_batch<1, 0, false>, SMEM_B);
-        attr((const void *)k_fp32_batch<0, 1, false>, SMEM_B); attr((const void *)k_fp32_batch<1, 1, false>, SMEM_B);
-        attr((const void *)k_fp32_batch<0, 2, false>, SMEM_B); attr((const void *)k_fp32_batch<1, 2, false>, SMEM_B);
-        attr((const void *)k_fp32_batch<0, 0, true>, SMEM_BS); attr((const void *)k_fp32_batch<1, 0, true>, SMEM_BS);
-        attr((const void *)k_fp32_batch<0, 1, true>, SMEM_BS); attr((const void *)k_fp32_batch<1, 1, true>, SMEM_BS);
+        attr((const void *)k_fp32_batch<0, 0, 0>, SMEM_B); attr((const void *)k_fp32_batch<1, 0, 0>, SMEM_B);
+        attr((const void *)k_fp32_batch<0, 1, 0>, SMEM_B); attr((const void *)k_fp32_batch<1, 1, 0>, SMEM_B);
+        attr((const void *)k_fp32_batch<0, 2, 0>, SMEM_B); attr((const void *)k_fp32_batch<1, 2, 0>, SMEM_B);
+        attr((const void *)k_fp32_batch<0, 0, 1>, SMEM_BS); attr((const void *)k_fp32_batch<1, 0, 1>, SMEM_BS);
+        attr((const void *)k_fp32_batch<0, 1, 1>, SMEM_BS); attr((const void *)k_fp32_batch<1, 1, 1>, SMEM_BS);
+        auto attrw = [&](const void *f) {
+            attr(f, SMEM_BATCHW);
+            ck(cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, 100), "attr");
+        };
+        attrw((const void *)k_fp32_batch<0, 0, 2>); attrw((const void *)k_fp32_batch<1, 0, 2>);
+        attrw((const void *)k_fp32_batch<0, 1, 2>); attrw((const void *)k_fp32_batch<1, 1, 2>);
     }
     ck(cudaStreamSynchronize(b.stream), "batch set-up");
 }
@@ -3267,6 +3322,7 @@ int Fp32Batch::add(Fp32Sim *sim, int t0) {
     ck(cudaMemcpyToSymbolAsync(c_jobs, &ba, sizeof(Args), sizeof(Args) * s, cudaMemcpyHostToDevice, b.stream),
        "cudaMemcpyToSymbol");
     ck(cudaMemcpyAsync(b.d_maps + s, &m.maps, sizeof(Maps), cudaMemcpyHostToDevice, b.stream), "H2D");
+    ck(cudaMemcpyAsync(b.d_mapsw + s, &m.mapsw, sizeof(Maps), cudaMemcpyHostToDevice, b.stream), "H2D");
     int zero = 0, end = m.tsteps;
     ck(cudaMemcpyAsync(b.d_t + s, &zero, 4, cudaMemcpyHostToDevice, b.stream), "H2D");
     ck(cudaMemcpyAsync(b.d_end + s, &end, 4, cudaMemcpyHostToDevice, b.stream), "H2D");
@@ -3338,7 +3394,10 @@ static void build_items(Fp32Batch::Impl &b) {
                 v.push_back(w);
             }
         };
-        if (b.slabk == 1) {
+        if (b.slabk == 1 && b.tile_cols == 64) {
+            for (int tl : m.edgew) add(slow, tl, 0, Nx, MARCH_SLAB);
+            for (int tl : m.pairs32) add(mid, tl, 0, Nx, MARCH_WIDE);
+        } else if (b.slabk == 1) {
             const int w = m.wband;
             for (int tl : m.edge32) add(slow, tl, 0, Nx, MARCH_SLAB);
             for (int tl : m.inner32) add(mid, tl, w, Nx - w, MARCH_FAST);
@@ -3381,21 +3440,23 @@ static void apply_chunk(Fp32Batch::Impl &b) {
     }
 }
 
+static int batch_kind(const Fp32Batch::Impl &b) { return b.slabk == 1 ? (b.tile_cols == 64 ? 2 : 1) : 0; }
+
 static void launch_tick(Fp32Batch::Impl &b, int par) {
+    const int kind = batch_kind(b);
     const dim3 grid(b.sms * b.ctas_per_sm);
-    const int smem = b.slabk == 1 ? SMEM_BS : SMEM_B;
+    const int smem = kind == 2 ? SMEM_BATCHW : kind == 1 ? SMEM_BS : SMEM_B;
     auto go = [&](auto kern) {
-        kern<<<grid, NTHREADS, smem, b.stream>>>(b.items, b.d_n, b.d_next, b.d_maps, b.d_t, b.d_end);
+        kern<<<grid, NTHREADS, smem, b.stream>>>(b.items, b.d_n, b.d_next, b.d_maps, b.d_mapsw, b.d_t, b.d_end);
     };
-    const bool sk = b.slabk == 1;
     if (par == 0) {
-        if (b.jm == 0) sk ? go(k_fp32_batch<0, 0, true>) : go(k_fp32_batch<0, 0, false>);
-        else if (b.jm == 1) sk ? go(k_fp32_batch<0, 1, true>) : go(k_fp32_batch<0, 1, false>);
-        else go(k_fp32_batch<0, 2, false>);
+        if (b.jm == 0) kind == 2 ? go(k_fp32_batch<0, 0, 2>) : kind == 1 ? go(k_fp32_batch<0, 0, 1>) : go(k_fp32_batch<0, 0, 0>);
+        else if (b.jm == 1) kind == 2 ? go(k_fp32_batch<0, 1, 2>) : kind == 1 ? go(k_fp32_batch<0, 1, 1>) : go(k_fp32_batch<0, 1, 0>);
+        else go(k_fp32_batch<0, 2, 0>);
     } else {
-        if (b.jm == 0) sk ? go(k_fp32_batch<1, 0, true>) : go(k_fp32_batch<1, 0, false>);
-        else if (b.jm == 1) sk ? go(k_fp32_batch<1, 1, true>) : go(k_fp32_batch<1, 1, false>);
-        else go(k_fp32_batch<1, 2, false>);
+        if (b.jm == 0) kind == 2 ? go(k_fp32_batch<1, 0, 2>) : kind == 1 ? go(k_fp32_batch<1, 0, 1>) : go(k_fp32_batch<1, 0, 0>);
+        else if (b.jm == 1) kind == 2 ? go(k_fp32_batch<1, 1, 2>) : kind == 1 ? go(k_fp32_batch<1, 1, 1>) : go(k_fp32_batch<1, 1, 0>);
+        else go(k_fp32_batch<1, 2, 0>);
     }
     const dim3 pgrid(b.sms, kMaxBatch);
     if (par == 0) k_batch_post<0><<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);
@@ -3405,7 +3466,7 @@ static void launch_tick(Fp32Batch::Impl &b, int par) {
 
 // Two ticks (one of each parity) captured once and replayed.
 static void ensure_graph(Fp32Batch::Impl &b) {
-    if (b.graph && b.graph_ctas == b.ctas_per_sm) return;
+    if (b.graph && b.graph_ctas == b.ctas_per_sm && b.graph_cols == b.tile_cols) return;
     if (b.graph) { cudaGraphExecDestroy(b.graph); b.graph = nullptr; }
     cudaGraph_t g;
     ck(cudaStreamBeginCapture(b.stream, cudaStreamCaptureModeThreadLocal), "capture");
@@ -3415,6 +3476,7 @@ static void ensure_graph(Fp32Batch::Impl &b) {
     ck(cudaGraphInstantiate(&b.graph, g, 0), "cudaGraphInstantiate");
     cudaGraphDestroy(g);
     b.graph_ctas = b.ctas_per_sm;
+    b.graph_cols = b.tile_cols;
 }
 
 int Fp32Batch::run(int nticks) {
@@ -3458,36 +3520,51 @@ int Fp32Batch::tune(const int *chunks, int nchunks, const int *ctas, int nctas) 
     Impl &b = *impl_;
     if (b.jm < 0) return 0;
     double best = 1e300;
-    int best_chunk = b.chunk, best_ctas = b.ctas_per_sm, ticks = 0;
+    int best_chunk = b.chunk, best_ctas = b.ctas_per_sm, best_cols = b.tile_cols, ticks = 0;
     b.tune_log.clear();
-    for (int ci = 0; ci < nchunks; ci++)
-        for (int ki = 0; ki < nctas; ki++) {
-            int left = 1 << 30;
-            for (int q = 0; q < kMaxBatch; q++)
-                if (b.slot[q]) left = std::min(left, b.tsteps[q] - b.host_t[q]);
-            if (left < 4) break;
-            b.chunk = chunks[ci];
-            b.ctas_per_sm = std::max(1, std::min(ctas[ki], b.jm == 2 ? 2 : 3));
-            apply_chunk(b);
-            b.dirty = true;
-            run(2);  // settle (graph capture, item rebuild)
-            ck(cudaEventRecord(b.e0, b.stream), "event");
-            run(2);
-            ck(cudaEventRecord(b.e1, b.stream), "event");
-            ck(cudaEventSynchronize(b.e1), "event");
-            float ms = 0;
-            cudaEventElapsedTime(&ms, b.e0, b.e1);
-            b.tune_log.push_back({chunks[ci] * 16 + b.ctas_per_sm, ms / 2});
-            ticks += 4;
-            if (ms < best) { best = ms; best_chunk = b.chunk; best_ctas = b.ctas_per_sm; }
-        }
+    // tile shapes: 8 x 32 everywhere, or (slab class) interior tiles paired
+    // into 8 x 64 on the wide path, at most two CTAs per SM
+    const int shapes[2] = {32, 64};
+    const int nshapes = b.slabk == 1 ? 2 : 1;
+    for (int si = 0; si < nshapes; si++)
+        for (int ci = 0; ci < nchunks; ci++)
+            for (int ki = 0; ki < nctas; ki++) {
+                int left = 1 << 30;
+                for (int q = 0; q < kMaxBatch; q++)
+                    if (b.slot[q]) left = std::min(left, b.tsteps[q] - b.host_t[q]);
+                if (left < 4) break;
+                const int cap = (b.jm == 2 || shapes[si] == 64) ? 2 : 3;
+                if (ctas[ki] > cap && nctas > 1) continue;  // that occupancy does not exist for the shape
+                b.tile_cols = shapes[si];
+                b.chunk = chunks[ci];
+                b.ctas_per_sm = std::max(1, std::min(ctas[ki], cap));
+                apply_chunk(b);
+                b.dirty = true;
+                run(2);  // settle (graph capture, item rebuild)
+                ck(cudaEventRecord(b.e0, b.stream), "event");
+                run(2);
+                ck(cudaEventRecord(b.e1, b.stream), "event");
+                ck(cudaEventSynchronize(b.e1), "event");
+                float ms = 0;
+                cudaEventElapsedTime(&ms, b.e0, b.e1);
+                b.tune_log.push_back({(b.tile_cols * 1024 + chunks[ci]) * 16 + b.ctas_per_sm, ms / 2});
+                ticks += 4;
+                if (ms < best) {
+                    best = ms;
+                    best_chunk = b.chunk;
+                    best_ctas = b.ctas_per_sm;
+                    best_cols = b.tile_cols;
+                }
+            }
     b.chunk = best_chunk;
     b.ctas_per_sm = best_ctas;
+    b.tile_cols = best_cols;
     apply_chunk(b);
     b.dirty = true;
     return ticks;
 }
 
+int Fp32Batch::tuned_tile_cols() const { return impl_->tile_cols; }
 int Fp32Batch::tuned_chunk() const { return impl_->chunk; }
 int Fp32Batch::impl_device() const { return impl_->device; }
 int Fp32Batch::tuned_ctas() const { return impl_->ctas_per_sm; }

@@ -928,6 +928,14 @@ int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depth
     });
 }
 
+int mfdtd_batch_tile_shape(const mfdtd_batch *b, int32_t *rows, int32_t *cols) {
+    return guarded([&] {
+        if (!b) throw Error(MFDTD_EINVAL, "NULL batch");
+        if (rows) *rows = 8;
+        if (cols) *cols = b->fb->tuned_tile_cols();
+    });
+}
+
 int mfdtd_run_rundir(const char *dir, const mfdtd_run_opts *opts) {
     return guarded([&] {
         if (!dir) throw Error(MFDTD_EINVAL, "NULL dir");

@@ -39,6 +39,7 @@ EXPORTS = (
     "mfdtd_batch_run", "mfdtd_batch_sync", "mfdtd_batch_tune", "mfdtd_server_create",
     "mfdtd_server_destroy", "mfdtd_server_submit", "mfdtd_server_poll", "mfdtd_server_stats",
     "mfdtd_server_cancel", "mfdtd_sim_read_slices", "mfdtd_sim_plasma_fraction",
+    "mfdtd_batch_tile_shape",
 )
 
 
@@ -133,6 +134,7 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
         "mfdtd_batch_sync": (C.c_int, [vp]),
         "mfdtd_batch_tune": (C.c_int, [vp, C.POINTER(i32), i32, C.POINTER(i32), i32,
                                        C.POINTER(i32), C.POINTER(i32)]),
+        "mfdtd_batch_tile_shape": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i32)]),
         "mfdtd_server_create": (C.c_int, [i32, i64, i32, C.POINTER(vp)]),
         "mfdtd_server_destroy": (None, [vp]),
         "mfdtd_server_submit": (C.c_int, [vp, vp, i32, dp, dp, C.POINTER(i64)]),
@@ -417,12 +419,20 @@ class Batch:
         _check(load_library().mfdtd_batch_sync(self._h))
 
     def tune(self, slab_depths=(16, 32, 64, 128), ctas_per_sm=(2, 3)):
+        """Try every (tile shape, slab depth, CTAs per SM); returns the chosen
+        (slab depth, CTAs per SM).  tile_shape() gives the chosen shape."""
         d = (C.c_int32 * len(slab_depths))(*slab_depths)
         c = (C.c_int32 * len(ctas_per_sm))(*ctas_per_sm)
         bd, bc = C.c_int32(), C.c_int32()
         _check(load_library().mfdtd_batch_tune(self._h, d, len(slab_depths), c, len(ctas_per_sm),
                                                C.byref(bd), C.byref(bc)))
         return bd.value, bc.value
+
+    def tile_shape(self):
+        """(rows, cols) of the (j, k) tiles the batch runs its interior on."""
+        r, c = C.c_int32(), C.c_int32()
+        _check(load_library().mfdtd_batch_tile_shape(self._h, C.byref(r), C.byref(c)))
+        return r.value, c.value
 
     def close(self):
         if self._h:

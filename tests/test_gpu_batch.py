@@ -166,3 +166,36 @@ def test_two_batches_on_one_device_keep_their_members_apart(built):
     b.close()
     for s in full:
         s.close()
+
+
+def test_batch_tile_shapes_under_the_autotuner(built):
+    """Members that qualify for the CPML slab march (oblique trails with a pair
+    of interior 8 x 32 tiles along k): the autotuner times 8 x 32 tiles (fast
+    path) and 8 x 64 tiles (wide path, two cells per thread) on the live batch,
+    so the members advance under both shapes while it tunes, and the results
+    still match the stand-alone runs."""
+    cases = []
+    for N, steps in (((40, 48, 128), 140), ((48, 40, 128), 130)):
+        cases.append(golden_cases.trail_case(N=N, steps=steps))
+
+    def problem(c):
+        p, wp, nu, B0, ext, tr = c
+        pb = E.Problem.from_params(p, np.asarray(wp).reshape(-1, order="F").reshape(p.Nx, p.Ny),
+                                   np.asarray(nu).reshape(-1, order="F").reshape(p.Nx, p.Ny), B0)
+        return pb.set_ext(ext).set_trail(tr)
+
+    want = [_alone(problem(c)) for c in cases]
+    b = E.Batch()
+    sims = [E.Simulation(problem(c), form=E.FORM_FP32_FUSED) for c in cases]
+    for s in sims:
+        b.add(s)
+    depth, ctas = b.tune((16, 48), (2, 3))   # 2 shapes x 2 depths, 4 steps each
+    assert b.tile_shape() in ((8, 32), (8, 64))
+    b.run(200)
+    b.sync()
+    for s, c, (ntf, prb) in zip(sims, cases, want):
+        assert s.step_index == c[0].tsteps
+        assert np.abs(ntf).max() > 0
+        assert H.rel_l2(s.read_ntf(), ntf) < TOL
+        assert H.rel_l2(s.read_probes(), prb) < TOL_PROBE
+    b.close()
