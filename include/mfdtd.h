@@ -322,7 +322,9 @@ int mfdtd_batch_tile_shape(const mfdtd_batch *b, int32_t *rows, int32_t *cols);
  * batches (one per current-update kind, overlapping on the device), retires
  * the jobs that reached their step count -- far field computed on the device
  * (method 1: the contraction on the tensor cores), device memory freed -- and
- * admits waiting jobs into the freed space.
+ * admits waiting jobs into the freed space.  A job of at least 2^25 cells
+ * fills the GPU by itself: it takes no batch slot and marches alone, with the
+ * single-simulation kernels on its own stream, while the batches run.
  * Fields stay on the device from admission to retirement. */
 typedef struct mfdtd_server mfdtd_server;
 int mfdtd_server_create(int32_t device, int64_t hbm_cap_bytes, int32_t steps_per_round,

@@ -724,9 +724,53 @@ __device__ __forceinline__ SlabCell slab_cell(const Args &a, int j, int k) {
     return c;
 }
 
+// The six psi values of a cell's H (or E) update on plane i, as h_slab (or
+// e_slab) uses them; zero where unused.  The slab march loads them one plane
+// ahead, so that their latency overlaps the previous plane's work.
+struct Psi6 {
+    float p0, p1, p2, p3, p4, p5;
+};
+template <int PAR>
+__device__ __forceinline__ Psi6 h_slab_psi(const Args &a, int i, const SlabCell &sc, bool want_y, bool want_z) {
+    const int sxh = hslab(i, a.Nx, a.L, a.xshift);
+    const bool xin = i < a.Nx - 1;
+    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const bool ux = sc.jn && sc.kn, uy = want_y && xin && sc.kn, uz = want_z && xin && sc.jn;
+    const unsigned oy = sc.oyh + (unsigned)i * PY, oz = sc.ozh + (unsigned)i * PZ,
+                   ox = (unsigned)max(sxh, 0) * PX + sc.ox;
+    float *const *R = a.Ph[PAR];
+    Psi6 q{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (ux && sc.syh >= 0) q.p0 = R[0][oy];
+    if (ux && sc.szh >= 0) q.p1 = R[1][oz];
+    if (uy && sxh >= 0) q.p2 = R[2][ox];
+    if (uy && sc.szh >= 0) q.p3 = R[3][oz];
+    if (uz && sxh >= 0) q.p4 = R[4][ox];
+    if (uz && sc.syh >= 0) q.p5 = R[5][oy];
+    return q;
+}
+__device__ __forceinline__ Psi6 e_slab_psi(const Args &a, int i, const SlabCell &sc) {
+    const int sxe = eslab(i, a.Nx, a.L, a.xshift);
+    const bool iy = i >= 1 && i < a.Nx - 1;
+    const bool ux = i < a.Nx - 1 && sc.j1 && sc.jn && sc.k1 && sc.kn, uy = iy && sc.k1, uz = iy && sc.j1;
+    const bool xp = sxe >= 0 && sc.jn && sc.kn;
+    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const unsigned oy = sc.oye + (unsigned)i * PY, oz = sc.oze + (unsigned)i * PZ,
+                   ox = (unsigned)max(sxe, 0) * PX + sc.ox;
+    float *const *Pe = a.Pe;
+    Psi6 q{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (ux && sc.sye >= 0) q.p0 = Pe[0][oy];
+    if (ux && sc.sze >= 0) q.p1 = Pe[1][oz];
+    if (uy && xp) q.p2 = Pe[2][ox];
+    if (uy && sc.sze >= 0 && sc.jn) q.p3 = Pe[3][oz];
+    if (uz && xp) q.p4 = Pe[4][ox];
+    if (uz && sc.sye >= 0 && sc.kn) q.p5 = Pe[5][oy];
+    return q;
+}
+
 template <int PAR, class Src>
 __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, int sxh, const Src &src,
-                                       const SlabCell &sc, bool store_psi, bool want_y, bool want_z) {
+                                       const SlabCell &sc, bool store_psi, bool want_y, bool want_z,
+                                       const Psi6 &ps) {
     HVal o;
     o.x = src.h(0);
     o.y = src.h(1);
@@ -737,15 +781,8 @@ __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, in
     const bool ux = sc.jn && sc.kn, uy = want_y && xin && sc.kn, uz = want_z && xin && sc.jn;
     const unsigned oy = sc.oyh + (unsigned)i * PY, oz = sc.ozh + (unsigned)i * PZ,
                    ox = (unsigned)max(sxh, 0) * PX + sc.ox;
-    float *const *R = a.Ph[PAR];
     float *const *W = a.Ph[PAR ^ 1];
-    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f;
-    if (ux && sc.syh >= 0) p0 = R[0][oy];
-    if (ux && sc.szh >= 0) p1 = R[1][oz];
-    if (uy && sxh >= 0) p2 = R[2][ox];
-    if (uy && sc.szh >= 0) p3 = R[3][oz];
-    if (uz && sxh >= 0) p4 = R[4][ox];
-    if (uz && sc.syh >= 0) p5 = R[5][oy];
+    const float p0 = ps.p0, p1 = ps.p1, p2 = ps.p2, p3 = ps.p3, p4 = ps.p4, p5 = ps.p5;
     if (ux) {
         const float dEz = src.ej(2) - ez;
         const float dEy = src.ek(1) - ey;
@@ -806,22 +843,15 @@ __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, in
 template <int PAR, class HS>
 __device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, int sxe, float ex, float ey, float ez,
                                        const HVal &hv, const HS &hs, float jx, float jy, float jz,
-                                       const SlabCell &sc) {
+                                       const SlabCell &sc, const Psi6 &ps) {
     const float c1 = a.c1e0, c2 = a.c2e0, cx = a.cex, cy = a.cey, cz = a.cez;
     const bool iy = i >= 1 && i < a.Nx - 1;
     const bool ux = i < a.Nx - 1 && sc.j1 && sc.jn && sc.k1 && sc.kn, uy = iy && sc.k1, uz = iy && sc.j1;
-    const bool xp = sxe >= 0 && sc.jn && sc.kn;
     const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
     const unsigned oy = sc.oye + (unsigned)i * PY, oz = sc.oze + (unsigned)i * PZ,
                    ox = (unsigned)max(sxe, 0) * PX + sc.ox;
     float *const *Pe = a.Pe;
-    float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f, p4 = 0.f, p5 = 0.f;
-    if (ux && sc.sye >= 0) p0 = Pe[0][oy];
-    if (ux && sc.sze >= 0) p1 = Pe[1][oz];
-    if (uy && xp) p2 = Pe[2][ox];
-    if (uy && sc.sze >= 0 && sc.jn) p3 = Pe[3][oz];
-    if (uz && xp) p4 = Pe[4][ox];
-    if (uz && sc.sye >= 0 && sc.kn) p5 = Pe[5][oy];
+    const float p0 = ps.p0, p1 = ps.p1, p2 = ps.p2, p3 = ps.p3, p4 = ps.p4, p5 = ps.p5;
     if (ux) {
         const float dHz = hv.z - hs.hj(2);
         const float dHy = hv.y - hs.hk(1);
@@ -1085,7 +1115,7 @@ enum : int { MARCH_GENERAL = 0, MARCH_FAST = 1, MARCH_SLAB = 2 };
 
 // The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
 // or -1.
-template <int PAR, int JM, bool CLEAN, int MODE = MARCH_GENERAL>
+template <int PAR, int JM, bool CLEAN, int MODE = MARCH_GENERAL, bool PSIPF = true>
 __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &c, int t, int record,
                                      bool tf_in) {
     constexpr bool FASTONLY = MODE == MARCH_FAST, SLAB = MODE == MARCH_SLAB;
@@ -1156,7 +1186,14 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
     float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
     SlabCell sc{};
-    if constexpr (SLAB) sc = slab_cell(a, j, k);
+    Psi6 nhp{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nep = nhp;  // SLAB with PSIPF: psi of the next plane
+    if constexpr (SLAB) {
+        sc = slab_cell(a, j, k);
+        if (PSIPF && in_grid) {
+            nhp = h_slab_psi<PAR>(a, c.p0, sc, warp != TJ, warp != TJ + 1);
+            if (valid && c.p0 >= c.i_begin) nep = e_slab_psi(a, c.p0, sc);
+        }
+    }
     // The stage slot of plane q and the cell offset advance with q (no
     // modulo or 64-bit multiply per plane).
     int slot = 0;
@@ -1167,6 +1204,15 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         const bool pl = npl;  // this plane's block holds plasma
         npl = q + 1 < c.i_end && plasma_at(a, c, q + 1);
         if (npl) pf_load(q + 1, nwq, nnu);
+        Psi6 hps{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, eps = hps;  // SLAB: this plane's psi
+        if constexpr (SLAB && PSIPF) {
+            hps = nhp;
+            eps = nep;
+            if (in_grid && q + 1 < c.i_end) {
+                nhp = h_slab_psi<PAR>(a, q + 1, sc, warp != TJ, warp != TJ + 1);
+                if (valid && q + 1 >= c.i_begin) nep = e_slab_psi(a, q + 1, sc);
+            }
+        }
         const int slot1 = slot == NS - 1 ? 0 : slot + 1;
         float *hn = c.hn + (q & 1) * (align128(HN_B) / 4);  // this plane's new-H buffer
         // Stages q and q+1 are resident: the barrier of the previous plane
@@ -1303,9 +1349,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         // ---- H of this plane: tile (all comps), halo row (Hx, Hz), halo column (Hx, Hy)
         HVal hv = {0.f, 0.f, 0.f};
         if constexpr (SLAB) {
-            if (in_grid)
+            if (in_grid) {
+                if constexpr (!PSIPF) hps = h_slab_psi<PAR>(a, i, sc, warp != TJ, warp != TJ + 1);
                 hv = h_slab<PAR>(a, *c.tbs, i, hslab(i, Nx, L, a.xshift), StageSrc{s, s1, dj, dk}, sc, tile && real,
-                                 warp != TJ, warp != TJ + 1);
+                                 warp != TJ, warp != TJ + 1, hps);
+            }
         } else {
             if (in_grid)
                 hv = h_cell<PAR, CLEAN>(a, i, j, k, StageSrc{s, s1, dj, dk}, tile && real, warp != TJ,
@@ -1327,9 +1375,11 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         if (valid && real) {
             const float ex_old = s.e[0][EIDX(dj, dk)];
             EVal ev;
+            if constexpr (SLAB && !PSIPF) eps = e_slab_psi(a, i, sc);
             if constexpr (SLAB)
                 ev = e_slab<PAR>(a, *c.tbs, i, eslab(i, Nx, L, a.xshift), ex_old, s.e[1][EIDX(dj, dk)],
-                                 s.e[2][EIDX(dj, dk)], hv, StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, sc);
+                                 s.e[2][EIDX(dj, dk)], hv, StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, sc,
+                                 eps);
             else
                 ev = e_cell<PAR, CLEAN>(a, i, j, k, ex_old, s.e[1][EIDX(dj, dk)], s.e[2][EIDX(dj, dk)], hv,
                                         StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, tf_in,
@@ -1439,7 +1489,7 @@ __device__ __forceinline__ void record_probes(const Args &a, int t) {
 // CTA's stage mbarriers hold an earlier item's objects (they are invalidated
 // and re-initialised).  Returns false when a bounded wait ran out (the
 // simulation's error flag is then set).
-template <int PAR, int JM, int MODE = MARCH_GENERAL>
+template <int PAR, int JM, int MODE = MARCH_GENERAL, bool PSIPF = true>
 __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int tile_id, int i_begin, int i_end,
                                          bool first, int t, int record, unsigned char *smem_raw,
                                          bool inited) {
@@ -1506,7 +1556,7 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
 
     int fail_q;
     if constexpr (MODE == MARCH_SLAB) {
-        fail_q = march<PAR, JM, false, MARCH_SLAB>(maps, a, c, t, 0, false);
+        fail_q = march<PAR, JM, false, MARCH_SLAB, PSIPF>(maps, a, c, t, 0, false);
     } else {
         const TileInfo ti = classify(a, c.j0, c.k0, record);
         if constexpr (MODE == MARCH_FAST)
@@ -1561,16 +1611,20 @@ __global__ void __launch_bounds__(NTHREADS, 4)
 
 // The CPML slabs and domain edges of a non-record step, as marches of their
 // own (MARCH_SLAB), run on a second stream alongside k_fp32_step_wide, which
-// then marches only the tiles and planes whose every cell is interior.  A work
-// item is (tile, first plane, end plane): every tile over the x-slab planes
-// [0, w) and [Nx - w, Nx), and the tiles that reach into the y or z slabs (or
-// past the grid) over all planes, in x-chunks (w = L + 1 with the CPML, else
-// 1).  The two kernels write disjoint cells of the new state and read the old
-// one, so they need no ordering; each CTA recomputes the halo H its E update
-// needs, as in the pass.  The CPML corrections are those of the general path
-// (h_cell, e_cell), so the results are the pass-plus-band-kernels ones.
+// marches the tile pairs whose every cell is interior in j and k over every
+// plane (the x-slab planes with their x-normal CPML terms).  A work item is
+// (tile, first plane, end plane): the tiles that reach into the y or z slabs
+// (or past the grid), and interior tiles left without a partner, over all
+// planes in x-chunks.  The two kernels write disjoint cells of the new state
+// and read the old one, so they need no ordering; each CTA recomputes the
+// halo H its E update needs, as in the pass.  The CPML corrections are those
+// of the general path (h_cell, e_cell) in lean form (h_slab, e_slab), equal
+// to the pass-plus-band-kernels results up to FP32 rounding.  Each thread
+// loads its cell's psi values one plane ahead (Psi6), which takes their
+// latency off the plane loop; the registers that holds limit the kernel to
+// two CTAs per SM (at three it spills and runs slower).
 template <int PAR, int JM>
-__global__ void __launch_bounds__(NTHREADS, 3)
+__global__ void __launch_bounds__(NTHREADS, 2)
     k_fp32_slab(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t,
                 const int4 *__restrict__ items) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -1968,9 +2022,9 @@ __global__ void __launch_bounds__(NTHREADS, (JM == 2 || KIND == 2) ? 2 : 3)
             if (w.mode == MARCH_FAST)
                 ok = run_item<PAR, JM, MARCH_FAST>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw,
                                                    false);
-            else
-                ok = run_item<PAR, JM, MARCH_SLAB>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0,
-                                                   smem_raw, false);
+            else  // (three CTAs per SM: no registers for the psi prefetch)
+                ok = run_item<PAR, JM, MARCH_SLAB, false>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0,
+                                                          smem_raw, false);
             last = 1;
         } else {
             ok = run_item<PAR, JM>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw, false);

@@ -979,6 +979,7 @@ struct ServerJob {
     std::unique_ptr<mfdtd_sim> sim;
     int64_t bytes = 0;
     int kind = -1;                 // batch key: current-update kind + 3 x batch class
+    bool solo = false;             // marched alone on its own stream (kSoloCells), not in a batch
     double t_submit = 0, t_admit = 0, t_done = 0;
     int state = 0;                 // 0 queued, 1 running, 2 retired, 3 failed
     bool cancel = false;           // leave at the end of the current round
@@ -986,6 +987,12 @@ struct ServerJob {
     std::string err;
     std::vector<double> result;
 };
+
+// A job of at least this many cells fills the GPU by itself: batching gains it
+// nothing, and inside a batch every tick waits for it.  The server marches it
+// as a single simulation (its own stream, the single-simulation kernels)
+// beside the batches.
+constexpr int64_t kSoloCells = int64_t(1) << 25;
 
 }  // namespace
 
@@ -1019,10 +1026,10 @@ struct mfdtd_server {
                 while (!queued.empty()) {
                     ServerJob *j = queued.front();
                     if (j->bytes > free_bytes) break;  // arrival order: no overtaking
-                    if (slots <= 0) break;
+                    if (!j->solo && slots <= 0) break;
                     queued.pop_front();
                     free_bytes -= j->bytes;
-                    slots--;
+                    if (!j->solo) slots--;
                     used += j->bytes;
                     admit.push_back(j);
                 }
@@ -1035,14 +1042,16 @@ struct mfdtd_server {
                     o.quiet = 1;
                     j->sim.reset(new mfdtd_sim());
                     j->sim->init(j->P, &o);
-                    auto &b = batches[j->kind];
-                    if (!b) {
-                        b.reset(new mfdtd_batch());
-                        b->fb.reset(new mfdtd::Fp32Batch(device));
+                    if (!j->solo) {
+                        auto &b = batches[j->kind];
+                        if (!b) {
+                            b.reset(new mfdtd_batch());
+                            b->fb.reset(new mfdtd::Fp32Batch(device));
+                        }
+                        b->fb->add(j->sim->f32.get(), 0);
+                        j->sim->batch = b.get();
+                        b->members.push_back(j->sim.get());
                     }
-                    b->fb->add(j->sim->f32.get(), 0);
-                    j->sim->batch = b.get();
-                    b->members.push_back(j->sim.get());
                     std::lock_guard<std::mutex> lk(mu);
                     j->state = 1;
                     j->t_admit = mfdtd::wall_s();
@@ -1057,6 +1066,22 @@ struct mfdtd_server {
             // one round: every batch advances; the batches overlap on the device
             for (auto &kv : batches)
                 if (!kv.second->members.empty()) kv.second->fb->run(steps);
+            // the jobs marched alone, on their own streams, while the batches run
+            for (ServerJob *j : running) {
+                if (!j->solo || j->code) continue;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    if (j->cancel) continue;
+                }
+                mfdtd_sim *m = j->sim.get();
+                try {
+                    m->advance(std::min(steps, m->P.tsteps - m->t), false);
+                } catch (const Error &e) {
+                    j->code = e.code, j->err = e.what();
+                } catch (const std::exception &e) {
+                    j->code = MFDTD_ECUDA, j->err = e.what();
+                }
+            }
             for (auto &kv : batches) {
                 if (kv.second->members.empty()) continue;
                 try {
@@ -1087,10 +1112,11 @@ struct mfdtd_server {
                 try {
                     if (j->code) throw Error(j->code, j->err);
                     if (cancel) throw Error(MFDTD_ECANCELED, "canceled");
-                    mfdtd_batch *b = m->batch;
-                    b->fb->remove(m->f32.get());
-                    b->members.erase(std::find(b->members.begin(), b->members.end(), m));
-                    m->batch = nullptr;
+                    if (mfdtd_batch *b = m->batch) {
+                        b->fb->remove(m->f32.get());
+                        b->members.erase(std::find(b->members.begin(), b->members.end(), m));
+                        m->batch = nullptr;
+                    }
                     const int nd = (int)j->theta.size();
                     j->result.assign((size_t)m->P.nntf() * nd * 3, 0.0);
                     m->flush();
@@ -1189,6 +1215,7 @@ int mfdtd_server_submit(mfdtd_server *s, const mfdtd_problem *pb, int32_t ndir, 
             kind = uniform ? 1 : 2;
         }
         j->kind = kind + 3 * mfdtd::Fp32Sim::batch_class(P);  // and the batch class
+        j->solo = (int64_t)P.Nx * P.Ny * P.Nz >= kSoloCells;
         j->t_submit = mfdtd::wall_s();
         std::lock_guard<std::mutex> lk(s->mu);
         j->id = s->next_id++;

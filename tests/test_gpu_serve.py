@@ -8,6 +8,8 @@
 * The device memory of admitted jobs never exceeds the cap.
 * A job larger than the cap is refused at submission.
 * Queued and running jobs can be canceled.
+* A job of at least 2^25 cells marches alone, beside the batches, and its
+  result is the stand-alone run's bit for bit.
 """
 import time
 
@@ -61,6 +63,30 @@ def test_served_results_match_standalone_runs(built):
         assert np.max(np.abs(served - s32) / np.maximum(s32, 1e-300)) < 1e-5
         mask = s64 > s64.max() * 1e-3
         assert np.abs(10 * np.log10(served[mask] / s64[mask])).max() < 0.1
+
+
+def test_large_job_marches_alone_beside_the_batches(built):
+    th, ph = sweep.direction_grid(15.0)
+    rng = np.random.default_rng(21)
+    big = sweep.random_trail(rng, 120, (256, 256, 512))  # 2^25 cells: the solo lane
+    small = _jobs(2, 120, seed=22)
+    srv = E.Server(hbm_cap_bytes=16 * 10 ** 9, steps_per_round=40)
+    ids = [srv.submit(j.problem(E), th, ph) for j in [small[0], big, small[1]]]
+    got = {}
+    deadline = time.time() + 180
+    while len(got) < len(ids) and time.time() < deadline:
+        for jid in ids:
+            if jid not in got:
+                done, sig, _ = srv.poll(jid, 50)
+                if done:
+                    got[jid] = sig
+    srv.close()
+    assert len(got) == len(ids)
+    want = _standalone(big, E.FORM_FP32_FUSED, th, ph, method=1)
+    assert np.array_equal(got[ids[1]], want)
+    for jid, job in ((ids[0], small[0]), (ids[2], small[1])):
+        s32 = _standalone(job, E.FORM_FP32_FUSED, th, ph, method=1)[..., 0]
+        assert np.max(np.abs(got[jid][..., 0] - s32) / np.maximum(s32, 1e-300)) < 1e-5
 
 
 def test_admission_respects_the_device_cap(built):
