@@ -15,6 +15,10 @@ public:
     // Enqueue one time step; returns the number of kernels launched.  `ev`
     // (may be null) receives kernel_classes()+1 boundary events.
     int step(int t, bool record, void *stream, void *const *ev);
+    // Add the running-DFT steps still held in the ring to the FP64 sums (the
+    // caller does so at the end of every advance, before anything reads the
+    // sums); returns the number of kernels launched.
+    int drain_ntf(void *stream);
     static int kernel_classes();
     // Batch class of a problem's FP32 simulation: 1 when batches march it
     // with the fast path and the CPML slab march (CPML band on every axis,

@@ -245,16 +245,16 @@ __device__ __forceinline__ float obl_e_at(const Args &a, float s) {
     const float *e = a.inc[PAR][1];
     const float fl = floorf(s);
     const int n = (int)fl;
-    return e[n] + (s - fl) * (e[n + 1] - e[n]);
+    return __fadd_rn(e[n], __fmul_rn(__fsub_rn(s, fl), __fsub_rn(e[n + 1], e[n])));
 }
 template <int PAR>
 __device__ __forceinline__ float obl_h_new_at(const Args &a, float s) {
     const float *e = a.inc[PAR][1], *h = a.inc[PAR][2];
     const float fl = floorf(s);
     const int n = (int)fl;
-    const float h0 = a.c1h * h[n] - a.chl * (e[n + 1] - e[n]);
-    const float h1 = a.c1h * h[n + 1] - a.chl * (e[n + 2] - e[n + 1]);
-    return h0 + (s - fl) * (h1 - h0);
+    const float h0 = __fsub_rn(__fmul_rn(a.c1h, h[n]), __fmul_rn(a.chl, __fsub_rn(e[n + 1], e[n])));
+    const float h1 = __fsub_rn(__fmul_rn(a.c1h, h[n + 1]), __fmul_rn(a.chl, __fsub_rn(e[n + 2], e[n + 1])));
+    return __fadd_rn(h0, __fmul_rn(__fsub_rn(s, fl), __fsub_rn(h1, h0)));
 }
 // Crossing term along axis AX for component C of E (IS_E) or H at cell
 // (i,j,k), already scaled by c2/d_AX.  Along one axis a node type crosses the
@@ -290,15 +290,20 @@ __device__ __forceinline__ float obl_axis(const Args &a, int i, int j, int k) {
         P[d] = d == AX ? 2 * nb + st : 2 * idx[d] + tst;
         if (d != AX && (P[d] < 2 * b1[d] || P[d] > 2 * (b2[d] - 1))) return 0.f;
     }
-    const float sp = a.kr[0] * (0.5f * P[0]) + a.kr[1] * (0.5f * P[1]) + a.kr[2] * (0.5f * P[2]) + a.s0;
-    const float inc = IS_E ? a.kh[Q] * obl_h_new_at<PAR>(a, sp - 0.5f) : a.ke[Q] * obl_e_at<PAR>(a, sp);
+    // (explicitly rounded operations: the corrections come out the same bits
+    // in every kernel that inlines them, whatever the compiler contracts)
+    const float sp = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(a.kr[0], 0.5f * P[0]), __fmul_rn(a.kr[1], 0.5f * P[1])),
+                                         __fmul_rn(a.kr[2], 0.5f * P[2])),
+                               a.s0);
+    const float inc = IS_E ? __fmul_rn(a.kh[Q], obl_h_new_at<PAR>(a, __fsub_rn(sp, 0.5f)))
+                           : __fmul_rn(a.ke[Q], obl_e_at<PAR>(a, sp));
     const float cd = IS_E ? (AX == 0 ? a.cex : AX == 1 ? a.cey : a.cez)
                           : (AX == 0 ? a.chx : AX == 1 ? a.chy : a.chz);
-    return sgn * inc * cd;
+    return __fmul_rn(__fmul_rn(sgn, inc), cd);
 }
 template <int PAR, bool IS_E, int C>
 __device__ __forceinline__ float obl_corr(const Args &a, int i, int j, int k) {
-    return obl_axis<PAR, IS_E, C, (C + 1) % 3>(a, i, j, k) + obl_axis<PAR, IS_E, C, (C + 2) % 3>(a, i, j, k);
+    return __fadd_rn(obl_axis<PAR, IS_E, C, (C + 1) % 3>(a, i, j, k), obl_axis<PAR, IS_E, C, (C + 2) % 3>(a, i, j, k));
 }
 
 // Per-tile facts that are uniform across the CTA.
@@ -2041,13 +2046,14 @@ __global__ void k_batch_advance(int *job_t, const int *job_end, int njobs, int *
 }
 
 // ---------------------------------------------------------------------------
-// The running DFT on the Huygens surface as a kernel of its own (single
-// simulations): one thread per face cell of the six faces, reading the state
-// pass t wrote (set `cur`) -- E at the face node, H averaged over the face
-// node and the one behind it -- with the FP64 accumulation of the step
+// The running DFT on the Huygens surface after a batch member's pass
+// (k_batch_post): one thread per face cell of the six faces, reading the
+// state pass t wrote (set `cur`) -- E at the face node, H averaged over the
+// face node and the one behind it -- with the FP64 accumulation of the step
 // kernel's inline form (source/meteor-2.1.cpp:942-992, 1386-1438).  Taking
 // the sums' read-modify-writes out of the step kernel takes their latency off
-// the plane loop of the tiles that hold a face.
+// the plane loop of the tiles that hold a face.  (Single simulations batch
+// the steps in a ring: k_fp32_ntf, k_fp32_ntf_flush below.)
 // Face cells q0, q0 + dq, ... of the six faces (x faces, then y, then z).
 __device__ __forceinline__ void ntf_cells(const Args &a, int t, int cur, size_t q0, size_t dq) {
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, nb = a.ntfb, nf = a.nntf;
@@ -2096,8 +2102,141 @@ __device__ __forceinline__ void ntf_cells(const Args &a, int t, int cur, size_t 
         else { acc2v(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2v(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
     }
 }
-__global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a, int t, int cur) {
-    ntf_cells(a, t, cur, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+
+// The running DFT of a single simulation, in two kernels.  Each step,
+// k_fp32_ntf copies the face values the sums need from the state pass t
+// wrote (set `cur`) into slot `slot` of a ring of kNtfRing steps: per face
+// cell, the two tangential H components at the face node and at the node
+// behind it, and the two tangential E components (six floats, component-major
+// for coalescing).  Every kNtfRing steps, and at the end of every advance,
+// k_fp32_ntf_flush adds the ring's steps to the FP64 sums: per cell and
+// frequency it forms the same terms as ntf_cells -- H averaged over the two
+// nodes, E at the face node, signs per face, times the step's phase -- in
+// double-float arithmetic (value pairs hi + lo of FP32 numbers: the H average
+// kept exact by a two-sum, the phase split into two floats, each product
+// kept with its exact rounding error by an FMA), sums them over the ring's
+// steps with a compensated two-sum accumulation, and adds the result to the
+// FP64 sums once.  The terms carry about 44 bits, so the sums match the
+// per-step FP64 accumulation to about 1e-13 relative; the sums'
+// read-modify-writes and their FP64 arithmetic (a slow pipe on this part)
+// are paid once per ring instead of every step.
+constexpr int kNtfRing = 8;
+struct NtfFace {
+    int arr;     // first of the face's four sum arrays (Args::ntf)
+    float sgn;   // +1 on the front, top and left faces, -1 opposite
+    size_t c, s; // face node offset, offset to the node behind it
+    size_t r;    // cell index within the face (row of the sum arrays)
+};
+__device__ __forceinline__ NtfFace ntf_face(const Args &a, size_t q) {
+    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, nb = a.ntfb;
+    const size_t fx = (size_t)Ny * Nz, fy = (size_t)Nx * Nz, fz = (size_t)Nx * Ny;
+    const size_t sJ = a.Nzp, sI = (size_t)Ny * a.Nzp;
+    NtfFace f;
+    size_t r = q;
+    if (r < 2 * fx) {  // x faces: front (i = nb), back (i = Nx - nb); r = j * Nz + k
+        const bool back = r >= fx;
+        if (back) r -= fx;
+        const int i = back ? Nx - nb : nb, j = (int)((unsigned)r / (unsigned)Nz), k = (int)((unsigned)r % (unsigned)Nz);
+        f.c = i * sI + j * sJ + k;
+        f.s = sI;
+        f.arr = back ? 4 : 0;
+        f.sgn = back ? -1.f : 1.f;
+    } else if ((r -= 2 * fx) < 2 * fy) {  // y faces: top (j = Ny - nb), bottom (j = nb); r = i * Nz + k
+        const bool bottom = r >= fy;
+        if (bottom) r -= fy;
+        const int j = bottom ? nb : Ny - nb, i = (int)((unsigned)r / (unsigned)Nz), k = (int)((unsigned)r % (unsigned)Nz);
+        f.c = i * sI + j * sJ + k;
+        f.s = sJ;
+        f.arr = bottom ? 12 : 8;
+        f.sgn = bottom ? -1.f : 1.f;
+    } else {  // z faces: left (k = nb), right (k = Nz - nb); r = i * Ny + j
+        r -= 2 * fy;
+        const bool right = r >= fz;
+        if (right) r -= fz;
+        const int k = right ? Nz - nb : nb, i = (int)((unsigned)r / (unsigned)Ny), j = (int)((unsigned)r % (unsigned)Ny);
+        f.c = i * sI + j * sJ + k;
+        f.s = 1;
+        f.arr = right ? 20 : 16;
+        f.sgn = right ? -1.f : 1.f;
+    }
+    f.r = r;
+    return f;
+}
+__global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a, int cur, float *__restrict__ ring,
+                                                  int slot) {
+    const size_t fx = (size_t)a.Ny * a.Nz, fy = (size_t)a.Nx * a.Nz, fz = (size_t)a.Nx * a.Ny;
+    const size_t total = 2 * (fx + fy + fz);
+    float *const r = ring + (size_t)slot * 6 * total;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+        const NtfFace f = ntf_face(a, q);
+        // (Ha, Hb, Ea, Eb): x faces (Hz, Hy, Ey, Ez), y faces (Hz, Hx, Ex, Ez), z faces (Hy, Hx, Ex, Ey)
+        const int xf = f.arr < 8, yf = f.arr >= 8 && f.arr < 16;
+        const float *Ha = a.H[cur][xf || yf ? 2 : 1], *Hb = a.H[cur][xf ? 1 : 0];
+        const float *Ea = a.E[cur][xf ? 1 : 0], *Eb = a.E[cur][xf || yf ? 2 : 1];
+        r[q] = Ha[f.c];
+        r[total + q] = Ha[f.c - f.s];
+        r[2 * total + q] = Hb[f.c];
+        r[3 * total + q] = Hb[f.c - f.s];
+        r[4 * total + q] = Ea[f.c];
+        r[5 * total + q] = Eb[f.c];
+    }
+}
+// s + y = t + e exactly (Knuth's two-sum).
+__device__ __forceinline__ float two_sum(float s, float y, float &e) {
+    const float t = __fadd_rn(s, y), bp = __fsub_rn(t, s);
+    e = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(y, bp));
+    return t;
+}
+// Adds (vh + vl) * (ph + pl) to the compensated sum (s, c); the product's
+// high part is exact up to its rounding error, which an FMA recovers.
+__device__ __forceinline__ void df_mac(float &s, float &c, float vh, float vl, float ph, float pl) {
+    const float p = __fmul_rn(vh, ph);
+    const float pe = __fmaf_rn(vh, ph, -p);
+    float e;
+    s = two_sum(s, p, e);
+    c += e + (pe + (vh * pl + vl * ph));
+}
+// Ring slots 0 .. count-1 hold steps t0 .. t0 + count - 1.  The terms follow
+// ntf_cells: arrays arr+2, arr+3 take (sgn * H_a, -sgn * H_b) and arrays
+// arr, arr+1 take (-sgn * E_b, sgn * E_a), each times (cos, sin) of the
+// step's phase; phase4 holds per (step, frequency) the phase's FP32 high
+// parts and the FP32 remainders.
+__global__ void __launch_bounds__(256) k_fp32_ntf_flush(const __grid_constant__ Args a, const float *__restrict__ ring,
+                                                        const float4 *__restrict__ phase4, int t0, int count) {
+    const int nf = a.nntf;
+    const size_t fx = (size_t)a.Ny * a.Nz, fy = (size_t)a.Nx * a.Nz, fz = (size_t)a.Nx * a.Ny;
+    const size_t total = 2 * (fx + fy + fz), slot = 6 * total;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+        const NtfFace f = ntf_face(a, q);
+        const size_t base = f.r * 2 * (size_t)nf;
+        for (int m = 0; m < nf; m++) {
+            float s[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, c[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+            for (int u = 0; u < count; u++) {
+                const float *r = ring + u * slot + q;
+                // the H averages as exact pairs: 0.5 (x + y) = 0.5 t + 0.5 e
+                float ea_, eb_;
+                const float ta = two_sum(r[0], r[total], ea_), tb = two_sum(r[2 * total], r[3 * total], eb_);
+                const float g = f.sgn;
+                const float vh[4] = {g * 0.5f * ta, -g * 0.5f * tb, -g * r[5 * total], g * r[4 * total]};
+                const float vl[4] = {g * 0.5f * ea_, -g * 0.5f * eb_, 0.f, 0.f};
+                const float4 p = phase4[(size_t)(t0 + u) * nf + m];
+#pragma unroll
+                for (int w = 0; w < 4; w++) {
+                    df_mac(s[2 * w], c[2 * w], vh[w], vl[w], p.x, p.z);
+                    df_mac(s[2 * w + 1], c[2 * w + 1], vh[w], vl[w], p.y, p.w);
+                }
+            }
+            const int arr[4] = {f.arr + 2, f.arr + 3, f.arr, f.arr + 1};
+#pragma unroll
+            for (int w = 0; w < 4; w++) {
+                double2 *d = (double2 *)(a.ntf[arr[w]] + base) + m;
+                double2 x = *d;
+                x.x += (double)s[2 * w] + (double)c[2 * w];
+                x.y += (double)s[2 * w + 1] + (double)c[2 * w + 1];
+                *d = x;
+            }
+        }
+    }
 }
 
 // The oblique TF/SF corrections as a pass of their own (single simulations
@@ -2112,6 +2251,76 @@ __global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a
 // The line values are the ones of the pass's start (set PAR; the pass wrote
 // the next line into the other set).  On record steps the slice entries of
 // band cells get the same increments.
+// One cell of the TF/SF band: its H correction dH, and its E correction plus
+// the curl of the dH of the cell and of its -x, -y, -z neighbours, added to
+// the new state (and to the slices on record steps).  Bit AX of MASK says
+// that crossing terms along axis AX can be nonzero for the cell and those
+// neighbours; the terms of the other axes are exactly zero there and are not
+// evaluated (obl_corr_m), which leaves the sums unchanged.
+template <int PAR, bool IS_E, int C, int MASK>
+__device__ __forceinline__ float obl_corr_m(const Args &a, int i, int j, int k) {
+    constexpr int A1 = (C + 1) % 3, A2 = (C + 2) % 3;
+    float v1 = 0.f, v2 = 0.f;
+    if constexpr ((MASK >> A1) & 1) v1 = obl_axis<PAR, IS_E, C, A1>(a, i, j, k);
+    if constexpr ((MASK >> A2) & 1) v2 = obl_axis<PAR, IS_E, C, A2>(a, i, j, k);
+    return __fadd_rn(v1, v2);
+}
+template <int PAR, int MASK>
+__device__ __forceinline__ void tfsf_cell(const Args &a, int record, int i, int j, int k, size_t plane) {
+    const float hx = obl_corr_m<PAR, false, 0, MASK>(a, i, j, k);
+    const float hy = obl_corr_m<PAR, false, 1, MASK>(a, i, j, k);
+    const float hz = obl_corr_m<PAR, false, 2, MASK>(a, i, j, k);
+    // E's own correction plus the E update's curl of the neighbouring dH
+    // (explicitly rounded: see obl_axis)
+    auto curl = [](float c1, float d1, float c2, float d2, float own) {
+        return __fadd_rn(__fsub_rn(__fmul_rn(c1, d1), __fmul_rn(c2, d2)), own);
+    };
+    const float ex = curl(a.cey, __fsub_rn(hz, obl_corr_m<PAR, false, 2, MASK>(a, i, j - 1, k)), a.cez,
+                          __fsub_rn(hy, obl_corr_m<PAR, false, 1, MASK>(a, i, j, k - 1)),
+                          obl_corr_m<PAR, true, 0, MASK>(a, i, j, k));
+    const float ey = curl(a.cez, __fsub_rn(hx, obl_corr_m<PAR, false, 0, MASK>(a, i, j, k - 1)), a.cex,
+                          __fsub_rn(hz, obl_corr_m<PAR, false, 2, MASK>(a, i - 1, j, k)),
+                          obl_corr_m<PAR, true, 1, MASK>(a, i, j, k));
+    const float ez = curl(a.cex, __fsub_rn(hy, obl_corr_m<PAR, false, 1, MASK>(a, i - 1, j, k)), a.cey,
+                          __fsub_rn(hx, obl_corr_m<PAR, false, 0, MASK>(a, i, j - 1, k)),
+                          obl_corr_m<PAR, true, 2, MASK>(a, i, j, k));
+    const size_t c = (size_t)i * plane + (size_t)j * a.Nzp + k;
+    if (hx != 0.f) a.H[PAR ^ 1][0][c] += hx;
+    if (hy != 0.f) a.H[PAR ^ 1][1][c] += hy;
+    if (hz != 0.f) a.H[PAR ^ 1][2][c] += hz;
+    if (ex != 0.f) a.E[PAR ^ 1][0][c] += ex;
+    if (ey != 0.f) a.E[PAR ^ 1][1][c] += ey;
+    if (ez != 0.f) a.E[PAR ^ 1][2][c] += ez;
+    if (record) {  // slices written by the pass (source/meteor-2.1.cpp:996-1013, 1322-1340)
+        const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
+        const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
+        if (k == a.ssz) {
+            a.slE[oz + (size_t)i * Ny + j] += ey;
+            a.slE[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] += ez;
+            if (j < Ny - 1) {
+                a.slH[oz + (size_t)i * Ny + j] += hy;
+                a.slH[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] += hz;
+            }
+        }
+        if (j == a.ssy) {
+            a.slE[oy + (size_t)i * Nz + k] += ey;
+            a.slE[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] += ez;
+            if (k < Nz - 1) {
+                a.slH[oy + (size_t)i * Nz + k] += hy;
+                a.slH[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] += hz;
+            }
+        }
+        if (i == a.ssx) {
+            a.slE[ox + (size_t)j * Nz + k] += ey;
+            a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] += ez;
+            if (j < Ny - 1 && k < Nz - 1) {
+                a.slH[ox + (size_t)j * Nz + k] += hy;
+                a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] += hz;
+            }
+        }
+    }
+}
+
 template <int PAR>
 __device__ __forceinline__ void tfsf_band(const Args &a, int record, size_t q0, size_t dq) {
     const int bx1 = a.bx1, bx2 = a.bx2, by1 = a.by1, by2 = a.by2, bz1 = a.bz1, bz2 = a.bz2;
@@ -2141,48 +2350,21 @@ __device__ __forceinline__ void tfsf_band(const Args &a, int record, size_t q0, 
             i = bx1 + 1 + (int)(r / uJr2);
             j = by1 + 1 + (int)(r % uJr2);
         }
-        const float hx = obl_corr<PAR, false, 0>(a, i, j, k), hy = obl_corr<PAR, false, 1>(a, i, j, k),
-                    hz = obl_corr<PAR, false, 2>(a, i, j, k);
-        const float ex = a.cey * (hz - obl_corr<PAR, false, 2>(a, i, j - 1, k)) -
-                         a.cez * (hy - obl_corr<PAR, false, 1>(a, i, j, k - 1)) + obl_corr<PAR, true, 0>(a, i, j, k);
-        const float ey = a.cez * (hx - obl_corr<PAR, false, 0>(a, i, j, k - 1)) -
-                         a.cex * (hz - obl_corr<PAR, false, 2>(a, i - 1, j, k)) + obl_corr<PAR, true, 1>(a, i, j, k);
-        const float ez = a.cex * (hy - obl_corr<PAR, false, 1>(a, i - 1, j, k)) -
-                         a.cey * (hx - obl_corr<PAR, false, 0>(a, i, j - 1, k)) + obl_corr<PAR, true, 2>(a, i, j, k);
-        const size_t c = (size_t)i * plane + (size_t)j * a.Nzp + k;
-        if (hx != 0.f) a.H[PAR ^ 1][0][c] += hx;
-        if (hy != 0.f) a.H[PAR ^ 1][1][c] += hy;
-        if (hz != 0.f) a.H[PAR ^ 1][2][c] += hz;
-        if (ex != 0.f) a.E[PAR ^ 1][0][c] += ex;
-        if (ey != 0.f) a.E[PAR ^ 1][1][c] += ey;
-        if (ez != 0.f) a.E[PAR ^ 1][2][c] += ez;
-        if (record) {  // slices written by the pass (source/meteor-2.1.cpp:996-1013, 1322-1340)
-            const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz;
-            const size_t oz = 0, oy = 2 * (size_t)Nx * Ny, ox = oy + 2 * (size_t)Nx * Nz;
-            if (k == a.ssz) {
-                a.slE[oz + (size_t)i * Ny + j] += ey;
-                a.slE[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] += ez;
-                if (j < Ny - 1) {
-                    a.slH[oz + (size_t)i * Ny + j] += hy;
-                    a.slH[oz + (size_t)Nx * Ny + (size_t)i * Ny + j] += hz;
-                }
-            }
-            if (j == a.ssy) {
-                a.slE[oy + (size_t)i * Nz + k] += ey;
-                a.slE[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] += ez;
-                if (k < Nz - 1) {
-                    a.slH[oy + (size_t)i * Nz + k] += hy;
-                    a.slH[oy + (size_t)Nx * Nz + (size_t)i * Nz + k] += hz;
-                }
-            }
-            if (i == a.ssx) {
-                a.slE[ox + (size_t)j * Nz + k] += ey;
-                a.slE[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] += ez;
-                if (j < Ny - 1 && k < Nz - 1) {
-                    a.slH[ox + (size_t)j * Nz + k] += hy;
-                    a.slH[ox + (size_t)Ny * Nz + (size_t)j * Nz + k] += hz;
-                }
-            }
+        // Crossing terms along an axis need the cell's (or its -1
+        // neighbour's) index on that axis in {b1 - 1, b1, b2 - 1, b2}.  The x
+        // layers span j, k over [b1 - 1, b2], the y layers k over
+        // [bz1 - 1, bz2] with i inside, the z layers i and j inside.
+        if (q < nX) {
+            const bool yedge = j <= by1 || j >= by2 - 1, zedge = k <= bz1 || k >= bz2 - 1;
+            if (yedge && zedge) tfsf_cell<PAR, 7>(a, record, i, j, k, plane);
+            else if (yedge) tfsf_cell<PAR, 3>(a, record, i, j, k, plane);
+            else if (zedge) tfsf_cell<PAR, 5>(a, record, i, j, k, plane);
+            else tfsf_cell<PAR, 1>(a, record, i, j, k, plane);
+        } else if (q < nX + nY) {
+            if (k <= bz1 || k >= bz2 - 1) tfsf_cell<PAR, 6>(a, record, i, j, k, plane);
+            else tfsf_cell<PAR, 2>(a, record, i, j, k, plane);
+        } else {
+            tfsf_cell<PAR, 4>(a, record, i, j, k, plane);
         }
     }
 }
@@ -2560,6 +2742,13 @@ struct Fp32Sim::Impl {
     bool slab_ok = false;
     const int4 *slab_items = nullptr;
     int n_slab_items = 0;
+    // Running DFT (single simulations): the ring of face values (allocated at
+    // the first step: batch members never use it), the FP32 phase table, and
+    // the ring's first step and fill.
+    float *ntf_ring = nullptr;
+    const float4 *phase4 = nullptr;
+    size_t nface = 0;
+    int ring_t0 = 0, ring_fill = 0;
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // In a batch of class 1 (Fp32Sim::batch_class): the tiles whose cells are
@@ -2618,8 +2807,12 @@ int64_t Fp32Sim::footprint(const Problem &P) {
     // Lee-Kalluri table: a matrix pair per cell (padded layout) when nu varies
     // along all three axes
     const int64_t lkt = (P.doB0 && P.lk_mode == LK_PER_CELL) ? cells * 4 * kLkStride : 4 * (int64_t)P.lk.size();
+    // running-DFT ring of a single simulation and the split phase table
+    const int64_t ring = P.nntf() > 0 ? 4 * (kNtfRing * 6 * 2 * ((int64_t)P.Ny * P.Nz + (int64_t)P.Nx * P.Nz +
+                                                                 (int64_t)P.Nx * P.Ny) + 2 * (int64_t)P.tsteps * nf2)
+                                      : 0;
     return cells * 4 * 15 + maps + psi * 4 * 3 + 8 * ntf + 8 * (int64_t)P.tsteps * (nf2 + 6 * P.nprobes() + 2) + band +
-           ptab + slab + lkt;
+           ptab + slab + lkt + ring;
 }
 
 void Fp32Sim::init(const Problem &P, void *stream) {
@@ -2782,6 +2975,17 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         a.src = m.upload(src, s);
     }
     a.phase = m.upload(P.phase, s);
+    if (P.nntf() > 0) {
+        m.nface = 2 * ((size_t)P.Ny * P.Nz + (size_t)P.Nx * P.Nz + (size_t)P.Nx * P.Ny);
+        // per (step, frequency): the phase's FP32 high parts and remainders
+        std::vector<float4> pf(P.phase.size() / 2);
+        for (size_t q = 0; q < pf.size(); q++) {
+            const double c = P.phase[2 * q], sn = P.phase[2 * q + 1];
+            const float ch = (float)c, sh = (float)sn;
+            pf[q] = make_float4(ch, sh, (float)(c - (double)ch), (float)(sn - (double)sh));
+        }
+        m.phase4 = m.upload(pf, s);
+    }
     a.xc = m.upload(P.x, s); a.yc = m.upload(P.y, s); a.zc = m.upload(P.z, s);
     const size_t nf2 = 2 * (size_t)P.nntf();
     const size_t fb = (size_t)P.Ny * P.Nz * nf2, tb = (size_t)P.Nx * P.Nz * nf2, lr = (size_t)P.Nx * P.Ny * nf2;
@@ -3114,12 +3318,26 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     }
     if (ev) cudaEventRecord((cudaEvent_t)ev[2], s);
     if (!m.a.ntf_inline && m.a.nntf > 0) {
-        k_fp32_ntf<<<m.sms * 8, 256, 0, s>>>(m.a, t, m_cur_ ^ 1);
+        if (!m.ntf_ring) {
+            m.ntf_ring = m.alloc<float>((size_t)kNtfRing * 6 * m.nface, s);
+            bytes_ = m.bytes;
+        }
+        if (m.ring_fill == 0) m.ring_t0 = t;
+        k_fp32_ntf<<<m.sms * 8, 256, 0, s>>>(m.a, m_cur_ ^ 1, m.ntf_ring, m.ring_fill);
         launches++;
+        if (++m.ring_fill == kNtfRing) launches += drain_ntf(stream);
     }
     if (ev) cudaEventRecord((cudaEvent_t)ev[3], s);
     m_cur_ ^= 1;
     return launches;
+}
+
+int Fp32Sim::drain_ntf(void *stream) {
+    Impl &m = *impl_;
+    if (m.ring_fill == 0) return 0;
+    k_fp32_ntf_flush<<<m.sms * 8, 256, 0, (cudaStream_t)stream>>>(m.a, m.ntf_ring, m.phase4, m.ring_t0, m.ring_fill);
+    m.ring_fill = 0;
+    return 1;
 }
 
 void Fp32Sim::check(void *stream) {

@@ -418,6 +418,7 @@ struct mfdtd_sim {
             }
             if (opts.guard_period > 0 && (t + 1) % opts.guard_period == 0) guard();
         }
+        if (f32) launches += f32->drain_ntf(stream);  // the DFT sums are whole after every advance
         mfdtd::ck(cudaEventRecord(ev1, stream), "cudaEventRecord");
         mfdtd::ck(cudaGetLastError(), "kernel launch");
         last_launches = launches;
