@@ -142,6 +142,10 @@ struct Args {
     const int2 *band_units;
     int n_band_units;
     double *ntf[24];
+    // Running-DFT ring (k_fp32_ntf's layout) and split phase table
+    // (k_fp32_ntf_flush); a batch member's are set when it joins its batch.
+    float *ntf_ring;
+    const float4 *phase4;
     double *probe;       // [6][tsteps][nprobes]
     const int *probe_ijk;
     float *slE, *slH;
@@ -1021,21 +1025,6 @@ __device__ __forceinline__ void acc2(double *A, double *B, size_t base, double v
 // per frequency.  The (sin, cos) pairs of the sums and of the phase table are
 // adjacent and 16-byte aligned (base and the phase row start are even), so
 // each pair moves as one double2.
-__device__ __forceinline__ void acc2v(double *A, double *B, size_t base, double va, double vb,
-                                     const double *ph, int nf) {
-    double2 *a2 = (double2 *)(A + base), *b2 = (double2 *)(B + base);
-    const double2 *p2 = (const double2 *)ph;
-    for (int m = 0; m < nf; m++) {
-        const double2 p = p2[m];
-        double2 x = a2[m], y = b2[m];
-        x.x += va * p.x;
-        x.y += va * p.y;
-        y.x += vb * p.x;
-        y.y += vb * p.y;
-        a2[m] = x;
-        b2[m] = y;
-    }
-}
 
 // Everything a marching CTA keeps between planes.
 struct MarchCtx {
@@ -2046,72 +2035,18 @@ __global__ void k_batch_advance(int *job_t, const int *job_end, int njobs, int *
 }
 
 // ---------------------------------------------------------------------------
-// The running DFT on the Huygens surface after a batch member's pass
-// (k_batch_post): one thread per face cell of the six faces, reading the
-// state pass t wrote (set `cur`) -- E at the face node, H averaged over the
-// face node and the one behind it -- with the FP64 accumulation of the step
-// kernel's inline form (source/meteor-2.1.cpp:942-992, 1386-1438).  Taking
-// the sums' read-modify-writes out of the step kernel takes their latency off
-// the plane loop of the tiles that hold a face.  (Single simulations batch
-// the steps in a ring: k_fp32_ntf, k_fp32_ntf_flush below.)
-// Face cells q0, q0 + dq, ... of the six faces (x faces, then y, then z).
-__device__ __forceinline__ void ntf_cells(const Args &a, int t, int cur, size_t q0, size_t dq) {
-    const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, nb = a.ntfb, nf = a.nntf;
-    const size_t fx = (size_t)Ny * Nz, fy = (size_t)Nx * Nz, fz = (size_t)Nx * Ny;
-    const size_t total = 2 * (fx + fy + fz), n2 = 2 * (size_t)nf;
-    const size_t sJ = a.Nzp, sI = (size_t)Ny * a.Nzp;
-    const double *ph = a.phase + (size_t)t * nf * 2;
-    const float *E0 = a.E[cur][0], *E1 = a.E[cur][1], *E2 = a.E[cur][2];
-    const float *H0 = a.H[cur][0], *H1 = a.H[cur][1], *H2 = a.H[cur][2];
-    for (size_t q = q0; q < total; q += dq) {
-        size_t r = q;
-        if (r < 2 * fx) {  // x faces: front (i = nb), back (i = Nx - nb); r = j * Nz + k
-            const bool back = r >= fx;
-            if (back) r -= fx;
-            const int i = back ? Nx - nb : nb, j = (int)((unsigned)r / (unsigned)Nz),
-                      k = (int)((unsigned)r % (unsigned)Nz);
-            const size_t c = i * sI + j * sJ + k, base = r * n2;
-            const double hz = 0.5 * ((double)H2[c] + H2[c - sI]), hy = 0.5 * ((double)H1[c] + H1[c - sI]);
-            const float ey = E1[c], ez = E2[c];
-            if (!back) { acc2v(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2v(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
-            else { acc2v(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2v(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
-            continue;
-        }
-        r -= 2 * fx;
-        if (r < 2 * fy) {  // y faces: top (j = Ny - nb), bottom (j = nb); r = i * Nz + k
-            const bool bottom = r >= fy;
-            if (bottom) r -= fy;
-            const int j = bottom ? nb : Ny - nb, i = (int)((unsigned)r / (unsigned)Nz),
-                      k = (int)((unsigned)r % (unsigned)Nz);
-            const size_t c = i * sI + j * sJ + k, base = r * n2;
-            const double hz = 0.5 * ((double)H2[c] + H2[c - sJ]), hx = 0.5 * ((double)H0[c] + H0[c - sJ]);
-            const float ex = E0[c], ez = E2[c];
-            if (!bottom) { acc2v(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2v(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
-            else { acc2v(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2v(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
-            continue;
-        }
-        r -= 2 * fy;  // z faces: left (k = nb), right (k = Nz - nb); r = i * Ny + j
-        const bool right = r >= fz;
-        if (right) r -= fz;
-        const int k = right ? Nz - nb : nb, i = (int)((unsigned)r / (unsigned)Ny),
-                  j = (int)((unsigned)r % (unsigned)Ny);
-        const size_t c = i * sI + j * sJ + k, base = r * n2;
-        const double hy = 0.5 * ((double)H1[c] + H1[c - 1]), hx = 0.5 * ((double)H0[c] + H0[c - 1]);
-        const float ex = E0[c], ey = E1[c];
-        if (!right) { acc2v(a.ntf[18], a.ntf[19], base, hy, -hx, ph, nf); acc2v(a.ntf[16], a.ntf[17], base, -(double)ey, ex, ph, nf); }
-        else { acc2v(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2v(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
-    }
-}
 
-// The running DFT of a single simulation, in two kernels.  Each step,
-// k_fp32_ntf copies the face values the sums need from the state pass t
+// The running DFT on the Huygens surface (source/meteor-2.1.cpp:942-992,
+// 1386-1438), in two kernels.  Each step, k_fp32_ntf (or, in a batch,
+// k_batch_post) copies the face values the sums need from the state pass t
 // wrote (set `cur`) into slot `slot` of a ring of kNtfRing steps: per face
 // cell, the two tangential H components at the face node and at the node
 // behind it, and the two tangential E components (six floats, component-major
-// for coalescing).  Every kNtfRing steps, and at the end of every advance,
-// k_fp32_ntf_flush adds the ring's steps to the FP64 sums: per cell and
-// frequency it forms the same terms as ntf_cells -- H averaged over the two
-// nodes, E at the face node, signs per face, times the step's phase -- in
+// for coalescing).  Every kNtfRing steps, at the end of every advance, and at
+// a batch member's last step, k_fp32_ntf_flush (k_batch_flush) adds the
+// ring's steps to the FP64 sums: per cell and frequency it forms the
+// reference's terms -- H averaged over the two nodes, E at the face node,
+// signs per face, times the step's phase -- in
 // double-float arithmetic (value pairs hi + lo of FP32 numbers: the H average
 // kept exact by a two-sum, the phase split into two floats, each product
 // kept with its exact rounding error by an FMA), sums them over the ring's
@@ -2162,12 +2097,12 @@ __device__ __forceinline__ NtfFace ntf_face(const Args &a, size_t q) {
     f.r = r;
     return f;
 }
-__global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a, int cur, float *__restrict__ ring,
-                                                  int slot) {
+__device__ __forceinline__ void ntf_stash(const Args &a, int cur, float *__restrict__ ring, int slot, size_t q0,
+                                          size_t dq) {
     const size_t fx = (size_t)a.Ny * a.Nz, fy = (size_t)a.Nx * a.Nz, fz = (size_t)a.Nx * a.Ny;
     const size_t total = 2 * (fx + fy + fz);
     float *const r = ring + (size_t)slot * 6 * total;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    for (size_t q = q0; q < total; q += dq) {
         const NtfFace f = ntf_face(a, q);
         // (Ha, Hb, Ea, Eb): x faces (Hz, Hy, Ey, Ez), y faces (Hz, Hx, Ex, Ez), z faces (Hy, Hx, Ex, Ey)
         const int xf = f.arr < 8, yf = f.arr >= 8 && f.arr < 16;
@@ -2180,6 +2115,10 @@ __global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a
         r[4 * total + q] = Ea[f.c];
         r[5 * total + q] = Eb[f.c];
     }
+}
+__global__ void __launch_bounds__(256) k_fp32_ntf(const __grid_constant__ Args a, int cur, float *__restrict__ ring,
+                                                  int slot) {
+    ntf_stash(a, cur, ring, slot, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
 }
 // s + y = t + e exactly (Knuth's two-sum).
 __device__ __forceinline__ float two_sum(float s, float y, float &e) {
@@ -2196,17 +2135,18 @@ __device__ __forceinline__ void df_mac(float &s, float &c, float vh, float vl, f
     s = two_sum(s, p, e);
     c += e + (pe + (vh * pl + vl * ph));
 }
-// Ring slots 0 .. count-1 hold steps t0 .. t0 + count - 1.  The terms follow
-// ntf_cells: arrays arr+2, arr+3 take (sgn * H_a, -sgn * H_b) and arrays
+// Ring slots 0 .. count-1 hold steps t0 .. t0 + count - 1.  The terms:
+// arrays arr+2, arr+3 take (sgn * H_a, -sgn * H_b) and arrays
 // arr, arr+1 take (-sgn * E_b, sgn * E_a), each times (cos, sin) of the
 // step's phase; phase4 holds per (step, frequency) the phase's FP32 high
 // parts and the FP32 remainders.
-__global__ void __launch_bounds__(256) k_fp32_ntf_flush(const __grid_constant__ Args a, const float *__restrict__ ring,
-                                                        const float4 *__restrict__ phase4, int t0, int count) {
+__device__ __forceinline__ void ntf_flush_cells(const Args &a, const float *__restrict__ ring,
+                                                const float4 *__restrict__ phase4, int t0, int count, size_t q0,
+                                                size_t dq) {
     const int nf = a.nntf;
     const size_t fx = (size_t)a.Ny * a.Nz, fy = (size_t)a.Nx * a.Nz, fz = (size_t)a.Nx * a.Ny;
     const size_t total = 2 * (fx + fy + fz), slot = 6 * total;
-    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < total; q += (size_t)gridDim.x * blockDim.x) {
+    for (size_t q = q0; q < total; q += dq) {
         const NtfFace f = ntf_face(a, q);
         const size_t base = f.r * 2 * (size_t)nf;
         for (int m = 0; m < nf; m++) {
@@ -2237,6 +2177,11 @@ __global__ void __launch_bounds__(256) k_fp32_ntf_flush(const __grid_constant__ 
             }
         }
     }
+}
+__global__ void __launch_bounds__(256) k_fp32_ntf_flush(const __grid_constant__ Args a, const float *__restrict__ ring,
+                                                        const float4 *__restrict__ phase4, int t0, int count) {
+    ntf_flush_cells(a, ring, phase4, t0, count, (size_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (size_t)gridDim.x * blockDim.x);
 }
 
 // The oblique TF/SF corrections as a pass of their own (single simulations
@@ -2384,7 +2329,21 @@ __global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_
     const Args &a = c_jobs[q];
     const size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, dq = (size_t)gridDim.x * blockDim.x;
     if (a.oblique && !a.obl_inline) tfsf_band<PAR>(a, 0, q0, dq);
-    if (!a.ntf_inline && a.nntf > 0) ntf_cells(a, t, PAR ^ 1, q0, dq);
+    if (!a.ntf_inline && a.nntf > 0 && a.ntf_ring) ntf_stash(a, PAR ^ 1, a.ntf_ring, t % kNtfRing, q0, dq);
+}
+// After k_batch_post: a member whose tick filled its DFT ring (step t with
+// t % kNtfRing the last slot) or reached its last step adds the ring's steps
+// to its FP64 sums, as a single simulation's k_fp32_ntf_flush does.
+__global__ void __launch_bounds__(256) k_batch_flush(const int *__restrict__ job_t, const int *__restrict__ job_end) {
+    const int q = blockIdx.y;
+    const int t = job_t[q], end = job_end[q];
+    if (t >= end) return;
+    const Args &a = c_jobs[q];
+    if (a.ntf_inline || a.nntf <= 0 || !a.ntf_ring) return;
+    const int u = t % kNtfRing;
+    if (u != kNtfRing - 1 && t + 1 != end) return;
+    ntf_flush_cells(a, a.ntf_ring, a.phase4, t - u, u + 1, (size_t)blockIdx.x * blockDim.x + threadIdx.x,
+                    (size_t)gridDim.x * blockDim.x);
 }
 
 // ---------------------------------------------------------------------------
@@ -2985,6 +2944,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
             pf[q] = make_float4(ch, sh, (float)(c - (double)ch), (float)(sn - (double)sh));
         }
         m.phase4 = m.upload(pf, s);
+        a.phase4 = m.phase4;
     }
     a.xc = m.upload(P.x, s); a.yc = m.upload(P.y, s); a.zc = m.upload(P.z, s);
     const size_t nf2 = 2 * (size_t)P.nntf();
@@ -3590,6 +3550,19 @@ int Fp32Batch::add(Fp32Sim *sim, int t0) {
     // The state is all zeros in both sets, so the simulation can take the
     // parity of the current tick.
     sim->m_cur_ = (int)(b.tick & 1);
+    if (!m.a.ntf_inline && m.a.nntf > 0 && !m.ntf_ring) {  // the running-DFT ring (k_batch_post)
+        try {
+            m.ntf_ring = m.alloc<float>((size_t)kNtfRing * 6 * m.nface, b.stream);
+        } catch (...) {
+            release_slot(b.device, s);
+            throw;
+        }
+        sim->bytes_ = m.bytes;
+    }
+    m.ring_fill = 0;
+    // (in the simulation's own Args, so that every later copy into the
+    // constant bank -- apply_chunk -- carries it)
+    m.a.ntf_ring = m.ntf_ring;
     const Args ba = batch_args(m.a, 0);
     ck(cudaMemcpyToSymbolAsync(c_jobs, &ba, sizeof(Args), sizeof(Args) * s, cudaMemcpyHostToDevice, b.stream),
        "cudaMemcpyToSymbol");
@@ -3618,6 +3591,16 @@ void Fp32Batch::remove(Fp32Sim *sim) {
             ck(cudaStreamSynchronize(b.stream), "batch");
             int zero = 0;
             ck(cudaMemcpy(b.d_end + q, &zero, 4, cudaMemcpyHostToDevice), "H2D");
+            // DFT steps still in the ring (the member leaves before its last
+            // step, off a ring boundary) go to the sums now
+            Fp32Sim::Impl &m = *sim->impl_;
+            const int done = b.host_t[q], pend = done % kNtfRing;
+            if (m.ntf_ring && pend && done < b.tsteps[q]) {
+                m.ring_t0 = done - pend;
+                m.ring_fill = pend;
+                sim->drain_ntf(b.stream);
+                ck(cudaStreamSynchronize(b.stream), "batch");
+            }
             b.slot[q] = nullptr;
             release_slot(b.device, q);
             b.dirty = true;
@@ -3733,6 +3716,7 @@ static void launch_tick(Fp32Batch::Impl &b, int par) {
     const dim3 pgrid(b.sms, kMaxBatch);
     if (par == 0) k_batch_post<0><<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);
     else k_batch_post<1><<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);
+    k_batch_flush<<<pgrid, 256, 0, b.stream>>>(b.d_t, b.d_end);
     k_batch_advance<<<1, kMaxBatch, 0, b.stream>>>(b.d_t, b.d_end, kMaxBatch, b.d_next);
 }
 
