@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 
@@ -2723,12 +2724,16 @@ struct Fp32Sim::Impl {
     std::vector<int> pairs32, edgew;
 
 
+    // Device memory comes from the device's stream-ordered pool (see
+    // configure_pool), zeroed on the simulation's stream.
     template <class T> T *alloc(size_t n, cudaStream_t s) {
         void *p = nullptr;
         size_t b = std::max<size_t>(n, 1) * sizeof(T);
-        ck(cudaMalloc(&p, b), "cudaMalloc");
+        ck(cudaMallocAsync(&p, b, s), "cudaMallocAsync");
         allocs.push_back(p);
         bytes += (int64_t)b;
+        // TMA and the 16-byte vector accesses want at least 256-byte alignment
+        if (reinterpret_cast<uintptr_t>(p) % 256) throw Error(MFDTD_ECUDA, "pool allocation not 256-byte aligned");
         ck(cudaMemsetAsync(p, 0, b, s), "cudaMemset");
         return (T *)p;
     }
@@ -2744,8 +2749,10 @@ struct Fp32Sim::Impl {
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
-
-        for (void *p : allocs) cudaFree(p);
+        // No kernel may still use the memory when it goes back to the pool
+        // (as cudaFree would ensure); the frees then take no unmapping.
+        if (!allocs.empty()) cudaDeviceSynchronize();
+        for (void *p : allocs) cudaFreeAsync(p, 0);
     }
 };
 
@@ -2774,9 +2781,33 @@ int64_t Fp32Sim::footprint(const Problem &P) {
            ptab + slab + lkt + ring;
 }
 
+// The FP32 form takes its device memory from the device's default
+// stream-ordered pool, set once per device to keep up to a quarter of the
+// device's memory cached after frees: a simulation created after another one
+// ended (a server's next job, a sweep's next trail, a second run in the same
+// process) reuses that memory without new mappings, and freeing one takes no
+// unmapping.  Memory beyond that goes back to the system at the next
+// synchronisation.
+static void configure_pool() {
+    static std::mutex mu;
+    static std::vector<int> done;
+    int dev = 0;
+    ck(cudaGetDevice(&dev), "cudaGetDevice");
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), dev) != done.end()) return;
+    cudaMemPool_t pool;
+    ck(cudaDeviceGetDefaultMemPool(&pool, dev), "cudaDeviceGetDefaultMemPool");
+    size_t free_b = 0, total_b = 0;
+    ck(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    uint64_t keep = total_b / 4;
+    ck(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep), "cudaMemPoolSetAttribute");
+    done.push_back(dev);
+}
+
 void Fp32Sim::init(const Problem &P, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (P.L > kMaxPml) throw Error(MFDTD_EINVAL, "CPML too thick");
+    configure_pool();
     impl_ = new Impl();
     Impl &m = *impl_;
     Args &a = m.a;

@@ -401,7 +401,9 @@ struct mfdtd_sim {
             const int ps = t - t_begin;
             void *const *ev = ps < prof_steps ? (void *const *)&kev[(size_t)(nk + 1) * ps] : nullptr;
             if (form == MFDTD_FORM_FP64_PLAIN) launches += mfdtd::plain_launch_step(pa, t, rec, stream, ev);
-            else launches += f32->step(t, rec, stream, ev);
+            // (an FP32 record step takes the general pass to capture the
+            // slices; with nobody taking the records it is an ordinary step)
+            else launches += f32->step(t, rec && (collect || sink), stream, ev);
             mfdtd::ck(cudaGetLastError(), "kernel launch");
             if (rec && (collect || sink)) {
                 mfdtd::ck(cudaEventRecord(ev1, stream), "cudaEventRecord");

@@ -10,11 +10,12 @@ The large-trail workload's physics at 96 x 96 x 192 cells (bench.py workload
   node;
 * oblique TM plane wave at theta = 70, phi = 20 degrees.
 
-Every step but the record step t = 0 of the FP32 form runs the interior pass
-with two cells per thread (k_fp32_step_wide) and, on a second stream, the
-march over the CPML slabs and domain edges (k_fp32_slab), then the oblique
-TF/SF corrections and the Huygens-surface DFT kernel; the test checks that
-these are the kernels that ran.  The FP64 plain form runs the same inputs; on
+Every step of the FP32 form (no records are taken, so step 0 is an ordinary
+step too) runs the interior pass with two cells per thread
+(k_fp32_step_wide) and, on a second stream, the march over the CPML slabs
+and domain edges (k_fp32_slab), then the oblique TF/SF corrections and the
+Huygens-surface DFT kernels; the test checks that these are the kernels that
+ran.  The FP64 plain form runs the same inputs; on
 extended inputs it is byte-identical to the CPU oracle (tests/test_gpu_ext.py).
 
 Tolerances (FP32 fields against FP64 after 1200 steps):
@@ -60,8 +61,8 @@ def runs(built):
 def test_benchmark_pass_kernels_ran(runs):
     _, _, s32 = runs
     name = s32.kernel_stats()[0][0]
-    # the interior pass with the slab march; t = 0 is a record step (general pass)
-    assert name == "k_fp32_step_wide+k_fp32_slab+k_fp32_step", name
+    # the interior pass with the slab march on every step, t = 0 included
+    assert name == "k_fp32_step_wide+k_fp32_slab", name
 
 
 def test_fields_close_to_plain(runs):
