@@ -180,6 +180,11 @@ int mfdtd_problem_dims(const mfdtd_problem *pb, int64_t out[6]);
 int mfdtd_problem_footprint(const mfdtd_problem *pb, int32_t form, int64_t *bytes);
 
 /* ---- simulation (device) -------------------------------------------------- */
+/* The FP32 form takes its device memory from the device's default
+ * stream-ordered pool, which this library sets to keep up to a quarter of the
+ * device's memory cached after frees: memory a destroyed simulation held
+ * stays reserved by the process, for the next simulation, up to that amount
+ * (cudaMemPoolTrimTo on the default pool returns it). */
 int mfdtd_sim_create(const mfdtd_problem *pb, const mfdtd_run_opts *opts, mfdtd_sim **out);
 void mfdtd_sim_destroy(mfdtd_sim *s);  /* leaves its batch first, if any */
 /* Advance `nsteps` time steps (source/meteor-2.1.cpp:652-1574 per step).
