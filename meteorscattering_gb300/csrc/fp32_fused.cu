@@ -734,6 +734,29 @@ __device__ __forceinline__ SlabCell slab_cell(const Args &a, int j, int k) {
     return c;
 }
 
+// A slab-march tile whose cells and halos all lie inside the grid's y
+// interior (rows [w, Ny - w - 1], w = L + 1: no y slab, no y face) or its z
+// interior marches with that axis's slab indices and face flags as
+// constants: YZ bit 0 keeps the y ones, bit 1 the z ones.  The compiler then
+// drops that axis's psi terms and tests from the cell updates; the arithmetic
+// of the terms that remain is unchanged.
+template <int YZ>
+__device__ __forceinline__ SlabCell slab_view(SlabCell c) {
+    if constexpr (!(YZ & 1)) {
+        c.syh = -1;
+        c.sye = -1;
+        c.jn = true;
+        c.j1 = true;
+    }
+    if constexpr (!(YZ & 2)) {
+        c.szh = -1;
+        c.sze = -1;
+        c.kn = true;
+        c.k1 = true;
+    }
+    return c;
+}
+
 // The six psi values of a cell's H (or E) update on plane i, as h_slab (or
 // e_slab) uses them; zero where unused.  The slab march loads them one plane
 // ahead, so that their latency overlaps the previous plane's work.
@@ -1110,7 +1133,7 @@ enum : int { MARCH_GENERAL = 0, MARCH_FAST = 1, MARCH_SLAB = 2 };
 
 // The plane loop of one CTA.  Returns the plane at which a TMA wait ran out,
 // or -1.
-template <int PAR, int JM, bool CLEAN, int MODE = MARCH_GENERAL, bool PSIPF = true>
+template <int PAR, int JM, bool CLEAN, int MODE = MARCH_GENERAL, bool PSIPF = true, int YZ = 3>
 __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &c, int t, int record,
                                      bool tf_in) {
     constexpr bool FASTONLY = MODE == MARCH_FAST, SLAB = MODE == MARCH_SLAB;
@@ -1183,7 +1206,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     SlabCell sc{};
     Psi6 nhp{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nep = nhp;  // SLAB with PSIPF: psi of the next plane
     if constexpr (SLAB) {
-        sc = slab_cell(a, j, k);
+        sc = slab_view<YZ>(slab_cell(a, j, k));
         if (PSIPF && in_grid) {
             nhp = h_slab_psi<PAR>(a, c.p0, sc, warp != TJ, warp != TJ + 1);
             if (valid && c.p0 >= c.i_begin) nep = e_slab_psi(a, c.p0, sc);
@@ -1484,7 +1507,7 @@ __device__ __forceinline__ void record_probes(const Args &a, int t) {
 // CTA's stage mbarriers hold an earlier item's objects (they are invalidated
 // and re-initialised).  Returns false when a bounded wait ran out (the
 // simulation's error flag is then set).
-template <int PAR, int JM, int MODE = MARCH_GENERAL, bool PSIPF = true>
+template <int PAR, int JM, int MODE = MARCH_GENERAL, bool PSIPF = true, int YZ = 3>
 __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int tile_id, int i_begin, int i_end,
                                          bool first, int t, int record, unsigned char *smem_raw,
                                          bool inited) {
@@ -1551,7 +1574,7 @@ __device__ __forceinline__ bool run_item(const Maps &maps, const Args &a, int ti
 
     int fail_q;
     if constexpr (MODE == MARCH_SLAB) {
-        fail_q = march<PAR, JM, false, MARCH_SLAB, PSIPF>(maps, a, c, t, 0, false);
+        fail_q = march<PAR, JM, false, MARCH_SLAB, PSIPF, YZ>(maps, a, c, t, 0, false);
     } else {
         const TileInfo ti = classify(a, c.j0, c.k0, record);
         if constexpr (MODE == MARCH_FAST)
@@ -1623,8 +1646,10 @@ __global__ void __launch_bounds__(NTHREADS, 2)
     k_fp32_slab(const __grid_constant__ Maps maps, const __grid_constant__ Args a, int t,
                 const int4 *__restrict__ items) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int4 w = items[blockIdx.x];
-    run_item<PAR, JM, MARCH_SLAB>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
+    const int4 w = items[blockIdx.x];  // (tile, first plane, end plane, YZ: see slab_view)
+    if (w.w == 1) run_item<PAR, JM, MARCH_SLAB, true, 1>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
+    else if (w.w == 2) run_item<PAR, JM, MARCH_SLAB, true, 2>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
+    else run_item<PAR, JM, MARCH_SLAB>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
 }
 
 // ---------------------------------------------------------------------------
@@ -3162,8 +3187,17 @@ void Fp32Sim::init(const Problem &P, void *stream) {
             // Tiles reaching into the y/z slabs: every plane, in x-chunks of
             // about 96 planes (long marches first).
             const int ce = std::max(1, (P.Nx + 95) / 96), cl = (P.Nx + ce - 1) / ce;
+            // the axes whose slabs or faces the tile (halos included) touches
+            auto yz = [&](int tl) {
+                const int j0 = (tl / a.ntk) * TJ, k0 = (tl % a.ntk) * TK;
+                const bool yin = j0 - 1 >= w && j0 + TJ - 1 <= P.Ny - w - 1;
+                const bool zin = k0 - 1 >= w && k0 + TK - 1 <= P.Nz - w - 1;
+                const int m = (yin ? 0 : 1) | (zin ? 0 : 2);
+                return m == 0 ? 1 : m;
+            };
             for (int tl : edge)
-                for (int ib = 0; ib < P.Nx; ib += cl) items.push_back(make_int4(tl, ib, std::min(P.Nx, ib + cl), 0));
+                for (int ib = 0; ib < P.Nx; ib += cl)
+                    items.push_back(make_int4(tl, ib, std::min(P.Nx, ib + cl), yz(tl)));
             m.slab_items = m.upload(items, s);
             m.n_slab_items = (int)items.size();
         } else {
