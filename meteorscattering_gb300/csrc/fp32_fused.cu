@@ -1647,7 +1647,8 @@ __global__ void __launch_bounds__(NTHREADS, 2)
                 const int4 *__restrict__ items) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int4 w = items[blockIdx.x];  // (tile, first plane, end plane, YZ: see slab_view)
-    if (w.w == 1) run_item<PAR, JM, MARCH_SLAB, true, 1>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
+    if (w.w == 0) run_item<PAR, JM, MARCH_SLAB, true, 0>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
+    else if (w.w == 1) run_item<PAR, JM, MARCH_SLAB, true, 1>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
     else if (w.w == 2) run_item<PAR, JM, MARCH_SLAB, true, 2>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
     else run_item<PAR, JM, MARCH_SLAB>(maps, a, w.x, w.y, w.z, false, t, 0, smem_raw, false);
 }
@@ -1990,7 +1991,7 @@ __constant__ Args c_jobs[kMaxBatch];
 struct BatchItem {
     int job, tile;
     unsigned short ib, ie;
-    unsigned char mode, first, pad[2];
+    unsigned char mode, first, yz, pad;  // yz: MARCH_SLAB items' axis class (slab_view)
 };
 
 // KIND: 0, every item takes the general path; 1, a batch whose members all
@@ -2034,17 +2035,23 @@ __global__ void __launch_bounds__(NTHREADS, (JM == 2 || KIND == 2) ? 2 : 3)
                 ok = wide_item<PAR, JM>(mapsw[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, smem_raw);
                 last = 2;
             } else {
-                ok = run_item<PAR, JM, MARCH_SLAB>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0,
-                                                   smem_raw, false);
+                const Maps &mp = maps[w.job];
+                const bool f = w.first != 0;
+                if (w.yz == 1) ok = run_item<PAR, JM, MARCH_SLAB, true, 1>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
+                else if (w.yz == 2) ok = run_item<PAR, JM, MARCH_SLAB, true, 2>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
+                else ok = run_item<PAR, JM, MARCH_SLAB>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
                 last = 1;
             }
         } else if constexpr (KIND == 1) {
+            const Maps &mp = maps[w.job];
+            const bool f = w.first != 0;
             if (w.mode == MARCH_FAST)
-                ok = run_item<PAR, JM, MARCH_FAST>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw,
-                                                   false);
-            else  // (three CTAs per SM: no registers for the psi prefetch)
-                ok = run_item<PAR, JM, MARCH_SLAB, false>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0,
-                                                          smem_raw, false);
+                ok = run_item<PAR, JM, MARCH_FAST>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
+            // (three CTAs per SM: no registers for the psi prefetch)
+            else if (w.yz == 0) ok = run_item<PAR, JM, MARCH_SLAB, false, 0>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
+            else if (w.yz == 1) ok = run_item<PAR, JM, MARCH_SLAB, false, 1>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
+            else if (w.yz == 2) ok = run_item<PAR, JM, MARCH_SLAB, false, 2>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
+            else ok = run_item<PAR, JM, MARCH_SLAB, false>(mp, a, w.tile, w.ib, w.ie, f, t, 0, smem_raw, false);
             last = 1;
         } else {
             ok = run_item<PAR, JM>(maps[w.job], a, w.tile, w.ib, w.ie, w.first != 0, t, 0, smem_raw, false);
@@ -2829,6 +2836,15 @@ static void configure_pool() {
     done.push_back(dev);
 }
 
+// The axes whose CPML slabs or domain faces a slab-march tile touches, its
+// halo row and column included (slab_view): bit 0 y, bit 1 z.
+static int slab_yz(const Fp32Sim::Impl &m, int tl) {
+    const int w = m.wband, j0 = (tl / m.a.ntk) * TJ, k0 = (tl % m.a.ntk) * TK;
+    const bool yin = j0 - 1 >= w && j0 + TJ - 1 <= m.Ny - w - 1;
+    const bool zin = k0 - 1 >= w && k0 + TK - 1 <= m.Nz - w - 1;
+    return (yin ? 0 : 1) | (zin ? 0 : 2);
+}
+
 void Fp32Sim::init(const Problem &P, void *stream) {
     cudaStream_t s = (cudaStream_t)stream;
     if (P.L > kMaxPml) throw Error(MFDTD_EINVAL, "CPML too thick");
@@ -3187,17 +3203,9 @@ void Fp32Sim::init(const Problem &P, void *stream) {
             // Tiles reaching into the y/z slabs: every plane, in x-chunks of
             // about 96 planes (long marches first).
             const int ce = std::max(1, (P.Nx + 95) / 96), cl = (P.Nx + ce - 1) / ce;
-            // the axes whose slabs or faces the tile (halos included) touches
-            auto yz = [&](int tl) {
-                const int j0 = (tl / a.ntk) * TJ, k0 = (tl % a.ntk) * TK;
-                const bool yin = j0 - 1 >= w && j0 + TJ - 1 <= P.Ny - w - 1;
-                const bool zin = k0 - 1 >= w && k0 + TK - 1 <= P.Nz - w - 1;
-                const int m = (yin ? 0 : 1) | (zin ? 0 : 2);
-                return m == 0 ? 1 : m;
-            };
             for (int tl : edge)
                 for (int ib = 0; ib < P.Nx; ib += cl)
-                    items.push_back(make_int4(tl, ib, std::min(P.Nx, ib + cl), yz(tl)));
+                    items.push_back(make_int4(tl, ib, std::min(P.Nx, ib + cl), slab_yz(m, tl)));
             m.slab_items = m.upload(items, s);
             m.n_slab_items = (int)items.size();
         } else {
@@ -3709,6 +3717,7 @@ static void build_items(Fp32Batch::Impl &b) {
                 w.ib = (unsigned short)c0;
                 w.ie = (unsigned short)std::min(ie, c0 + chunk);
                 w.mode = (unsigned char)mode;
+                w.yz = (unsigned char)(mode == MARCH_SLAB ? slab_yz(m, tile) : 3);
                 w.first = first ? 1 : 0;
                 first = false;
                 v.push_back(w);
