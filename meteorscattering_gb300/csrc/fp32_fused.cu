@@ -1155,9 +1155,10 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
     // The plasma weight (and collision frequency) of the thread's cell is
     // prefetched one plane ahead into registers, so its latency overlaps the
-    // previous plane's work.  (Prefetching the x-normal CPML psi the same way
-    // was measured slower: the registers it holds across the plane loop made
-    // the boundary path spill.)
+    // previous plane's work.  (In the general path, prefetching the x-normal
+    // CPML psi the same way was measured slower: the registers it holds
+    // across the plane loop made the boundary path spill.  The slab march,
+    // at two CTAs per SM, prefetches all of its cell's psi values: Psi6.)
     const int jj = valid ? j : 0, kk = valid ? k : 0;
     auto pf_load = [&](int qq, float &wq, float &nu) {
         if (!valid || qq >= Nx) return;
