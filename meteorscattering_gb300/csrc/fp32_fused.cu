@@ -764,8 +764,8 @@ struct Psi6 {
     float p0, p1, p2, p3, p4, p5;
 };
 template <int PAR>
-__device__ __forceinline__ Psi6 h_slab_psi(const Args &a, int i, const SlabCell &sc, bool want_y, bool want_z) {
-    const int sxh = hslab(i, a.Nx, a.L, a.xshift);
+__device__ __forceinline__ Psi6 h_slab_psi(const Args &a, int i, int sxh, const SlabCell &sc, bool want_y,
+                                           bool want_z) {
     const bool xin = i < a.Nx - 1;
     const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
     const bool ux = sc.jn && sc.kn, uy = want_y && xin && sc.kn, uz = want_z && xin && sc.jn;
@@ -781,8 +781,7 @@ __device__ __forceinline__ Psi6 h_slab_psi(const Args &a, int i, const SlabCell 
     if (uz && sc.syh >= 0) q.p5 = R[5][oy];
     return q;
 }
-__device__ __forceinline__ Psi6 e_slab_psi(const Args &a, int i, const SlabCell &sc) {
-    const int sxe = eslab(i, a.Nx, a.L, a.xshift);
+__device__ __forceinline__ Psi6 e_slab_psi(const Args &a, int i, int sxe, const SlabCell &sc) {
     const bool iy = i >= 1 && i < a.Nx - 1;
     const bool ux = i < a.Nx - 1 && sc.j1 && sc.jn && sc.k1 && sc.kn, uy = iy && sc.k1, uz = iy && sc.j1;
     const bool xp = sxe >= 0 && sc.jn && sc.kn;
@@ -1206,11 +1205,14 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     float hy_prev = 0.f, hz_prev = 0.f, ex_prev = 0.f;
     SlabCell sc{};
     Psi6 nhp{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, nep = nhp;  // SLAB with PSIPF: psi of the next plane
+    // SLAB: the next plane's x-slab indices (plane-uniform), computed once
+    // for the prefetch and the update
+    int nsxh = hslab(c.p0, Nx, L, a.xshift), nsxe = eslab(c.p0, Nx, L, a.xshift);
     if constexpr (SLAB) {
         sc = slab_view<YZ>(slab_cell(a, j, k));
         if (PSIPF && in_grid) {
-            nhp = h_slab_psi<PAR>(a, c.p0, sc, warp != TJ, warp != TJ + 1);
-            if (valid && c.p0 >= c.i_begin) nep = e_slab_psi(a, c.p0, sc);
+            nhp = h_slab_psi<PAR>(a, c.p0, nsxh, sc, warp != TJ, warp != TJ + 1);
+            if (valid && c.p0 >= c.i_begin) nep = e_slab_psi(a, c.p0, nsxe, sc);
         }
     }
     // The stage slot of plane q and the cell offset advance with q (no
@@ -1224,12 +1226,17 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         npl = q + 1 < c.i_end && plasma_at(a, c, q + 1);
         if (npl) pf_load(q + 1, nwq, nnu);
         Psi6 hps{0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, eps = hps;  // SLAB: this plane's psi
+        const int sxh = nsxh, sxe = nsxe;
+        if constexpr (SLAB) {
+            nsxh = hslab(q + 1, Nx, L, a.xshift);
+            nsxe = eslab(q + 1, Nx, L, a.xshift);
+        }
         if constexpr (SLAB && PSIPF) {
             hps = nhp;
             eps = nep;
             if (in_grid && q + 1 < c.i_end) {
-                nhp = h_slab_psi<PAR>(a, q + 1, sc, warp != TJ, warp != TJ + 1);
-                if (valid && q + 1 >= c.i_begin) nep = e_slab_psi(a, q + 1, sc);
+                nhp = h_slab_psi<PAR>(a, q + 1, nsxh, sc, warp != TJ, warp != TJ + 1);
+                if (valid && q + 1 >= c.i_begin) nep = e_slab_psi(a, q + 1, nsxe, sc);
             }
         }
         const int slot1 = slot == NS - 1 ? 0 : slot + 1;
@@ -1369,8 +1376,8 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         HVal hv = {0.f, 0.f, 0.f};
         if constexpr (SLAB) {
             if (in_grid) {
-                if constexpr (!PSIPF) hps = h_slab_psi<PAR>(a, i, sc, warp != TJ, warp != TJ + 1);
-                hv = h_slab<PAR>(a, *c.tbs, i, hslab(i, Nx, L, a.xshift), StageSrc{s, s1, dj, dk}, sc, tile && real,
+                if constexpr (!PSIPF) hps = h_slab_psi<PAR>(a, i, sxh, sc, warp != TJ, warp != TJ + 1);
+                hv = h_slab<PAR>(a, *c.tbs, i, sxh, StageSrc{s, s1, dj, dk}, sc, tile && real,
                                  warp != TJ, warp != TJ + 1, hps);
             }
         } else {
@@ -1394,9 +1401,9 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         if (valid && real) {
             const float ex_old = s.e[0][EIDX(dj, dk)];
             EVal ev;
-            if constexpr (SLAB && !PSIPF) eps = e_slab_psi(a, i, sc);
+            if constexpr (SLAB && !PSIPF) eps = e_slab_psi(a, i, sxe, sc);
             if constexpr (SLAB)
-                ev = e_slab<PAR>(a, *c.tbs, i, eslab(i, Nx, L, a.xshift), ex_old, s.e[1][EIDX(dj, dk)],
+                ev = e_slab<PAR>(a, *c.tbs, i, sxe, ex_old, s.e[1][EIDX(dj, dk)],
                                  s.e[2][EIDX(dj, dk)], hv, StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, sc,
                                  eps);
             else
