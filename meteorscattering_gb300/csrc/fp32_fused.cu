@@ -119,6 +119,9 @@ struct Args {
     float *E[2][3], *H[2][3], *J[3];
     float *Ph[2][6];     // H psi: xy, xz, yx, yz, zx, zy
     float *Pe[6];        // E psi: xy, xz, yx, yz, zx, zy
+    // psi plane strides: y-normal arrays [Nx][2L][Nz], z-normal [Nx][Ny][2L],
+    // and the x-normal arrays' slab stride ([2L][Ny][Nz])
+    unsigned psi_py, psi_pz, psi_px;
     float *inc[2][4];    // 1-D line: Eyinc, Ezinc, Hyinc, Hzinc
     float *incP[2][4];   // 1-D psi: PeyxI, PezxI, PhyxI, PhzxI
     const float *wq2;    // E0 * wp2^2 per (i,j)
@@ -767,7 +770,7 @@ template <int PAR>
 __device__ __forceinline__ Psi6 h_slab_psi(const Args &a, int i, int sxh, const SlabCell &sc, bool want_y,
                                            bool want_z) {
     const bool xin = i < a.Nx - 1;
-    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const unsigned PY = a.psi_py, PZ = a.psi_pz, PX = a.psi_px;
     const bool ux = sc.jn && sc.kn, uy = want_y && xin && sc.kn, uz = want_z && xin && sc.jn;
     const unsigned oy = sc.oyh + (unsigned)i * PY, oz = sc.ozh + (unsigned)i * PZ,
                    ox = (unsigned)max(sxh, 0) * PX + sc.ox;
@@ -785,7 +788,7 @@ __device__ __forceinline__ Psi6 e_slab_psi(const Args &a, int i, int sxe, const 
     const bool iy = i >= 1 && i < a.Nx - 1;
     const bool ux = i < a.Nx - 1 && sc.j1 && sc.jn && sc.k1 && sc.kn, uy = iy && sc.k1, uz = iy && sc.j1;
     const bool xp = sxe >= 0 && sc.jn && sc.kn;
-    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const unsigned PY = a.psi_py, PZ = a.psi_pz, PX = a.psi_px;
     const unsigned oy = sc.oye + (unsigned)i * PY, oz = sc.oze + (unsigned)i * PZ,
                    ox = (unsigned)max(sxe, 0) * PX + sc.ox;
     float *const *Pe = a.Pe;
@@ -809,7 +812,7 @@ __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, in
     o.z = src.h(2);
     const float ex = src.e(0), ey = src.e(1), ez = src.e(2);
     const bool xin = i < a.Nx - 1;
-    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const unsigned PY = a.psi_py, PZ = a.psi_pz, PX = a.psi_px;
     const bool ux = sc.jn && sc.kn, uy = want_y && xin && sc.kn, uz = want_z && xin && sc.jn;
     const unsigned oy = sc.oyh + (unsigned)i * PY, oz = sc.ozh + (unsigned)i * PZ,
                    ox = (unsigned)max(sxh, 0) * PX + sc.ox;
@@ -879,7 +882,7 @@ __device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, in
     const float c1 = a.c1e0, c2 = a.c2e0, cx = a.cex, cy = a.cey, cz = a.cez;
     const bool iy = i >= 1 && i < a.Nx - 1;
     const bool ux = i < a.Nx - 1 && sc.j1 && sc.jn && sc.k1 && sc.kn, uy = iy && sc.k1, uz = iy && sc.j1;
-    const unsigned PY = 2u * a.L * a.Nz, PZ = (unsigned)a.Ny * 2u * a.L, PX = (unsigned)a.Ny * a.Nz;
+    const unsigned PY = a.psi_py, PZ = a.psi_pz, PX = a.psi_px;
     const unsigned oy = sc.oye + (unsigned)i * PY, oz = sc.oze + (unsigned)i * PZ,
                    ox = (unsigned)max(sxe, 0) * PX + sc.ox;
     float *const *Pe = a.Pe;
@@ -2866,6 +2869,9 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     if (m.nprobes > 24) throw Error(MFDTD_EINVAL, "FP32 form supports at most 24 probes");
     a.Nx = P.Nx; a.Ny = P.Ny; a.Nz = P.Nz; a.Nzp = m.Nzp; a.L = P.L;
     a.xshift = P.xshift; a.yshift = P.yshift; a.zshift = P.zshift;
+    a.psi_py = 2u * P.L * P.Nz;
+    a.psi_pz = (unsigned)P.Ny * 2u * P.L;
+    a.psi_px = (unsigned)P.Ny * P.Nz;
     a.bx1 = P.bx1; a.bx2 = P.bx2; a.by1 = P.by1; a.by2 = P.by2; a.bz1 = P.bz1; a.bz2 = P.bz2;
     a.ntfb = P.ntfb; a.nntf = P.nntf(); a.ssx = P.ssx; a.ssy = P.ssy; a.ssz = P.ssz;
     a.dopml = P.dopml; a.doplate = P.doplate; a.doB0 = P.doB0; a.lk_mode = P.lk_mode;
