@@ -717,6 +717,9 @@ struct SlabCell {
     bool jn, kn, j1, k1;            // j < Ny-1, k < Nz-1, j >= 1, k >= 1
     unsigned oyh, oye, ozh, oze;    // y- and z-normal psi offsets at plane 0
     unsigned ox;                    // x-normal psi offset within a slab plane
+    // the y- and z-normal CPML coefficients of the cell (B, A, K of H and E),
+    // read once per item in the axis-specialized marches (slab_coef)
+    float bhy, ahy, khy, bey, aey, key, bhz, ahz, khz, bez, aez, kez;
 };
 __device__ __forceinline__ SlabCell slab_cell(const Args &a, int j, int k) {
     SlabCell c;
@@ -756,6 +759,34 @@ __device__ __forceinline__ SlabCell slab_view(SlabCell c) {
         c.sze = -1;
         c.kn = true;
         c.k1 = true;
+    }
+    return c;
+}
+
+// In a march specialized to one axis (YZ 0, 1, 2) the cell's CPML
+// coefficients along the axis it keeps are loaded from the shared-memory
+// tables once per item instead of on every plane (the plane loop's barriers
+// and fences keep the compiler from hoisting those loads itself).  The
+// general march (YZ 3) reads them at the point of use.
+template <int YZ>
+__device__ __forceinline__ SlabCell slab_coef(SlabCell c, const Tables &T) {
+    if constexpr (YZ == 1) {
+        const int h = max(c.syh, 0), e = max(c.sye, 0);
+        c.bhy = T.Bh[h];
+        c.ahy = T.Ahy[h];
+        c.khy = T.Khy[h];
+        c.bey = T.Be[e];
+        c.aey = T.Aey[e];
+        c.key = T.Key[e];
+    }
+    if constexpr (YZ == 2) {
+        const int h = max(c.szh, 0), e = max(c.sze, 0);
+        c.bhz = T.Bh[h];
+        c.ahz = T.Ahz[h];
+        c.khz = T.Khz[h];
+        c.bez = T.Be[e];
+        c.aez = T.Aez[e];
+        c.kez = T.Kez[e];
     }
     return c;
 }
@@ -802,7 +833,7 @@ __device__ __forceinline__ Psi6 e_slab_psi(const Args &a, int i, int sxe, const 
     return q;
 }
 
-template <int PAR, class Src>
+template <int PAR, int YZ, class Src>
 __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, int sxh, const Src &src,
                                        const SlabCell &sc, bool store_psi, bool want_y, bool want_z,
                                        const Psi6 &ps) {
@@ -823,16 +854,16 @@ __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, in
         const float dEy = src.ek(1) - ey;
         float h = a.c1h * o.x - (a.chy * dEz - a.chz * dEy);
         if (sc.syh >= 0) {
-            const float p = T.Bh[sc.syh] * p0 + T.Ahy[sc.syh] * dEz;
+            const float p = (YZ == 1 ? sc.bhy : T.Bh[sc.syh]) * p0 + (YZ == 1 ? sc.ahy : T.Ahy[sc.syh]) * dEz;
             if (store_psi) W[0][oy] = p;
             h -= a.c2h * p;
-            if (a.kappa_on) h -= a.c2h * (T.Khy[sc.syh] * dEz);
+            if (a.kappa_on) h -= a.c2h * ((YZ == 1 ? sc.khy : T.Khy[sc.syh]) * dEz);
         }
         if (sc.szh >= 0) {
-            const float p = T.Bh[sc.szh] * p1 + T.Ahz[sc.szh] * dEy;
+            const float p = (YZ == 2 ? sc.bhz : T.Bh[sc.szh]) * p1 + (YZ == 2 ? sc.ahz : T.Ahz[sc.szh]) * dEy;
             if (store_psi) W[1][oz] = p;
             h += a.c2h * p;
-            if (a.kappa_on) h += a.c2h * (T.Khz[sc.szh] * dEy);
+            if (a.kappa_on) h += a.c2h * ((YZ == 2 ? sc.khz : T.Khz[sc.szh]) * dEy);
         }
         o.x = h;
     }
@@ -847,10 +878,10 @@ __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, in
             if (a.kappa_on) h += a.c2h * (T.Khx[sxh] * dEz);
         }
         if (sc.szh >= 0) {
-            const float p = T.Bh[sc.szh] * p3 + T.Ahz[sc.szh] * dEx;
+            const float p = (YZ == 2 ? sc.bhz : T.Bh[sc.szh]) * p3 + (YZ == 2 ? sc.ahz : T.Ahz[sc.szh]) * dEx;
             if (store_psi) W[3][oz] = p;
             h -= a.c2h * p;
-            if (a.kappa_on) h -= a.c2h * (T.Khz[sc.szh] * dEx);
+            if (a.kappa_on) h -= a.c2h * ((YZ == 2 ? sc.khz : T.Khz[sc.szh]) * dEx);
         }
         o.y = h;
     }
@@ -865,17 +896,17 @@ __device__ __forceinline__ HVal h_slab(const Args &a, const Tables &T, int i, in
             if (a.kappa_on) h -= a.c2h * (T.Khx[sxh] * dEy);
         }
         if (sc.syh >= 0) {
-            const float p = T.Bh[sc.syh] * p5 + T.Ahy[sc.syh] * dEx;
+            const float p = (YZ == 1 ? sc.bhy : T.Bh[sc.syh]) * p5 + (YZ == 1 ? sc.ahy : T.Ahy[sc.syh]) * dEx;
             if (store_psi) W[5][oy] = p;
             h += a.c2h * p;
-            if (a.kappa_on) h += a.c2h * (T.Khy[sc.syh] * dEx);
+            if (a.kappa_on) h += a.c2h * ((YZ == 1 ? sc.khy : T.Khy[sc.syh]) * dEx);
         }
         o.z = h;
     }
     return o;
 }
 
-template <int PAR, class HS>
+template <int PAR, int YZ, class HS>
 __device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, int sxe, float ex, float ey, float ez,
                                        const HVal &hv, const HS &hs, float jx, float jy, float jz,
                                        const SlabCell &sc, const Psi6 &ps) {
@@ -892,16 +923,16 @@ __device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, in
         const float dHy = hv.y - hs.hk(1);
         float e = c1 * ex + (cy * dHz - cz * dHy) - c2 * jx;
         if (sc.sye >= 0) {
-            const float p = T.Be[sc.sye] * p0 + T.Aey[sc.sye] * dHz;
+            const float p = (YZ == 1 ? sc.bey : T.Be[sc.sye]) * p0 + (YZ == 1 ? sc.aey : T.Aey[sc.sye]) * dHz;
             Pe[0][oy] = p;
             e += a.c2e0 * p;
-            if (a.kappa_on) e += a.c2e0 * (T.Key[sc.sye] * dHz);
+            if (a.kappa_on) e += a.c2e0 * ((YZ == 1 ? sc.key : T.Key[sc.sye]) * dHz);
         }
         if (sc.sze >= 0) {
-            const float p = T.Be[sc.sze] * p1 + T.Aez[sc.sze] * dHy;
+            const float p = (YZ == 2 ? sc.bez : T.Be[sc.sze]) * p1 + (YZ == 2 ? sc.aez : T.Aez[sc.sze]) * dHy;
             Pe[1][oz] = p;
             e -= a.c2e0 * p;
-            if (a.kappa_on) e -= a.c2e0 * (T.Kez[sc.sze] * dHy);
+            if (a.kappa_on) e -= a.c2e0 * ((YZ == 2 ? sc.kez : T.Kez[sc.sze]) * dHy);
         }
         ex = e;
     }
@@ -921,11 +952,11 @@ __device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, in
         if (sc.sze >= 0) {
             float p = 0.f;
             if (sc.jn) {
-                p = T.Be[sc.sze] * p3 + T.Aez[sc.sze] * dHx;
+                p = (YZ == 2 ? sc.bez : T.Be[sc.sze]) * p3 + (YZ == 2 ? sc.aez : T.Aez[sc.sze]) * dHx;
                 Pe[3][oz] = p;
             }
             e += a.c2e0 * p;
-            if (a.kappa_on) e += a.c2e0 * (T.Kez[sc.sze] * dHx);
+            if (a.kappa_on) e += a.c2e0 * ((YZ == 2 ? sc.kez : T.Kez[sc.sze]) * dHx);
         }
         ey = e;
     }
@@ -943,10 +974,10 @@ __device__ __forceinline__ EVal e_slab(const Args &a, const Tables &T, int i, in
             if (a.kappa_on) e += a.c2e0 * (T.Kex[sxe] * dHy);
         }
         if (sc.sye >= 0 && sc.kn) {
-            const float p = T.Be[sc.sye] * p5 + T.Aey[sc.sye] * dHx;
+            const float p = (YZ == 1 ? sc.bey : T.Be[sc.sye]) * p5 + (YZ == 1 ? sc.aey : T.Aey[sc.sye]) * dHx;
             Pe[5][oy] = p;
             e -= a.c2e0 * p;
-            if (a.kappa_on) e -= a.c2e0 * (T.Key[sc.sye] * dHx);
+            if (a.kappa_on) e -= a.c2e0 * ((YZ == 1 ? sc.key : T.Key[sc.sye]) * dHx);
         }
         ez = e;
     }
@@ -1139,6 +1170,9 @@ template <int PAR, int JM, bool CLEAN, int MODE = MARCH_GENERAL, bool PSIPF = tr
 __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &c, int t, int record,
                                      bool tf_in) {
     constexpr bool FASTONLY = MODE == MARCH_FAST, SLAB = MODE == MARCH_SLAB;
+    // per-item CPML coefficients (slab_coef) where the registers allow: not in
+    // the three-CTAs-per-SM form without the psi prefetch
+    constexpr int CYZ = PSIPF ? YZ : 3;
     const int Nx = a.Nx, Ny = a.Ny, Nz = a.Nz, L = a.L;
     const size_t plane = (size_t)Ny * a.Nzp;
     const int dj = c.dj, dk = c.dk, j = c.j, k = c.k, warp = c.warp;
@@ -1212,7 +1246,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     // for the prefetch and the update
     int nsxh = hslab(c.p0, Nx, L, a.xshift), nsxe = eslab(c.p0, Nx, L, a.xshift);
     if constexpr (SLAB) {
-        sc = slab_view<YZ>(slab_cell(a, j, k));
+        sc = slab_coef<CYZ>(slab_view<YZ>(slab_cell(a, j, k)), *c.tbs);
         if (PSIPF && in_grid) {
             nhp = h_slab_psi<PAR>(a, c.p0, nsxh, sc, warp != TJ, warp != TJ + 1);
             if (valid && c.p0 >= c.i_begin) nep = e_slab_psi(a, c.p0, nsxe, sc);
@@ -1380,7 +1414,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
         if constexpr (SLAB) {
             if (in_grid) {
                 if constexpr (!PSIPF) hps = h_slab_psi<PAR>(a, i, sxh, sc, warp != TJ, warp != TJ + 1);
-                hv = h_slab<PAR>(a, *c.tbs, i, sxh, StageSrc{s, s1, dj, dk}, sc, tile && real,
+                hv = h_slab<PAR, CYZ>(a, *c.tbs, i, sxh, StageSrc{s, s1, dj, dk}, sc, tile && real,
                                  warp != TJ, warp != TJ + 1, hps);
             }
         } else {
@@ -1406,7 +1440,7 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
             EVal ev;
             if constexpr (SLAB && !PSIPF) eps = e_slab_psi(a, i, sxe, sc);
             if constexpr (SLAB)
-                ev = e_slab<PAR>(a, *c.tbs, i, sxe, ex_old, s.e[1][EIDX(dj, dk)],
+                ev = e_slab<PAR, CYZ>(a, *c.tbs, i, sxe, ex_old, s.e[1][EIDX(dj, dk)],
                                  s.e[2][EIDX(dj, dk)], hv, StageHSrc{hn, dj, dk, hy_prev, hz_prev}, jx, jy, jz, sc,
                                  eps);
             else
