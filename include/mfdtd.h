@@ -314,7 +314,8 @@ int mfdtd_batch_tune(mfdtd_batch *b, const int32_t *slab_depths, int32_t n_depth
                      const int32_t *ctas_per_sm, int32_t n_ctas, int32_t *best_depth,
                      int32_t *best_ctas);
 /* The (j, k) tile shape the batch runs its interior tiles with: 8 x 32 or
- * 8 x 64 (see mfdtd_batch_tune). */
+ * 8 x 64 (see mfdtd_batch_tune).  Untuned, a batch whose members qualify for
+ * the slab march runs 8 x 64 at two CTAs per SM. */
 int mfdtd_batch_tile_shape(const mfdtd_batch *b, int32_t *rows, int32_t *cols);
 
 /* ---- serving loop (chosen form) ---------------------------------------------

@@ -3543,9 +3543,12 @@ struct Fp32Batch::Impl {
     long long tick = 0;             // global step counter: parity of every slot's pass
     bool dirty = true;
     int chunk = 0;                  // planes per item (0: per-simulation default)
-    int ctas_per_sm = 3;
+    int ctas_per_sm = 3;            // (at most 2 for the wide path and tabulated Lee-Kalluri: launch_tick)
     int slabk = -1;                 // batch class of the members (Fp32Sim::batch_class); -1: empty
-    int tile_cols = 32;             // class 1: interior tiles 8 x 32 (fast path) or 8 x 64 (wide path)
+    // class 1: interior tiles 8 x 64 on the wide path (the default: on 24
+    // sweep trails 4.86 ms a tick against 5.15 at 8 x 32) or 8 x 32 on the
+    // fast path
+    int tile_cols = 64;
     int graph_cols = 0;
     Maps *d_mapsw = nullptr;        // the members' maps with the wide path's boxes
     cudaGraphExec_t graph = nullptr;
@@ -3821,7 +3824,9 @@ static int batch_kind(const Fp32Batch::Impl &b) { return b.slabk == 1 ? (b.tile_
 
 static void launch_tick(Fp32Batch::Impl &b, int par) {
     const int kind = batch_kind(b);
-    const dim3 grid(b.sms * b.ctas_per_sm);
+    // the kernels of the wide path and of tabulated Lee-Kalluri fit two CTAs per SM
+    const int cap = (kind == 2 || b.jm == 2) ? 2 : 3;
+    const dim3 grid(b.sms * std::min(b.ctas_per_sm, cap));
     const int smem = kind == 2 ? SMEM_BATCHW : kind == 1 ? SMEM_BS : SMEM_B;
     auto go = [&](auto kern) {
         kern<<<grid, NTHREADS, smem, b.stream>>>(b.items, b.d_n, b.d_next, b.d_maps, b.d_mapsw, b.d_t, b.d_end);
