@@ -131,6 +131,28 @@ def test_batch_membership_rules(built):
     b.close()
 
 
+def test_member_removed_between_dft_ring_flushes_keeps_its_sums(built):
+    """The running DFT of a member goes through a ring of 8 steps that its
+    batch flushes into the sums every 8 ticks.  A member leaving the batch
+    off a ring boundary (101 steps: 96 flushed, 5 still in the ring) has the
+    pending steps added on removal: continued alone to its end, it matches
+    the stand-alone run."""
+    pb = _problem(_long("lk_trail", 160))
+    ntf, _ = _alone(pb)
+    b = E.Batch()
+    s = E.Simulation(pb, form=E.FORM_FP32_FUSED)
+    b.add(s)
+    b.run(101)
+    b.sync()
+    b.remove(s)
+    assert s.step_index == 101
+    s.advance(59)
+    assert np.abs(ntf).max() > 0
+    assert H.rel_l2(s.read_ntf(), ntf) < TOL
+    b.close()
+    s.close()
+
+
 def test_two_batches_on_one_device_keep_their_members_apart(built):
     """Batches of different current updates (Lee-Kalluri, Young DI) run side by
     side on one device, as a server with several batch keys runs them.  The
