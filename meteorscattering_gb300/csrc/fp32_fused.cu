@@ -2345,7 +2345,56 @@ __device__ __forceinline__ void tfsf_cell(const Args &a, int record, int i, int 
 }
 
 template <int PAR>
-__device__ __forceinline__ void tfsf_band(const Args &a, int record, size_t q0, size_t dq) {
+__device__ __forceinline__ void tfsf_band(const Args &a, int record, int r0, int dr, int c0, int dc) {
+    const int bx1 = a.bx1, bx2 = a.bx2, by1 = a.by1, by2 = a.by2, bz1 = a.bz1, bz2 = a.bz2;
+    const int Jr = by2 - by1 + 2, Kr = bz2 - bz1 + 2, Ir2 = max(bx2 - bx1 - 2, 0), Jr2 = by2 - by1 - 2;
+    const size_t plane = (size_t)a.Ny * a.Nzp;
+    auto pick = [](int b1, int b2, int s) { return s == 0 ? b1 - 1 : s == 1 ? b1 : s == 2 ? b2 - 1 : b2; };
+    // The band as rows, each cell once: the x layers' rows (4 x Jr rows along
+    // j, cells along k over [bz1 - 1, bz2]), the y layers' rows (4 x Ir2
+    // along i, cells along k) and the z layers' rows (4 x Ir2 along i, cells
+    // along j over [by1 + 1, by2 - 2]).  Rows r0, r0 + dr, ... and a row's
+    // cells c0, c0 + dc, ...: no division in the indexing.
+    const int rX = 4 * Jr, rY = 4 * Ir2, rZ = 4 * Ir2;
+    auto layer = [](int r, int n) { return r < n ? 0 : r < 2 * n ? 1 : r < 3 * n ? 2 : 3; };
+    // Crossing terms along an axis need the cell's (or its -1 neighbour's)
+    // index on that axis in {b1 - 1, b1, b2 - 1, b2}: the x layers away from
+    // their y and z edges, the y layers away from their z edges and every z
+    // layer cell need one axis's terms only.
+    for (int r = r0; r < rX + rY + rZ; r += dr) {
+        if (r < rX) {
+            const int l = layer(r, Jr);
+            const int i = pick(bx1, bx2, l), j = by1 - 1 + (r - l * Jr);
+            const bool yedge = j <= by1 || j >= by2 - 1;
+            for (int c = c0; c < Kr; c += dc) {
+                const int k = bz1 - 1 + c;
+                const bool zedge = k <= bz1 || k >= bz2 - 1;
+                if (yedge && zedge) tfsf_cell<PAR, 7>(a, record, i, j, k, plane);
+                else if (yedge) tfsf_cell<PAR, 3>(a, record, i, j, k, plane);
+                else if (zedge) tfsf_cell<PAR, 5>(a, record, i, j, k, plane);
+                else tfsf_cell<PAR, 1>(a, record, i, j, k, plane);
+            }
+        } else if (r < rX + rY) {
+            const int rr = r - rX, l = layer(rr, Ir2);
+            const int j = pick(by1, by2, l), i = bx1 + 1 + (rr - l * Ir2);
+            for (int c = c0; c < Kr; c += dc) {
+                const int k = bz1 - 1 + c;
+                if (k <= bz1 || k >= bz2 - 1) tfsf_cell<PAR, 6>(a, record, i, j, k, plane);
+                else tfsf_cell<PAR, 2>(a, record, i, j, k, plane);
+            }
+        } else {
+            const int rr = r - rX - rY, l = layer(rr, Ir2);
+            const int k = pick(bz1, bz2, l), i = bx1 + 1 + (rr - l * Ir2);
+            for (int c = c0; c < Jr2; c += dc) tfsf_cell<PAR, 4>(a, record, i, by1 + 1 + c, k, plane);
+        }
+    }
+}
+// The same band as one flat index space (one cell per thread and stride,
+// divisions in the indexing): the batch follow-up kernel's form, whose
+// members' bands are small (on 64-256-cell grids the row form left most of
+// a block idle and needed 109 registers there: a tick 6 % slower).
+template <int PAR>
+__device__ __forceinline__ void tfsf_band_flat(const Args &a, int record, size_t q0, size_t dq) {
     const int bx1 = a.bx1, bx2 = a.bx2, by1 = a.by1, by2 = a.by2, bz1 = a.bz1, bz2 = a.bz2;
     const int Jr = by2 - by1 + 2, Kr = bz2 - bz1 + 2, Ir2 = bx2 - bx1 - 2, Jr2 = by2 - by1 - 2;
     const size_t nX = 4 * (size_t)Jr * Kr, nY = 4 * (size_t)Ir2 * Kr, nZ = 4 * (size_t)Ir2 * Jr2;
@@ -2393,7 +2442,7 @@ __device__ __forceinline__ void tfsf_band(const Args &a, int record, size_t q0, 
 }
 template <int PAR>
 __global__ void __launch_bounds__(256) k_fp32_tfsf(const __grid_constant__ Args a, int record) {
-    tfsf_band<PAR>(a, record, (size_t)blockIdx.x * blockDim.x + threadIdx.x, (size_t)gridDim.x * blockDim.x);
+    tfsf_band<PAR>(a, record, blockIdx.x, gridDim.x, threadIdx.x, blockDim.x);
 }
 
 // The same follow-up work for every member of a batch after its tick's pass
@@ -2406,7 +2455,7 @@ __global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_
     if (t >= job_end[q]) return;
     const Args &a = c_jobs[q];
     const size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, dq = (size_t)gridDim.x * blockDim.x;
-    if (a.oblique && !a.obl_inline) tfsf_band<PAR>(a, 0, q0, dq);
+    if (a.oblique && !a.obl_inline) tfsf_band_flat<PAR>(a, 0, q0, dq);
     if (!a.ntf_inline && a.nntf > 0 && a.ntf_ring) ntf_stash(a, PAR ^ 1, a.ntf_ring, t % kNtfRing, q0, dq);
 }
 // After k_batch_post: a member whose tick filled its DFT ring (step t with
