@@ -21,13 +21,15 @@ public:
     int drain_ntf(void *stream);
     static int kernel_classes();
     // Batch class of a problem's FP32 simulation: 1 when batches march it
-    // with the fast path and the CPML slab march (CPML band on every axis,
-    // oblique incidence without a plate or sphere, no Lee-Kalluri table, an
-    // 8 x 32 tile interior in j and k), else 0 (general path).  A batch holds
+    // with an interior path (the wide 8 x 64 one by default, or the fast 8 x
+    // 32 one) and the CPML slab march (CPML band on every axis, oblique
+    // incidence without a plate or sphere, no Lee-Kalluri table, an 8 x 32
+    // tile interior in j and k), else 0 (general path).  A batch holds
     // simulations of one class.
     static int batch_class(const Problem &P);
-    // Passes run so far by the fast kernel (k_fp32_step_fast: every tile and
-    // plane interior, no record step) and by the general one (k_fp32_step).
+    // Passes run so far by the fast form (k_fp32_step_wide with the slab
+    // march, or k_fp32_step_fast with the band kernels: steps whose records
+    // nobody takes) and by the general one (k_fp32_step).
     long long fast_passes() const;
     long long general_passes() const;
     // Kernel name(s) of a fast pass: "k_fp32_step_wide+k_fp32_slab" (the
