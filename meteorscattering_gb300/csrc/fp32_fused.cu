@@ -2835,8 +2835,11 @@ struct Fp32Sim::Impl {
     const float4 *phase4 = nullptr;
     size_t nface = 0;
     int ring_t0 = 0, ring_fill = 0;
+    // the Huygens faces and the nodes behind them lie outside the TF/SF band
+    bool ntf_outside_band = false;
     cudaStream_t aux = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    cudaEvent_t ev_post = nullptr, ev_dft = nullptr;  // the DFT copy beside the TF/SF corrections
     // In a batch of class 1 (Fp32Sim::batch_class): the tiles whose cells are
     // all interior in j and k (fast path over the interior planes, slab march
     // over the x-slab planes) and the rest (slab march over every plane);
@@ -2875,6 +2878,8 @@ struct Fp32Sim::Impl {
         }
         if (ev_fork) cudaEventDestroy(ev_fork);
         if (ev_join) cudaEventDestroy(ev_join);
+        if (ev_post) cudaEventDestroy(ev_post);
+        if (ev_dft) cudaEventDestroy(ev_dft);
         // No kernel may still use the memory when it goes back to the pool
         // (as cudaFree would ensure); the frees then take no unmapping.
         if (!allocs.empty()) cudaDeviceSynchronize();
@@ -3105,6 +3110,9 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     a.phase = m.upload(P.phase, s);
     if (P.nntf() > 0) {
         m.nface = 2 * ((size_t)P.Ny * P.Nz + (size_t)P.Nx * P.Nz + (size_t)P.Nx * P.Ny);
+        const int nb = P.ntfb;
+        m.ntf_outside_band = nb >= 1 && nb + 2 <= std::min(P.bx1, std::min(P.by1, P.bz1)) && P.Nx - nb >= P.bx2 + 2 &&
+                             P.Ny - nb >= P.by2 + 2 && P.Nz - nb >= P.bz2 + 2;
         // per (step, frequency): the phase's FP32 high parts and remainders
         std::vector<float4> pf(P.phase.size() / 2);
         for (size_t q = 0; q < pf.size(); q++) {
@@ -3335,6 +3343,8 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         ck(cudaStreamCreateWithFlags(&m.aux, cudaStreamNonBlocking), "cudaStreamCreate");
         ck(cudaEventCreateWithFlags(&m.ev_fork, cudaEventDisableTiming), "cudaEventCreate");
         ck(cudaEventCreateWithFlags(&m.ev_join, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&m.ev_post, cudaEventDisableTiming), "cudaEventCreate");
+        ck(cudaEventCreateWithFlags(&m.ev_dft, cudaEventDisableTiming), "cudaEventCreate");
     }
     bytes_ = m.bytes;
 }
@@ -3441,18 +3451,36 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
         launches += 2;
     }
     if (ev) cudaEventRecord((cudaEvent_t)ev[1], s);
-    if (m.a.oblique && !m.a.obl_inline) {
-        if (m_cur_ == 0) k_fp32_tfsf<0><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
-        else k_fp32_tfsf<1><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
-        launches++;
-    }
-    if (ev) cudaEventRecord((cudaEvent_t)ev[2], s);
-    if (!m.a.ntf_inline && m.a.nntf > 0) {
+    // The DFT copy reads only the Huygens-face cells, which the TF/SF
+    // corrections do not touch (the faces lie outside the band): with the
+    // second stream it runs beside them, and the step ends when both have.
+    const bool tfsf = m.a.oblique && !m.a.obl_inline;
+    const bool dft = !m.a.ntf_inline && m.a.nntf > 0;
+    const bool dft_beside = dft && tfsf && m.aux && m.ntf_outside_band;
+    if (dft) {
         if (!m.ntf_ring) {
             m.ntf_ring = m.alloc<float>((size_t)kNtfRing * 6 * m.nface, s);
             bytes_ = m.bytes;
         }
         if (m.ring_fill == 0) m.ring_t0 = t;
+    }
+    if (dft_beside) {
+        ck(cudaEventRecord(m.ev_post, s), "cudaEventRecord");
+        ck(cudaStreamWaitEvent(m.aux, m.ev_post, 0), "cudaStreamWaitEvent");
+        k_fp32_ntf<<<m.sms * 8, 256, 0, m.aux>>>(m.a, m_cur_ ^ 1, m.ntf_ring, m.ring_fill);
+        launches++;
+        if (++m.ring_fill == kNtfRing) launches += drain_ntf(m.aux);
+    }
+    if (tfsf) {
+        if (m_cur_ == 0) k_fp32_tfsf<0><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
+        else k_fp32_tfsf<1><<<m.sms * 8, 256, 0, s>>>(m.a, rec);
+        launches++;
+    }
+    if (ev) cudaEventRecord((cudaEvent_t)ev[2], s);
+    if (dft_beside) {
+        ck(cudaEventRecord(m.ev_dft, m.aux), "cudaEventRecord");
+        ck(cudaStreamWaitEvent(s, m.ev_dft, 0), "cudaStreamWaitEvent");
+    } else if (dft) {
         k_fp32_ntf<<<m.sms * 8, 256, 0, s>>>(m.a, m_cur_ ^ 1, m.ntf_ring, m.ring_fill);
         launches++;
         if (++m.ring_fill == kNtfRing) launches += drain_ntf(stream);
