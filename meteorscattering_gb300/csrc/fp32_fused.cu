@@ -103,10 +103,11 @@ struct Args {
     // oblique incidence: auxiliary line (E in inc[][1], H in inc[][2])
     int oblique, M, ashift, lk_colocated;
     float kr[3], s0, ke[3], kh[3], chl, cel;   // chl = c2h/dl, cel = c2e0/dl
-    // Work done inside the step kernel (1) or by the kernels that follow it
-    // (0): the running DFT on the Huygens surface (k_fp32_ntf), the oblique
-    // TF/SF corrections (k_fp32_tfsf).  A batch keeps both inside.
-    int ntf_inline, obl_inline;
+    // The oblique TF/SF corrections made inside the step kernel (1) or by the
+    // kernels that follow it (0: k_fp32_tfsf, in a batch k_batch_post).  The
+    // running DFT on the Huygens surface always follows the pass: k_fp32_ntf
+    // (k_batch_post) copies each step's face values into the DFT ring.
+    int obl_inline;
     // Planes [xbeg, xend) are marched by the pass (x-chunks of `chunk` planes
     // from xbeg).  The fast pass leaves the band's x planes to the band
     // kernels (xbeg = L + 1); otherwise 0 and Nx.
@@ -131,7 +132,6 @@ struct Args {
     const float *G, *G2; // z-Gaussian and its square per k
     const float *lk;     // Lee-Kalluri table (18 per entry)
     const float *src;    // [tsteps][2]
-    const double *phase; // [tsteps][nntf][2]
     const double *xc, *yc, *zc;
     const int *tile_order;  // CTA -> tile (ty * ntk + tk): boundary tiles first
     int ntk;                // tiles along k
@@ -334,8 +334,6 @@ __device__ TileInfo classify(const Args &a, int j0, int k0, int record) {
     if (!a.oblique || a.obl_inline)  // TF/SF rows, when the corrections are made here
         c = c && clear(a.by1 - 1, a.bz1 - 1) && clear(a.by1, a.bz1) && clear(a.by2 - 1, a.bz2 - 1) &&
             clear(a.by2, a.bz2);
-    if (a.ntf_inline)  // Huygens rows, when the DFT is accumulated here
-        c = c && clear(a.ntfb, a.ntfb) && clear(Ny - a.ntfb, Nz - a.ntfb);
     // slices are written on record steps only
     c = c && !(record && (hits(jlo, jhi, a.ssy) || hits(klo, khi, a.ssz)));
     ti.clean = c;
@@ -1068,21 +1066,6 @@ __device__ void line_update(const Args &a, int t) {
     }
 }
 
-__device__ __forceinline__ void acc2(double *A, double *B, size_t base, double va, double vb,
-                                     const double *ph, int nf) {
-    for (int m = 0; m < nf; m++) {
-        const double s = ph[2 * m], c = ph[2 * m + 1];
-        A[base + 2 * m] += va * s;
-        A[base + 2 * m + 1] += va * c;
-        B[base + 2 * m] += vb * s;
-        B[base + 2 * m + 1] += vb * c;
-    }
-}
-// One face cell's running-DFT terms (the separate DFT kernel's form): A += va (sin, cos), B += vb (sin, cos)
-// per frequency.  The (sin, cos) pairs of the sums and of the phase table are
-// adjacent and 16-byte aligned (base and the phase row start are even), so
-// each pair moves as one double2.
-
 // Everything a marching CTA keeps between planes.
 struct MarchCtx {
     unsigned char *smem;
@@ -1155,7 +1138,7 @@ __device__ __forceinline__ void j_advance(const Args &a, const float *m, float c
 
 // How a CTA marches its planes (template parameter of march and run_item):
 //   MARCH_GENERAL: per tile and plane, the fast path where it applies, else
-//     the general path (CPML, domain edges, TF/SF, DFT, slices as Args says);
+//     the general path (CPML, domain edges, TF/SF, slices as Args says);
 //   MARCH_FAST: a clean tile whose every plane is an interior one (oblique
 //     TF/SF corrections after the pass, no record step, the CPML slabs and
 //     domain edges left to other work): the warm-up plane also takes the fast
@@ -1185,8 +1168,6 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
     if (JM == 2 && a.lk_mode == LK_PER_K && valid)
         for (int q = 0; q < 18; q++) lkm[q] = a.lk[(size_t)k * 18 + q];
     const float Gk = valid ? a.G[k] : 0.f, G2k = valid ? a.G2[k] : 0.f;
-    const int nf = a.nntf;
-    const double *ph = a.phase + (size_t)t * nf * 2;
     const size_t col = (size_t)(valid ? j : 0) * a.Nzp + (valid ? k : 0);
 
     // The plasma weight (and collision frequency) of the thread's cell is
@@ -1287,14 +1268,13 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
 
         // Interior fast path: a clean tile on a plane outside the x CPML slabs
         // and away from every x-special plane (TF/SF faces when the tile is in
-        // the box and the corrections are made here, NTF faces when the DFT
-        // is accumulated here, the x slice on record steps).  No conditionals
-        // per cell; the arithmetic is the same as the general path's.
+        // the box and the corrections are made here, the x slice on record
+        // steps).  No conditionals per cell; the arithmetic is the same as the
+        // general path's.
         const int xlo = a.band ? 0 : a.dopml ? L + 1 : 1, xhi = a.band ? Nx - 1 : a.dopml ? Nx - L - 2 : Nx - 2;
         const bool x_tfsf = (!a.oblique || a.obl_inline) && tf_in &&
                             (i == a.bx1 - 1 || i == a.bx1 || i == a.bx2 - 1);
-        const bool x_ntf = a.ntf_inline && (i == a.ntfb || i == Nx - a.ntfb);
-        const bool fast = FASTONLY || (!SLAB && CLEAN && real && i >= xlo && i <= xhi && !x_ntf &&
+        const bool fast = FASTONLY || (!SLAB && CLEAN && real && i >= xlo && i <= xhi &&
                                         !(record && i == a.ssx) && !x_tfsf);
         if (fast) {
             // With the band kernels a clean tile may reach past the grid
@@ -1455,35 +1435,6 @@ __device__ __forceinline__ int march(const Maps &maps, const Args &a, MarchCtx &
                 a.J[0][cg] = jx;
                 a.J[1][cg] = jy;
                 a.J[2][cg] = jz;
-            }
-
-            // ---- running DFT on the Huygens surface (FP64 sums)
-            const int nb = a.ntfb;
-            const bool fr = i == nb, bk = i == Nx - nb;
-            const bool tp = !CLEAN && j == Ny - nb, bt = !CLEAN && j == nb;
-            const bool lf = !CLEAN && k == nb, rt = !CLEAN && k == Nz - nb;
-            if (!SLAB && a.ntf_inline && (fr || bk || tp || bt || lf || rt)) {
-                const size_t n2 = 2 * (size_t)nf;
-                if (fr || bk) {
-                    const size_t base = ((size_t)j * Nz + k) * n2;
-                    const double hz = 0.5 * ((double)hv.z + hz_prev), hy = 0.5 * ((double)hv.y + hy_prev);
-                    if (fr) { acc2(a.ntf[2], a.ntf[3], base, hz, -hy, ph, nf); acc2(a.ntf[0], a.ntf[1], base, -(double)ez, ey, ph, nf); }
-                    if (bk) { acc2(a.ntf[6], a.ntf[7], base, -hz, hy, ph, nf); acc2(a.ntf[4], a.ntf[5], base, ez, -(double)ey, ph, nf); }
-                }
-                if (!CLEAN && (tp || bt)) {
-                    const size_t base = ((size_t)i * Nz + k) * n2;
-                    const double hz = 0.5 * ((double)hv.z + HN(2, dj - 1, dk));
-                    const double hx = 0.5 * ((double)hv.x + HN(0, dj - 1, dk));
-                    if (tp) { acc2(a.ntf[10], a.ntf[11], base, hz, -hx, ph, nf); acc2(a.ntf[8], a.ntf[9], base, -(double)ez, ex, ph, nf); }
-                    if (bt) { acc2(a.ntf[14], a.ntf[15], base, -hz, hx, ph, nf); acc2(a.ntf[12], a.ntf[13], base, ez, -(double)ex, ph, nf); }
-                }
-                if (!CLEAN && (lf || rt)) {
-                    const size_t base = ((size_t)i * Ny + j) * n2;
-                    const double hy = 0.5 * ((double)hv.y + HN(1, dj, dk - 1));
-                    const double hx = 0.5 * ((double)hv.x + HN(0, dj, dk - 1));
-                    if (lf) { acc2(a.ntf[18], a.ntf[19], base, hy, -hx, ph, nf); acc2(a.ntf[16], a.ntf[17], base, -(double)ey, ex, ph, nf); }
-                    if (rt) { acc2(a.ntf[22], a.ntf[23], base, -hy, hx, ph, nf); acc2(a.ntf[20], a.ntf[21], base, ey, -(double)ex, ph, nf); }
-                }
             }
 
             // ---- slices on record steps
@@ -2456,7 +2407,7 @@ __global__ void __launch_bounds__(256) k_batch_post(const int *__restrict__ job_
     const Args &a = c_jobs[q];
     const size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x, dq = (size_t)gridDim.x * blockDim.x;
     if (a.oblique && !a.obl_inline) tfsf_band_flat<PAR>(a, 0, q0, dq);
-    if (!a.ntf_inline && a.nntf > 0 && a.ntf_ring) ntf_stash(a, PAR ^ 1, a.ntf_ring, t % kNtfRing, q0, dq);
+    if (a.nntf > 0 && a.ntf_ring) ntf_stash(a, PAR ^ 1, a.ntf_ring, t % kNtfRing, q0, dq);
 }
 // After k_batch_post: a member whose tick filled its DFT ring (step t with
 // t % kNtfRing the last slot) or reached its last step adds the ring's steps
@@ -2466,7 +2417,7 @@ __global__ void __launch_bounds__(256) k_batch_flush(const int *__restrict__ job
     const int t = job_t[q], end = job_end[q];
     if (t >= end) return;
     const Args &a = c_jobs[q];
-    if (a.ntf_inline || a.nntf <= 0 || !a.ntf_ring) return;
+    if (a.nntf <= 0 || !a.ntf_ring) return;
     const int u = t % kNtfRing;
     if (u != kNtfRing - 1 && t + 1 != end) return;
     ntf_flush_cells(a, a.ntf_ring, a.phase4, t - u, u + 1, (size_t)blockIdx.x * blockDim.x + threadIdx.x,
@@ -2978,7 +2929,6 @@ void Fp32Sim::init(const Problem &P, void *stream) {
     // A single simulation runs the DFT and (without a plate or sphere, whose
     // per-cell coefficients the follow-up pass does not carry) the oblique
     // TF/SF corrections as kernels of their own after each pass.
-    a.ntf_inline = 0;
     a.obl_inline = (P.oblique && P.doplate != 0) ? 1 : 0;
     // The CPML slabs and domain edges are recomputed by the band kernels
     // after each pass, where the grid has an interior on every axis.
@@ -3107,7 +3057,6 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         std::vector<float> src(P.src.begin(), P.src.end());
         a.src = m.upload(src, s);
     }
-    a.phase = m.upload(P.phase, s);
     if (P.nntf() > 0) {
         m.nface = 2 * ((size_t)P.Ny * P.Nz + (size_t)P.Nx * P.Nz + (size_t)P.Nx * P.Ny);
         const int nb = P.ntfb;
@@ -3210,7 +3159,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
                          jlo >= 1 && jhi <= P.Ny - 2 && klo >= 1 && khi <= P.Nz - 2;
                 const int sy[6] = {P.by1 - 1, P.by1, P.by2 - 1, P.by2, P.ntfb, P.Ny - P.ntfb};
                 const int sz[6] = {P.bz1 - 1, P.bz1, P.bz2 - 1, P.bz2, P.ntfb, P.Nz - P.ntfb};
-                const int q0 = (a.oblique && !a.obl_inline) ? 4 : 0, q1 = a.ntf_inline ? 6 : 4;
+                const int q0 = (a.oblique && !a.obl_inline) ? 4 : 0, q1 = 4;
                 for (int q = q0; q < q1; q++) cl = cl && !hits(jlo, jhi, sy[q]) && !hits(klo, khi, sz[q]);
                 (cl ? later : order).push_back(ty * ntk + tk);
             }
@@ -3218,7 +3167,7 @@ void Fp32Sim::init(const Problem &P, void *stream) {
         // Every tile clean and every plane interior on non-record steps: the
         // fast pass applies (k_fp32_step_fast; not with the per-k or per-cell
         // Lee-Kalluri table, whose 18 coefficients do not fit its registers).
-        m.fast_ok = a.band && a.oblique && !a.obl_inline && !a.ntf_inline && P.doplate == 0 && m.jm != 2 &&
+        m.fast_ok = a.band && a.oblique && !a.obl_inline && P.doplate == 0 && m.jm != 2 &&
                     m.n_boundary == 0;
         order.insert(order.end(), later.begin(), later.end());
         m.tile_order = order;
@@ -3455,7 +3404,7 @@ int Fp32Sim::step(int t, bool record, void *stream, void *const *ev) {
     // corrections do not touch (the faces lie outside the band): with the
     // second stream it runs beside them, and the step ends when both have.
     const bool tfsf = m.a.oblique && !m.a.obl_inline;
-    const bool dft = !m.a.ntf_inline && m.a.nntf > 0;
+    const bool dft = m.a.nntf > 0;
     const bool dft_beside = dft && tfsf && m.aux && m.ntf_outside_band;
     if (dft) {
         if (!m.ntf_ring) {
@@ -3751,7 +3700,7 @@ int Fp32Batch::add(Fp32Sim *sim, int t0) {
     // The state is all zeros in both sets, so the simulation can take the
     // parity of the current tick.
     sim->m_cur_ = (int)(b.tick & 1);
-    if (!m.a.ntf_inline && m.a.nntf > 0 && !m.ntf_ring) {  // the running-DFT ring (k_batch_post)
+    if (m.a.nntf > 0 && !m.ntf_ring) {  // the running-DFT ring (k_batch_post)
         try {
             m.ntf_ring = m.alloc<float>((size_t)kNtfRing * 6 * m.nface, b.stream);
         } catch (...) {
